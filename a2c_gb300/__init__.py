@@ -1,0 +1,239 @@
+"""a2c_gb300: GB300-native (sm_103a) GPP-EAM evaluator for a2c's diffusive
+molecular dynamics hot path.
+
+The product is the CUDA library behind the C ABI in include/a2c_gpp.h.
+This module is a thin Python view of that ABI (for tests, benchmarks and
+scripting); the reference-facing C++ host API is include/a2c_host.hpp.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+from ._native import A2CError, A2C_FP64, A2C_MIXED  # noqa: F401
+
+__all__ = ["Gpp", "lattice_fcc", "A2CError", "A2C_FP64", "A2C_MIXED", "LbfgsResult"]
+
+
+@dataclass
+class LbfgsResult:
+    X: np.ndarray
+    fmin: float
+    iters: int
+    nfev: int
+    gnorm: float
+    reason: int
+
+
+def _f64(a, n=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def _i32(a, n=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+class Gpp:
+    """One evaluator context (Minimizer + AppCtx of the reference)."""
+
+    def __init__(self, nPd: int, nH: int, *, T: float = 300.0, QWp: float = 1.0 / 12.0, eps: float = 1e-5,
+                 rc: float = 5.35, a_Pd: float = 3.89, box=(0.0, 0.0, 0.0), periodic=(0, 0, 0),
+                 coe_Pd=(0.0, 0.0, 0.0, 0.0), coe_H=(0.0, 0.0, 0.0, 0.0), precision: int | str = A2C_FP64,
+                 device: int = 0):
+        L = N.lib()
+        p = N.GppParams()
+        L.a2c_gpp_default_params(C.byref(p))
+        p.nPd, p.nH = int(nPd), int(nH)
+        p.T, p.QWp, p.eps, p.rc, p.a_Pd = T, QWp, eps, rc, a_Pd
+        for d in range(3):
+            p.box[d] = float(box[d])
+            p.periodic[d] = int(bool(periodic[d]))
+        for k in range(4):
+            p.coe_Pd[k] = float(coe_Pd[k])
+            p.coe_H[k] = float(coe_H[k])
+        if isinstance(precision, str):
+            precision = {"fp64": A2C_FP64, "mixed": A2C_MIXED}[precision]
+        p.precision = int(precision)
+        p.device = int(device)
+        self.params = p
+        self.nPd, self.nH = int(nPd), int(nH)
+        self.N = self.nPd + self.nH
+        h = C.c_void_p()
+        N.check(L.a2c_gpp_create(C.byref(p), C.byref(h)), "a2c_gpp_create")
+        self._h = h
+        self._L = L
+
+    # -- lifecycle -----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.a2c_gpp_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return int(self._L.a2c_gpp_stream(self._h) or 0)
+
+    def set_precision(self, precision: int | str) -> None:
+        if isinstance(precision, str):
+            precision = {"fp64": A2C_FP64, "mixed": A2C_MIXED}[precision]
+        N.check(self._L.a2c_gpp_set_precision(self._h, int(precision)), "a2c_gpp_set_precision")
+
+    # -- state ---------------------------------------------------------------
+    def set_occupancy(self, xH) -> None:
+        x = _f64(xH, self.nH)
+        N.check(self._L.a2c_gpp_set_occupancy(self._h, N.ptr(x)), "a2c_gpp_set_occupancy")
+
+    def occupancy(self) -> np.ndarray:
+        x = np.empty(self.nH)
+        N.check(self._L.a2c_gpp_get_occupancy(self._h, N.ptr(x)), "a2c_gpp_get_occupancy")
+        return x
+
+    def set_state(self, X) -> None:
+        X = _f64(X, 4 * self.N)
+        N.check(self._L.a2c_gpp_set_state(self._h, N.ptr(X)), "a2c_gpp_set_state")
+
+    def state(self) -> np.ndarray:
+        X = np.empty(4 * self.N)
+        N.check(self._L.a2c_gpp_get_state(self._h, N.ptr(X)), "a2c_gpp_get_state")
+        return X
+
+    # -- neighbors -----------------------------------------------------------
+    def build_neighbors(self, X) -> int:
+        X = _f64(X, 4 * self.N)
+        m = C.c_int(0)
+        N.check(self._L.a2c_gpp_build_neighbors(self._h, N.ptr(X), C.byref(m)), "a2c_gpp_build_neighbors")
+        return m.value
+
+    def neighbors(self, list_id: int) -> tuple[np.ndarray, np.ndarray]:
+        tot = C.c_int64(0)
+        N.check(self._L.a2c_gpp_neighbor_total(self._h, list_id, C.byref(tot)), "a2c_gpp_neighbor_total")
+        nsite = self.nPd if list_id in (N.LIST_PDPD, N.LIST_PDH) else self.nH
+        off = np.zeros(nsite + 1, dtype=np.int64)
+        idx = np.zeros(max(tot.value, 1), dtype=np.int32)
+        N.check(self._L.a2c_gpp_get_neighbors(self._h, list_id, N.ptr(off), N.ptr(idx)), "a2c_gpp_get_neighbors")
+        return off, idx[: tot.value]
+
+    def shell_counts(self) -> np.ndarray:
+        s = np.zeros(3 * max(self.nPd, 1), dtype=np.int32)
+        N.check(self._L.a2c_gpp_get_shell_counts(self._h, N.ptr(s)), "a2c_gpp_get_shell_counts")
+        return s[: 3 * self.nPd].reshape(self.nPd, 3)
+
+    # -- evaluation ----------------------------------------------------------
+    def eval(self, X) -> tuple[float, np.ndarray]:
+        X = _f64(X, 4 * self.N)
+        G = np.empty(4 * self.N)
+        f = C.c_double(0.0)
+        N.check(self._L.a2c_gpp_eval(self._h, N.ptr(X), C.byref(f), N.ptr(G)), "a2c_gpp_eval")
+        return f.value, G
+
+    def eval_device(self, dX: int, df: int, dG: int) -> None:
+        """Stream-ordered evaluation on device pointers (ints)."""
+        N.check(self._L.a2c_gpp_eval_device(self._h, C.c_void_p(dX), C.c_void_p(df), C.c_void_p(dG)),
+                "a2c_gpp_eval_device")
+
+    def density(self) -> np.ndarray:
+        r = np.empty(self.N)
+        N.check(self._L.a2c_gpp_get_density(self._h, N.ptr(r)), "a2c_gpp_get_density")
+        return r
+
+    def bounds(self) -> tuple[np.ndarray, np.ndarray]:
+        lb, ub = np.empty(4 * self.N), np.empty(4 * self.N)
+        N.check(self._L.a2c_gpp_bounds(self._h, N.ptr(lb), N.ptr(ub)), "a2c_gpp_bounds")
+        return lb, ub
+
+    def minimize(self, X, **kw) -> LbfgsResult:
+        lp = N.LbfgsParams()
+        self._L.a2c_lbfgs_default_params(C.byref(lp))
+        for k, v in kw.items():
+            setattr(lp, k, v)
+        X = _f64(X, 4 * self.N).copy()
+        f, it, nfev, gn, why = C.c_double(), C.c_int(), C.c_int(), C.c_double(), C.c_int()
+        N.check(self._L.a2c_gpp_minimize(self._h, N.ptr(X), C.byref(lp), C.byref(f), C.byref(it), C.byref(nfev),
+                                         C.byref(gn), C.byref(why)), "a2c_gpp_minimize")
+        return LbfgsResult(X, f.value, it.value, nfev.value, gn.value, why.value)
+
+    # -- occupancy dynamics --------------------------------------------------
+    def chem_potential(self, gamma_bd: float, gamma, full_H) -> tuple[np.ndarray, np.ndarray]:
+        g = _f64(gamma, self.nH).copy()
+        fh = _i32(full_H, self.nH).copy()
+        N.check(self._L.a2c_gpp_chem_potential(self._h, float(gamma_bd), N.ptr(g), N.ptr(fh)),
+                "a2c_gpp_chem_potential")
+        return g, fh
+
+    def apply_dirichlet(self, sites, gamma_bd: float, xUb: float, gamma, full_H) -> tuple[np.ndarray, np.ndarray]:
+        s = _i32(sites)
+        g = _f64(gamma, self.nH).copy()
+        fh = _i32(full_H, self.nH).copy()
+        N.check(self._L.a2c_gpp_apply_dirichlet(self._h, N.ptr(s), int(s.size), float(gamma_bd), float(xUb),
+                                                N.ptr(g), N.ptr(fh)), "a2c_gpp_apply_dirichlet")
+        return g, fh
+
+    def diffuse(self, dt, nu, Qm, xLb, xUb, gamma, full_H, x) -> np.ndarray:
+        g = _f64(gamma, self.nH)
+        fh = _i32(full_H, self.nH)
+        xo = _f64(x, self.nH).copy()
+        N.check(self._L.a2c_gpp_diffuse(self._h, dt, nu, Qm, xLb, xUb, N.ptr(g), N.ptr(fh), N.ptr(xo)),
+                "a2c_gpp_diffuse")
+        return xo
+
+    def macro_results(self, x, HSurf) -> tuple[float, float]:
+        x = _f64(x, self.nH)
+        hs = _i32(HSurf)
+        a, b = C.c_double(), C.c_double()
+        N.check(self._L.a2c_gpp_macro_results(self._h, N.ptr(x), N.ptr(hs) if hs.size else None, int(hs.size),
+                                              C.byref(a), C.byref(b)), "a2c_gpp_macro_results")
+        return a.value, b.value
+
+
+def lattice_fcc(ncell, *, a: float = 3.89, periodic=(1, 1, 1), pos_std: float = 0.0, sigma=(0.1, 0.1),
+                x_mode: int = 0, x_center: float = 0.05, x_half: float = 0.0, x_matrix: float = 0.02,
+                x_nucleus: float = 0.6, nucleus_radius: float = 80.0, interface_width: float = 5.0,
+                xLb: float = 1e-3, xUb: float = 1.0 - 1e-16, seed: int = 1):
+    """Seeded fcc Pd + octahedral H lattice (a2c_lattice_fcc).
+
+    Returns (X, xH, surface, box, nPd, nH)."""
+    if isinstance(ncell, int):
+        ncell = (ncell, ncell, ncell)
+    sp = N.LatticeSpec()
+    for d in range(3):
+        sp.ncell[d] = int(ncell[d])
+        sp.periodic[d] = int(bool(periodic[d]))
+    sp.a, sp.pos_std = a, pos_std
+    sp.sigma_lo, sp.sigma_hi = float(sigma[0]), float(sigma[1])
+    sp.x_mode, sp.x_center, sp.x_half = x_mode, x_center, x_half
+    sp.x_matrix, sp.x_nucleus, sp.nucleus_radius, sp.interface_width = x_matrix, x_nucleus, nucleus_radius, \
+        interface_width
+    sp.xLb, sp.xUb, sp.seed = xLb, xUb, seed
+    nc = int(ncell[0]) * int(ncell[1]) * int(ncell[2])
+    nPd = nH = 4 * nc
+    X = np.empty(4 * (nPd + nH))
+    xH = np.empty(nH)
+    surf = np.empty(nH, dtype=np.int32)
+    N.check(N.lib().a2c_lattice_fcc(C.byref(sp), N.ptr(X), N.ptr(xH), N.ptr(surf)), "a2c_lattice_fcc")
+    box = tuple(float(ncell[d]) * a for d in range(3))
+    return X, xH, surf, box, nPd, nH

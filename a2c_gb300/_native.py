@@ -1,0 +1,144 @@
+"""ctypes binding of liba2c_gpp.so (include/a2c_gpp.h).
+
+The library is the product: there is no Python or CPU fallback.  Loading
+fails loudly when the shared object has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "liba2c_gpp.so"
+
+A2C_OK = 0
+A2C_ERR_INVALID = 1
+A2C_ERR_CUDA = 2
+A2C_ERR_NOMEM = 3
+A2C_ERR_NEIGHBOR_OVERFLOW = 4
+A2C_ERR_NONFINITE = 5
+A2C_ERR_STATE = 6
+A2C_ERR_TIMEOUT = 7
+A2C_ERR_NO_DEVICE = 8
+
+A2C_FP64 = 0
+A2C_MIXED = 1
+
+LIST_PDPD, LIST_PDH, LIST_HPD, LIST_HH, LIST_HH1 = range(5)
+
+CONVERGED_GATOL = 3
+DIVERGED_MAXITS = -2
+DIVERGED_NAN = -4
+DIVERGED_MAXFCN = -5
+DIVERGED_LS_FAILURE = -6
+
+
+class GppParams(C.Structure):
+    _fields_ = [
+        ("nPd", C.c_int), ("nH", C.c_int),
+        ("T", C.c_double), ("QWp", C.c_double), ("eps", C.c_double), ("rc", C.c_double), ("a_Pd", C.c_double),
+        ("box", C.c_double * 3), ("periodic", C.c_int * 3),
+        ("coe_Pd", C.c_double * 4), ("coe_H", C.c_double * 4),
+        ("precision", C.c_int), ("device", C.c_int),
+    ]
+
+
+class LbfgsParams(C.Structure):
+    _fields_ = [
+        ("m", C.c_int), ("max_it", C.c_int), ("max_fev", C.c_int), ("max_ls", C.c_int),
+        ("gatol", C.c_double), ("c1", C.c_double), ("init_step", C.c_double), ("sigma_lb", C.c_double),
+    ]
+
+
+class LatticeSpec(C.Structure):
+    _fields_ = [
+        ("ncell", C.c_int * 3), ("a", C.c_double), ("periodic", C.c_int * 3),
+        ("pos_std", C.c_double), ("sigma_lo", C.c_double), ("sigma_hi", C.c_double),
+        ("x_mode", C.c_int), ("x_center", C.c_double), ("x_half", C.c_double),
+        ("x_matrix", C.c_double), ("x_nucleus", C.c_double), ("nucleus_radius", C.c_double),
+        ("interface_width", C.c_double), ("xLb", C.c_double), ("xUb", C.c_double),
+        ("seed", C.c_uint64),
+    ]
+
+
+_lib = None
+
+P = C.c_void_p
+D = C.c_double
+I = C.c_int
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the CUDA evaluator has no CPU fallback)")
+    L = C.CDLL(str(LIB_PATH))
+    sig = {
+        "a2c_gpp_default_params": (None, [C.POINTER(GppParams)]),
+        "a2c_lbfgs_default_params": (None, [C.POINTER(LbfgsParams)]),
+        "a2c_status_string": (C.c_char_p, [I]),
+        "a2c_gpp_create": (I, [C.POINTER(GppParams), C.POINTER(P)]),
+        "a2c_gpp_destroy": (I, [P]),
+        "a2c_gpp_stream": (P, [P]),
+        "a2c_gpp_set_precision": (I, [P, I]),
+        "a2c_gpp_set_occupancy": (I, [P, P]),
+        "a2c_gpp_get_occupancy": (I, [P, P]),
+        "a2c_gpp_set_state": (I, [P, P]),
+        "a2c_gpp_get_state": (I, [P, P]),
+        "a2c_gpp_build_neighbors": (I, [P, P, C.POINTER(I)]),
+        "a2c_gpp_neighbor_total": (I, [P, I, C.POINTER(C.c_int64)]),
+        "a2c_gpp_get_neighbors": (I, [P, I, P, P]),
+        "a2c_gpp_get_shell_counts": (I, [P, P]),
+        "a2c_gpp_eval": (I, [P, P, C.POINTER(D), P]),
+        "a2c_gpp_eval_device": (I, [P, P, P, P]),
+        "a2c_gpp_get_density": (I, [P, P]),
+        "a2c_gpp_bounds": (I, [P, P, P]),
+        "a2c_gpp_minimize": (I, [P, P, C.POINTER(LbfgsParams), C.POINTER(D), C.POINTER(I), C.POINTER(I),
+                                 C.POINTER(D), C.POINTER(I)]),
+        "a2c_gpp_chem_potential": (I, [P, D, P, P]),
+        "a2c_gpp_apply_dirichlet": (I, [P, P, I, D, D, P, P]),
+        "a2c_gpp_diffuse": (I, [P, D, D, D, D, D, P, P, P]),
+        "a2c_gpp_macro_results": (I, [P, P, P, I, C.POINTER(D), C.POINTER(D)]),
+        "a2c_lattice_fcc": (I, [C.POINTER(LatticeSpec), P, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def exported_symbols() -> list[str]:
+    """Names of the C ABI functions this binding expects the library to export."""
+    return ["a2c_gpp_default_params", "a2c_lbfgs_default_params", "a2c_status_string", "a2c_gpp_create",
+            "a2c_gpp_destroy", "a2c_gpp_stream", "a2c_gpp_set_precision", "a2c_gpp_set_occupancy",
+            "a2c_gpp_get_occupancy", "a2c_gpp_set_state", "a2c_gpp_get_state", "a2c_gpp_build_neighbors",
+            "a2c_gpp_neighbor_total", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
+            "a2c_gpp_eval_device", "a2c_gpp_get_density", "a2c_gpp_bounds", "a2c_gpp_minimize",
+            "a2c_gpp_chem_potential", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",
+            "a2c_lattice_fcc"]
+
+
+class A2CError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        msg = lib().a2c_status_string(status).decode()
+        super().__init__(f"{where}: status {status} ({msg})")
+        self.status = status
+
+
+def check(status: int, where: str) -> None:
+    if status != A2C_OK:
+        raise A2CError(status, where)
+
+
+def ptr(a: np.ndarray | None) -> int | None:
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "arrays crossing the C ABI must be contiguous"
+    return a.ctypes.data

@@ -1,0 +1,507 @@
+// The C ABI (include/a2c_gpp.h): context lifecycle, host<->device staging,
+// validation and the order of kernel launches.  No function here aborts,
+// traps or lets a C++ exception cross the boundary; every failure returns
+// an a2c_status.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace a2c {
+
+a2c_status cuda_status(cudaError_t e) {
+  switch (e) {
+    case cudaSuccess: return A2C_OK;
+    case cudaErrorMemoryAllocation: return A2C_ERR_NOMEM;
+    case cudaErrorNoDevice:
+    case cudaErrorInsufficientDriver:
+    case cudaErrorInvalidDevice: return A2C_ERR_NO_DEVICE;
+    default: return A2C_ERR_CUDA;
+  }
+}
+
+a2c_status eval_device_impl(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG) {
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  if (c->p.precision == A2C_MIXED) {
+    A2C_TRY(mixed_eval(c, dX, d_f, dG));
+  } else {
+    A2C_TRY(launch_density64(c, dX));
+    A2C_TRY(launch_gradient64(c, dX, dG));
+    A2C_TRY(reduce_objective(c, d_f));
+  }
+  c->has_density = (c->p.precision != A2C_MIXED);
+  return A2C_OK;
+}
+
+}  // namespace a2c
+
+using namespace a2c;
+
+namespace {
+
+bool valid_params(const a2c_gpp_params *p) {
+  if (!p) return false;
+  if (p->nPd < 0 || p->nH < 0) return false;
+  if ((int64_t)p->nPd + p->nH >= (int64_t(1) << kIdBits)) return false;
+  if (!(p->T > 0.0) || !(p->eps > 0.0) || !(p->rc > 0.0) || !std::isfinite(p->QWp)) return false;
+  if (!std::isfinite(p->a_Pd)) return false;
+  for (int d = 0; d < 3; ++d)
+    if (p->periodic[d] && !(p->box[d] > 2.0 * p->rc)) return false;
+  if (p->precision != A2C_FP64 && p->precision != A2C_MIXED) return false;
+  return true;
+}
+
+struct DeviceGuard {
+  explicit DeviceGuard(int d) { cudaSetDevice(d); }
+};
+
+a2c_status copy_in(a2c_gpp_ctx *c, double *dst, const double *src, int64_t n) {
+  if (n <= 0) return A2C_OK;
+  A2C_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  return A2C_OK;
+}
+
+a2c_status finish(a2c_gpp_ctx *c) {
+  A2C_CUDA(cudaStreamSynchronize(c->stream));
+  return check_status_word(c);
+}
+
+template <class T>
+a2c_status dalloc(T **p, int64_t n) {
+  if (cudaMalloc((void **)p, sizeof(T) * (size_t)std::max<int64_t>(n, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
+  return A2C_OK;
+}
+
+// per-call scratch on H sites (stream-ordered allocations)
+a2c_status ensure_hscratch(a2c_gpp_ctx *c, double **gamma, double **send, double **x, int **full) {
+  const int64_t nH = std::max(c->p.nH, 1);
+  A2C_CUDA(cudaMallocAsync((void **)gamma, sizeof(double) * nH, c->stream));
+  A2C_CUDA(cudaMallocAsync((void **)send, sizeof(double) * nH, c->stream));
+  A2C_CUDA(cudaMallocAsync((void **)x, sizeof(double) * nH, c->stream));
+  A2C_CUDA(cudaMallocAsync((void **)full, sizeof(int) * nH, c->stream));
+  return A2C_OK;
+}
+
+void free_hscratch(a2c_gpp_ctx *c, double *gamma, double *send, double *x, int *full) {
+  cudaFreeAsync(gamma, c->stream);
+  cudaFreeAsync(send, c->stream);
+  cudaFreeAsync(x, c->stream);
+  cudaFreeAsync(full, c->stream);
+}
+
+__global__ void k_fill(double *p, int64_t n, double v) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+}  // namespace
+
+extern "C" {
+
+void a2c_gpp_default_params(a2c_gpp_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->T = 300.0;           // DiffusionData::T0 default (IoData.cpp:626)
+  p->QWp = 1.0 / 12.0;    // 0.5/dim for dim = 6 (quadrature.cpp:96-97)
+  p->eps = 1.0e-5;        // InteratomicPotentialData::eps (IoData.cpp:517)
+  p->rc = 5.35;           // InteratomicPotentialData::rc (IoData.cpp:518)
+  p->a_Pd = 3.89;
+  p->precision = A2C_FP64;
+  p->device = 0;
+}
+
+void a2c_lbfgs_default_params(a2c_lbfgs_params *p) {
+  if (!p) return;
+  p->m = 5;
+  p->max_it = 10000;
+  p->max_fev = 20000;
+  p->max_ls = 30;
+  p->gatol = 1.0e-6;
+  p->c1 = 1.0e-4;
+  p->init_step = 1.0e-2;
+  p->sigma_lb = 1.0e-6;
+}
+
+const char *a2c_status_string(a2c_status s) {
+  switch (s) {
+    case A2C_OK: return "ok";
+    case A2C_ERR_INVALID: return "invalid argument";
+    case A2C_ERR_CUDA: return "CUDA runtime error";
+    case A2C_ERR_NOMEM: return "device allocation failed";
+    case A2C_ERR_NEIGHBOR_OVERFLOW: return "neighbor capacity exceeded (more than 1000 neighbors at a site)";
+    case A2C_ERR_NONFINITE: return "non-finite value in an input or result";
+    case A2C_ERR_STATE: return "call order violated (build neighbors / set state first)";
+    case A2C_ERR_TIMEOUT: return "bounded device wait gave up";
+    case A2C_ERR_NO_DEVICE: return "no usable CUDA device";
+    default: return "unknown status";
+  }
+}
+
+a2c_status a2c_gpp_create(const a2c_gpp_params *p, a2c_gpp_ctx **out) {
+  if (!out) return A2C_ERR_INVALID;
+  *out = nullptr;
+  if (!valid_params(p)) return A2C_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return A2C_ERR_NO_DEVICE;
+  if (p->device < 0 || p->device >= ndev) return A2C_ERR_NO_DEVICE;
+  A2C_CUDA(cudaSetDevice(p->device));
+  a2c_gpp_ctx *c = new (std::nothrow) a2c_gpp_ctx();
+  if (!c) return A2C_ERR_NOMEM;
+  c->p = *p;
+  c->device = p->device;
+  c->N = (int64_t)p->nPd + p->nH;
+  const int64_t N = c->N;
+  a2c_status s = A2C_OK;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) s = A2C_ERR_CUDA;
+  if (!s) s = dalloc(&c->d_X, 4 * N);
+  if (!s) s = dalloc(&c->d_G, 4 * N);
+  if (!s) s = dalloc(&c->d_occ, N);
+  if (!s) s = dalloc(&c->d_rho, N);
+  if (!s) s = dalloc(&c->d_Fp, N);
+  if (!s) s = dalloc(&c->d_Vs, N);
+  if (!s) s = dalloc(&c->d_Ss, N);
+  if (!s) s = dalloc(&c->d_red, 2 * 1024 + 64);
+  if (!s) s = dalloc(&c->d_status, 1);
+  if (!s) s = dalloc(&c->d_off, N + 1);
+  if (!s) s = dalloc(&c->d_npd, N);
+  if (!s) s = dalloc(&c->d_shell, 3 * (int64_t)p->nPd);
+  if (!s) s = dalloc(&c->d_hh1_off, (int64_t)p->nH + 1);
+  if (!s) {
+    if (N > 0) {
+      k_fill<<<grid_for(N, 256), 256, 0, c->stream>>>(c->d_occ, N, 0.0);
+      if (p->nPd > 0) k_fill<<<grid_for(p->nPd, 256), 256, 0, c->stream>>>(c->d_occ, p->nPd, 1.0);
+    }
+    if (cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream) != cudaSuccess) s = A2C_ERR_CUDA;
+    if (cudaMemsetAsync(c->d_X, 0, sizeof(double) * std::max<int64_t>(4 * N, 1), c->stream) != cudaSuccess)
+      s = A2C_ERR_CUDA;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) s = A2C_ERR_CUDA;
+  }
+  if (s) {
+    a2c_gpp_destroy(c);
+    return s;
+  }
+  *out = c;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_destroy(a2c_gpp_ctx *c) {
+  if (!c) return A2C_OK;
+  DeviceGuard g(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  mixed_free(c);
+  lbfgs_free(c);
+  for (void *p : {(void *)c->d_X, (void *)c->d_G, (void *)c->d_occ, (void *)c->d_rho, (void *)c->d_Fp,
+                  (void *)c->d_Vs, (void *)c->d_Ss, (void *)c->d_red, (void *)c->d_status, (void *)c->d_off,
+                  (void *)c->d_nbr, (void *)c->d_npd, (void *)c->d_shell, (void *)c->d_hh1_off, (void *)c->d_hh1})
+    if (p) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return A2C_OK;
+}
+
+void *a2c_gpp_stream(a2c_gpp_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+a2c_status a2c_gpp_set_precision(a2c_gpp_ctx *c, int precision) {
+  if (!c || (precision != A2C_FP64 && precision != A2C_MIXED)) return A2C_ERR_INVALID;
+  c->p.precision = precision;
+  c->has_density = false;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_set_occupancy(a2c_gpp_ctx *c, const double *xH) {
+  if (!c || (!xH && c->p.nH > 0)) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  for (int i = 0; i < c->p.nH; ++i)
+    if (!std::isfinite(xH[i])) return A2C_ERR_NONFINITE;
+  A2C_TRY(copy_in(c, c->d_occ + c->p.nPd, xH, c->p.nH));
+  c->has_density = false;
+  return finish(c);
+}
+
+a2c_status a2c_gpp_get_occupancy(a2c_gpp_ctx *c, double *xH) {
+  if (!c || (!xH && c->p.nH > 0)) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  if (c->p.nH > 0)
+    A2C_CUDA(cudaMemcpyAsync(xH, c->d_occ + c->p.nPd, sizeof(double) * c->p.nH, cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+a2c_status a2c_gpp_set_state(a2c_gpp_ctx *c, const double *X) {
+  if (!c || (!X && c->N > 0)) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  A2C_TRY(copy_in(c, c->d_X, X, 4 * c->N));
+  c->has_state = true;
+  c->has_density = false;
+  return finish(c);
+}
+
+a2c_status a2c_gpp_get_state(a2c_gpp_ctx *c, double *X) {
+  if (!c || (!X && c->N > 0)) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  if (c->N > 0) A2C_CUDA(cudaMemcpyAsync(X, c->d_X, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+a2c_status a2c_gpp_build_neighbors(a2c_gpp_ctx *c, const double *X, int *max_neighbors) {
+  if (!c || (!X && c->N > 0)) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  for (int64_t t = 0; t < 4 * c->N; ++t)
+    if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
+  for (int d = 0; d < 3; ++d)  // images are limited to one box length either way
+    if (c->p.periodic[d])
+      for (int64_t s = 0; s < c->N; ++s)
+        if (X[4 * s + d] < -0.5 * c->p.box[d] || X[4 * s + d] > 1.5 * c->p.box[d]) return A2C_ERR_INVALID;
+  A2C_TRY(copy_in(c, c->d_X, X, 4 * c->N));
+  c->has_state = true;
+  c->has_neighbors = false;
+  c->has_density = false;
+  A2C_TRY(build_neighbors_device(c, X));
+  c->has_neighbors = true;
+  if (max_neighbors) *max_neighbors = c->max_neighbors;
+  return finish(c);
+}
+
+namespace {
+// host copies of off / npd for list export
+a2c_status host_lists(a2c_gpp_ctx *c, std::vector<int64_t> &off, std::vector<int> &npd) {
+  off.resize(c->N + 1);
+  npd.resize(std::max<int64_t>(c->N, 1));
+  A2C_CUDA(cudaMemcpyAsync(off.data(), c->d_off, sizeof(int64_t) * (c->N + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (c->N > 0)
+    A2C_CUDA(cudaMemcpyAsync(npd.data(), c->d_npd, sizeof(int) * c->N, cudaMemcpyDeviceToHost, c->stream));
+  A2C_CUDA(cudaStreamSynchronize(c->stream));
+  return A2C_OK;
+}
+}  // namespace
+
+a2c_status a2c_gpp_neighbor_total(a2c_gpp_ctx *c, int list, int64_t *total) {
+  if (!c || !total || list < 0 || list > 4) return A2C_ERR_INVALID;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  if (list == A2C_LIST_HH1) {
+    *total = c->hh1_total;
+    return A2C_OK;
+  }
+  std::vector<int64_t> off;
+  std::vector<int> npd;
+  A2C_TRY(host_lists(c, off, npd));
+  const bool pdsite = (list == A2C_LIST_PDPD || list == A2C_LIST_PDH);
+  const bool pdnbr = (list == A2C_LIST_PDPD || list == A2C_LIST_HPD);
+  const int64_t lo = pdsite ? 0 : c->p.nPd, hi = pdsite ? c->p.nPd : c->N;
+  int64_t t = 0;
+  for (int64_t s = lo; s < hi; ++s) t += pdnbr ? npd[s] : (off[s + 1] - off[s] - npd[s]);
+  *total = t;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_get_neighbors(a2c_gpp_ctx *c, int list, int64_t *offsets, int *idx) {
+  if (!c || !offsets || list < 0 || list > 4) return A2C_ERR_INVALID;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  const int nPd = c->p.nPd, nH = c->p.nH;
+  if (list == A2C_LIST_HH1) {
+    A2C_CUDA(cudaMemcpyAsync(offsets, c->d_hh1_off, sizeof(int64_t) * (nH + 1), cudaMemcpyDeviceToHost, c->stream));
+    if (c->hh1_total > 0)
+      A2C_CUDA(cudaMemcpyAsync(idx, c->d_hh1, sizeof(int) * c->hh1_total, cudaMemcpyDeviceToHost, c->stream));
+    A2C_CUDA(cudaStreamSynchronize(c->stream));
+    return A2C_OK;
+  }
+  std::vector<int64_t> off;
+  std::vector<int> npd;
+  A2C_TRY(host_lists(c, off, npd));
+  std::vector<uint32_t> nbr((size_t)std::max<int64_t>(c->nbr_total, 1));
+  if (c->nbr_total > 0)
+    A2C_CUDA(cudaMemcpy(nbr.data(), c->d_nbr, sizeof(uint32_t) * c->nbr_total, cudaMemcpyDeviceToHost));
+  const bool pdsite = (list == A2C_LIST_PDPD || list == A2C_LIST_PDH);
+  const bool pdnbr = (list == A2C_LIST_PDPD || list == A2C_LIST_HPD);
+  const int64_t lo = pdsite ? 0 : nPd, hi = pdsite ? nPd : c->N;
+  int64_t w = 0;
+  offsets[0] = 0;
+  for (int64_t s = lo; s < hi; ++s) {
+    const int64_t b = pdnbr ? off[s] : off[s] + npd[s];
+    const int64_t e = pdnbr ? off[s] + npd[s] : off[s + 1];
+    for (int64_t t = b; t < e; ++t) {
+      const int64_t j = nbr[t] & kIdMask;
+      idx[w++] = (int)(pdnbr ? j : j - nPd);
+    }
+    offsets[s - lo + 1] = w;
+  }
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_get_shell_counts(a2c_gpp_ctx *c, int *PdPdnum) {
+  if (!c || (!PdPdnum && c->p.nPd > 0)) return A2C_ERR_INVALID;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  if (c->p.nPd > 0)
+    A2C_CUDA(cudaMemcpyAsync(PdPdnum, c->d_shell, sizeof(int) * 3 * c->p.nPd, cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *c, const double *dX, double *df, double *dG) {
+  if (!c || (!dX && c->N > 0) || !df || (!dG && c->N > 0)) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  A2C_TRY(eval_device_impl(c, dX, df, dG));
+  if (dX != c->d_X && c->N > 0)
+    A2C_CUDA(cudaMemcpyAsync(c->d_X, dX, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToDevice, c->stream));
+  c->has_state = true;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_eval(a2c_gpp_ctx *c, const double *X, double *f, double *G) {
+  if (!c || (!X && c->N > 0) || !f || (!G && c->N > 0)) return A2C_ERR_INVALID;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  A2C_TRY(copy_in(c, c->d_X, X, 4 * c->N));
+  c->has_state = true;
+  double *d_f = c->d_red + 2 * 1024 + 8;
+  A2C_TRY(launch_finite_check(c, c->d_X, 4 * c->N));
+  A2C_TRY(eval_device_impl(c, c->d_X, d_f, c->d_G));
+  A2C_CUDA(cudaMemcpyAsync(f, d_f, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (c->N > 0) A2C_CUDA(cudaMemcpyAsync(G, c->d_G, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+a2c_status a2c_gpp_get_density(a2c_gpp_ctx *c, double *rho) {
+  if (!c || (!rho && c->N > 0)) return A2C_ERR_INVALID;
+  if (!c->has_density) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  if (c->N > 0) A2C_CUDA(cudaMemcpyAsync(rho, c->d_rho, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+a2c_status a2c_gpp_bounds(a2c_gpp_ctx *c, double *lb, double *ub) {
+  if (!c || (!lb && c->N > 0) || (!ub && c->N > 0)) return A2C_ERR_INVALID;
+  for (int64_t s = 0; s < c->N; ++s) {
+    for (int d = 0; d < 3; ++d) {
+      lb[4 * s + d] = -HUGE_VAL;
+      ub[4 * s + d] = HUGE_VAL;
+    }
+    lb[4 * s + 3] = 1.0e-6;
+    ub[4 * s + 3] = HUGE_VAL;
+  }
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_minimize(a2c_gpp_ctx *c, double *X, const a2c_lbfgs_params *lp, double *fmin, int *iters,
+                            int *nfev, double *gnorm, int *reason) {
+  if (!c || (!X && c->N > 0) || !lp || !fmin || !iters || !nfev || !gnorm || !reason) return A2C_ERR_INVALID;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  for (int64_t t = 0; t < 4 * c->N; ++t)
+    if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
+  A2C_TRY(copy_in(c, c->d_X, X, 4 * c->N));
+  A2C_TRY(lbfgs_minimize(c, c->d_X, lp, fmin, iters, nfev, gnorm, reason));
+  c->has_state = true;
+  c->has_density = false;
+  if (c->N > 0) A2C_CUDA(cudaMemcpyAsync(X, c->d_X, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+a2c_status a2c_gpp_chem_potential(a2c_gpp_ctx *c, double gamma_bd, double *gamma, int *full_H) {
+  if (!c || ((!gamma || !full_H) && c->p.nH > 0)) return A2C_ERR_INVALID;
+  if (!c->has_neighbors || !c->has_state) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  const int nH = c->p.nH;
+  if (nH == 0) return A2C_OK;
+  double *dg, *dsend, *dx;
+  int *dfull;
+  A2C_TRY(ensure_hscratch(c, &dg, &dsend, &dx, &dfull));
+  a2c_status s = A2C_OK;
+  if (cudaMemcpyAsync(dg, gamma, sizeof(double) * nH, cudaMemcpyHostToDevice, c->stream) ||
+      cudaMemcpyAsync(dfull, full_H, sizeof(int) * nH, cudaMemcpyHostToDevice, c->stream))
+    s = A2C_ERR_CUDA;
+  // minimizer.cpp:607-633: densities at the current state, always FP64
+  if (!s) s = launch_density64(c, c->d_X);
+  if (!s) s = launch_chem64(c, c->d_X, gamma_bd, dsend, dfull);
+  if (!s) s = launch_gamma_update(c, dsend, gamma_bd, dg, dfull);
+  if (!s && (cudaMemcpyAsync(gamma, dg, sizeof(double) * nH, cudaMemcpyDeviceToHost, c->stream) ||
+             cudaMemcpyAsync(full_H, dfull, sizeof(int) * nH, cudaMemcpyDeviceToHost, c->stream)))
+    s = A2C_ERR_CUDA;
+  free_hscratch(c, dg, dsend, dx, dfull);
+  if (s) return s;
+  c->has_density = true;
+  return finish(c);
+}
+
+a2c_status a2c_gpp_apply_dirichlet(a2c_gpp_ctx *c, const int *sites, int n, double gamma_bd, double xUb,
+                                   double *gamma, int *full_H) {
+  if (!c || n < 0 || (n > 0 && (!sites || !gamma || !full_H))) return A2C_ERR_INVALID;
+  const int nH = c->p.nH;
+  for (int t = 0; t < n; ++t)
+    if (sites[t] < 0 || sites[t] >= nH) return A2C_ERR_INVALID;
+  if (n == 0) return A2C_OK;
+  DeviceGuard g(c->device);
+  int *dsites = nullptr;
+  double *dg = nullptr;
+  int *dfull = nullptr;
+  A2C_CUDA(cudaMallocAsync((void **)&dsites, sizeof(int) * n, c->stream));
+  A2C_CUDA(cudaMallocAsync((void **)&dg, sizeof(double) * nH, c->stream));
+  A2C_CUDA(cudaMallocAsync((void **)&dfull, sizeof(int) * nH, c->stream));
+  a2c_status s = A2C_OK;
+  if (cudaMemcpyAsync(dsites, sites, sizeof(int) * n, cudaMemcpyHostToDevice, c->stream) ||
+      cudaMemcpyAsync(dg, gamma, sizeof(double) * nH, cudaMemcpyHostToDevice, c->stream) ||
+      cudaMemcpyAsync(dfull, full_H, sizeof(int) * nH, cudaMemcpyHostToDevice, c->stream))
+    s = A2C_ERR_CUDA;
+  if (!s) s = launch_dirichlet(c, dsites, n, gamma_bd, xUb, dg, dfull);
+  if (!s && (cudaMemcpyAsync(gamma, dg, sizeof(double) * nH, cudaMemcpyDeviceToHost, c->stream) ||
+             cudaMemcpyAsync(full_H, dfull, sizeof(int) * nH, cudaMemcpyDeviceToHost, c->stream)))
+    s = A2C_ERR_CUDA;
+  cudaFreeAsync(dsites, c->stream);
+  cudaFreeAsync(dg, c->stream);
+  cudaFreeAsync(dfull, c->stream);
+  if (s) return s;
+  c->has_density = false;
+  return finish(c);
+}
+
+a2c_status a2c_gpp_diffuse(a2c_gpp_ctx *c, double dt, double nu, double Qm, double xLb, double xUb,
+                           const double *gamma, const int *full_H, double *x) {
+  if (!c || ((!gamma || !full_H || !x) && c->p.nH > 0)) return A2C_ERR_INVALID;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  const int nH = c->p.nH;
+  if (nH == 0) return A2C_OK;
+  DeviceGuard g(c->device);
+  double *dg, *dsend, *dx;
+  int *dfull;
+  A2C_TRY(ensure_hscratch(c, &dg, &dsend, &dx, &dfull));
+  a2c_status s = A2C_OK;
+  if (cudaMemcpyAsync(dg, gamma, sizeof(double) * nH, cudaMemcpyHostToDevice, c->stream) ||
+      cudaMemcpyAsync(dfull, full_H, sizeof(int) * nH, cudaMemcpyHostToDevice, c->stream) ||
+      cudaMemcpyAsync(dx, x, sizeof(double) * nH, cudaMemcpyHostToDevice, c->stream))
+    s = A2C_ERR_CUDA;
+  if (!s) s = launch_diffuse(c, dg, dfull, dt, nu, Qm, xLb, xUb, dx);
+  if (!s && cudaMemcpyAsync(x, dx, sizeof(double) * nH, cudaMemcpyDeviceToHost, c->stream)) s = A2C_ERR_CUDA;
+  free_hscratch(c, dg, dsend, dx, dfull);
+  if (s) return s;
+  return finish(c);
+}
+
+a2c_status a2c_gpp_macro_results(a2c_gpp_ctx *c, const double *x, const int *HSurf, int nSurf, double *xH,
+                                 double *xHinterior) {
+  if (!c || !xH || !xHinterior || nSurf < 0 || (c->p.nH > 0 && !x) || (nSurf > 0 && !HSurf)) return A2C_ERR_INVALID;
+  const int nH = c->p.nH;
+  if (nH == 0) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  std::vector<int> flags((size_t)nH, 0);
+  for (int t = 0; t < nSurf; ++t)
+    if (HSurf[t] >= 0 && HSurf[t] < nH) flags[(size_t)HSurf[t]] = 1;
+  double *dx = nullptr;
+  int *df = nullptr;
+  A2C_CUDA(cudaMallocAsync((void **)&dx, sizeof(double) * nH, c->stream));
+  A2C_CUDA(cudaMallocAsync((void **)&df, sizeof(int) * nH, c->stream));
+  a2c_status s = A2C_OK;
+  if (cudaMemcpyAsync(dx, x, sizeof(double) * nH, cudaMemcpyHostToDevice, c->stream) ||
+      cudaMemcpyAsync(df, flags.data(), sizeof(int) * nH, cudaMemcpyHostToDevice, c->stream))
+    s = A2C_ERR_CUDA;
+  if (!s) s = launch_macro(c, dx, df, nSurf, xH, xHinterior);
+  cudaFreeAsync(dx, c->stream);
+  cudaFreeAsync(df, c->stream);
+  if (s) return s;
+  return finish(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// Internal declarations shared by the CUDA translation units of liba2c_gpp.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "a2c_gpp.h"
+
+namespace a2c {
+
+// Neighbor entry: global site id in the low 27 bits, periodic image code
+// (mx+1) + 3(my+1) + 9(mz+1) in the top 5 bits; code 13 means no shift.
+constexpr uint32_t kIdBits = 27;
+constexpr uint32_t kIdMask = (1u << kIdBits) - 1u;
+constexpr uint32_t kNoShift = 13u;
+constexpr double kB = 8.6173324e-5;  // minimizer.cpp:92
+
+// Device pointers and scalars one FP64 kernel launch needs.
+struct SiteArgs {
+  int nPd, nH;
+  double T, W, eps;
+  double box[3];
+  const double *X;      // 4N AoS [qx,qy,qz,sigma]
+  const double *occ;    // N: 1 for Pd, x for H
+  const int64_t *off;   // N+1
+  const uint32_t *nbr;  // entries
+  const int *npd;       // N: number of Pd entries at the head of each list
+  double *rho;          // N
+  double *Fp;           // N: F'(rho) of the site's species (FD form)
+  double *G;            // 4N
+  double *Vs;           // N: per-site energy partial
+  double *Ss;           // N: per-site sigma-entropy partial
+  int *status;          // device status word (0 = ok)
+};
+
+// Device status bits (a2c never traps; kernels record and return).
+enum : int { kStatusNonfinite = 1, kStatusOverflow = 2, kStatusTimeout = 4, kStatusBadIndex = 8 };
+
+struct Mixed;   // mixed-precision buffers (k_mixed.cu)
+struct Lbfgs;   // L-BFGS buffers (lbfgs.cu)
+
+}  // namespace a2c
+
+struct a2c_gpp_ctx {
+  a2c_gpp_params p;
+  int64_t N;
+  int device;
+  cudaStream_t stream;
+  bool has_state, has_neighbors, has_density;
+  // state and results
+  double *d_X, *d_G, *d_occ, *d_rho, *d_Fp, *d_Vs, *d_Ss;
+  double *d_red;   // reduction scratch (partials + scalars)
+  int *d_status;
+  // neighbors
+  int64_t *d_off;
+  uint32_t *d_nbr;
+  int64_t nbr_cap, nbr_total;
+  int *d_npd;
+  int *d_shell;        // nPd x 3
+  int64_t *d_hh1_off;  // nH+1
+  int *d_hh1;
+  int64_t hh1_cap, hh1_total;
+  int max_neighbors;
+  // host staging
+  double *h_pinned;
+  int64_t h_pinned_n;
+  a2c::Mixed *mixed;
+  a2c::Lbfgs *lbfgs;
+};
+
+namespace a2c {
+
+// error helpers
+a2c_status cuda_status(cudaError_t e);
+#define A2C_CUDA(call)                               \
+  do {                                               \
+    cudaError_t e__ = (call);                        \
+    if (e__ != cudaSuccess) return a2c::cuda_status(e__); \
+  } while (0)
+#define A2C_TRY(call)                \
+  do {                               \
+    a2c_status s__ = (call);         \
+    if (s__ != A2C_OK) return s__;   \
+  } while (0)
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+// k_fp64.cu
+a2c_status launch_density64(a2c_gpp_ctx *c, const double *dX);
+a2c_status launch_gradient64(a2c_gpp_ctx *c, const double *dX, double *dG);
+a2c_status launch_chem64(a2c_gpp_ctx *c, const double *dX, double gamma_bd, double *d_send, const int *d_full);
+
+// k_misc.cu
+a2c_status reduce_objective(a2c_gpp_ctx *c, double *d_f);        // f from Vs, Ss
+a2c_status launch_finite_check(a2c_gpp_ctx *c, const double *d, int64_t n);
+a2c_status launch_gamma_update(a2c_gpp_ctx *c, const double *d_send, double gamma_bd, double *d_gamma, int *d_full);
+a2c_status launch_diffuse(a2c_gpp_ctx *c, const double *d_gamma, const int *d_full, double dt, double nu,
+                          double Qm, double xLb, double xUb, double *d_x);
+a2c_status launch_dirichlet(a2c_gpp_ctx *c, const int *d_sites, int n, double gamma_bd, double xUb, double *d_gamma,
+                            int *d_full);
+a2c_status launch_macro(a2c_gpp_ctx *c, const double *d_x, const int *d_surf_flags, int nSurf, double *h_xH,
+                        double *h_xHint);
+a2c_status check_status_word(a2c_gpp_ctx *c);
+
+// k_neighbors.cu
+a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X);
+
+// k_mixed.cu
+a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG);
+void mixed_free(a2c_gpp_ctx *c);
+
+// lbfgs.cu
+a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp, double *fmin, int *iters,
+                          int *nfev, double *gnorm, int *reason);
+void lbfgs_free(a2c_gpp_ctx *c);
+
+// api.cu
+a2c_status eval_device_impl(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG);
+
+}  // namespace a2c

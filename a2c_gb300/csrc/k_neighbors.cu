@@ -1,0 +1,352 @@
+// Cell-list neighbor build.  Replaces findNeighbors (neighbors.cpp:8-115,
+// KD-tree + inclusive d^2 <= rc^2 test, self excluded) followed by
+// Minimizer::findLocalNeighbors (minimizer.cpp:833-1144: refilter at rc, Pd
+// shell counts PdPdnum, first H shell HH1).  Compiled with -fmad=false so
+// the distance test reproduces the reference's arithmetic exactly: the
+// neighbor SETS are bit-exact; each list is sorted by global id (the
+// reference's order is a KD-tree traversal artefact).
+//
+// Periodic dimensions use the minimum image, which the reference lacks: the
+// image multiplier m = -rint((q_j - q_i)/L) is fixed at build time and
+// stored in the entry's top bits, as the reference holds its lists fixed
+// through a solve.
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace a2c {
+namespace {
+
+constexpr int kBlock = 128;
+constexpr int kMaxPerSite = 1000;  // neighbors.cpp:42 (maxNei)
+
+struct GridArgs {
+  int n[3];
+  int scan_all[3];  // periodic with fewer than 3 cells: visit every cell once
+  int periodic[3];
+  double lo[3], cs[3], box[3];
+  double rc, rc2, A75, A125;
+  int nPd;
+  int64_t N;
+  const double *X;
+};
+
+__device__ __forceinline__ int cell_coord(const GridArgs &g, double x, int d) {
+  double t;
+  if (g.periodic[d]) t = x - g.box[d] * floor(x / g.box[d]);
+  else t = x - g.lo[d];
+  int c = (int)floor(t / g.cs[d]);
+  return c < 0 ? 0 : (c >= g.n[d] ? g.n[d] - 1 : c);
+}
+
+__device__ __forceinline__ int64_t cell_of(const GridArgs &g, int64_t s) {
+  const int c0 = cell_coord(g, g.X[4 * s], 0), c1 = cell_coord(g, g.X[4 * s + 1], 1),
+            c2 = cell_coord(g, g.X[4 * s + 2], 2);
+  return ((int64_t)c2 * g.n[1] + c1) * g.n[0] + c0;
+}
+
+// The reference's acceptance test (KDTree.h:250-254 Chebyshev prefilter,
+// neighbors.cpp:77-82 self and squared distance), with the image shift.
+__device__ __forceinline__ bool pair_test(const GridArgs &g, int64_t i, int64_t j, uint32_t &entry, double &d2) {
+  if (i == j) return false;
+  double dd[3];
+  int m[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double qi = g.X[4 * i + d];
+    double qj = g.X[4 * j + d];
+    m[d] = 0;
+    if (g.periodic[d]) {
+      const double n = rint((qj - qi) / g.box[d]);
+      m[d] = -(int)n;
+      if (m[d] != 0) qj = qj + m[d] * g.box[d];
+    }
+    dd[d] = qj - qi;
+    if (fabs(dd[d]) > g.rc) return false;
+  }
+  d2 = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
+  if (d2 > g.rc2) return false;
+  if (m[0] < -1 || m[0] > 1 || m[1] < -1 || m[1] > 1 || m[2] < -1 || m[2] > 1) return false;
+  entry = (uint32_t)j | ((uint32_t)((m[0] + 1) + 3 * (m[1] + 1) + 9 * (m[2] + 1)) << kIdBits);
+  return true;
+}
+
+template <class Fn>
+__device__ __forceinline__ void for_candidates(const GridArgs &g, const int64_t *cstart, const int *items,
+                                               int64_t i, Fn fn) {
+  int c[3], lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) {
+    c[d] = cell_coord(g, g.X[4 * i + d], d);
+    if (g.scan_all[d]) {
+      lo[d] = 0;
+      hi[d] = g.n[d] - 1;
+    } else {
+      lo[d] = c[d] - 1;
+      hi[d] = c[d] + 1;
+    }
+  }
+  for (int a = lo[2]; a <= hi[2]; ++a) {
+    int ca = a;
+    if (!g.scan_all[2]) {
+      if (g.periodic[2]) ca = (a + g.n[2]) % g.n[2];
+      else if (a < 0 || a >= g.n[2]) continue;
+    }
+    for (int b = lo[1]; b <= hi[1]; ++b) {
+      int cb = b;
+      if (!g.scan_all[1]) {
+        if (g.periodic[1]) cb = (b + g.n[1]) % g.n[1];
+        else if (b < 0 || b >= g.n[1]) continue;
+      }
+      for (int e = lo[0]; e <= hi[0]; ++e) {
+        int ce = e;
+        if (!g.scan_all[0]) {
+          if (g.periodic[0]) ce = (e + g.n[0]) % g.n[0];
+          else if (e < 0 || e >= g.n[0]) continue;
+        }
+        const int64_t cell = ((int64_t)ca * g.n[1] + cb) * g.n[0] + ce;
+        for (int64_t t = cstart[cell]; t < cstart[cell + 1]; ++t) fn((int64_t)items[t]);
+      }
+    }
+  }
+}
+
+__global__ void k_cell_count(GridArgs g, int *cell, int *ccount) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= g.N) return;
+  const int64_t c = cell_of(g, s);
+  cell[s] = (int)c;
+  atomicAdd(&ccount[c], 1);
+}
+
+__global__ void k_cell_fill(GridArgs g, const int *cell, const int64_t *cstart, int *cfill, int *items) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= g.N) return;
+  const int c = cell[s];
+  const int slot = atomicAdd(&cfill[c], 1);
+  items[cstart[c] + slot] = (int)s;
+}
+
+__global__ void __launch_bounds__(kBlock) k_nbr_count(GridArgs g, const int64_t *cstart, const int *items,
+                                                      int64_t *count, int *npd, int64_t *hh1count, int *shell,
+                                                      int *status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.N) return;
+  int64_t n = 0, nP = 0, n1 = 0;
+  int sh[3] = {0, 0, 0};
+  const bool iPd = i < g.nPd;
+  for_candidates(g, cstart, items, i, [&](int64_t j) {
+    uint32_t e;
+    double d2;
+    if (!pair_test(g, i, j, e, d2)) return;
+    ++n;
+    const bool jPd = j < g.nPd;
+    if (jPd) {
+      ++nP;
+      if (iPd) {  // minimizer.cpp:935-947
+        if (d2 < g.A75) ++sh[0];
+        else if (d2 > g.A75 && d2 < g.A125) ++sh[1];
+        else ++sh[2];
+      }
+    } else if (!iPd && d2 < g.A75) {  // minimizer.cpp:999-1004
+      ++n1;
+    }
+  });
+  count[i] = n;
+  npd[i] = (int)nP;
+  if (iPd) {
+    shell[3 * i] = sh[0];
+    shell[3 * i + 1] = sh[1];
+    shell[3 * i + 2] = sh[2];
+  } else {
+    hh1count[i - g.nPd] = n1;
+  }
+  if (n > kMaxPerSite) atomicOr(status, kStatusOverflow);
+}
+
+__global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, const int64_t *cstart, const int *items,
+                                                     const int64_t *off, uint32_t *nbr, const int64_t *hh1_off,
+                                                     int *hh1, int *status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.N) return;
+  const int64_t b = off[i], e = off[i + 1];
+  int64_t w = b;
+  for_candidates(g, cstart, items, i, [&](int64_t j) {
+    uint32_t en;
+    double d2;
+    if (!pair_test(g, i, j, en, d2)) return;
+    if (w < e) nbr[w] = en;
+    ++w;
+  });
+  if (w != e) {
+    atomicOr(status, kStatusBadIndex);
+    return;
+  }
+  // insertion sort of the segment by global id
+  for (int64_t t = b + 1; t < e; ++t) {
+    const uint32_t v = nbr[t];
+    const uint32_t key = v & kIdMask;
+    int64_t u = t - 1;
+    while (u >= b && (nbr[u] & kIdMask) > key) {
+      nbr[u + 1] = nbr[u];
+      --u;
+    }
+    nbr[u + 1] = v;
+  }
+  if (i >= g.nPd) {
+    const int64_t h = i - g.nPd;
+    int64_t w1 = hh1_off[h];
+    for (int64_t t = b; t < e; ++t) {
+      const int64_t j = nbr[t] & kIdMask;
+      if (j < g.nPd) continue;
+      uint32_t en;
+      double d2;
+      if (pair_test(g, i, j, en, d2) && d2 < g.A75) {
+        if (w1 < hh1_off[h + 1]) hh1[w1] = (int)(j - g.nPd);
+        ++w1;
+      }
+    }
+    if (w1 != hh1_off[h + 1]) atomicOr(status, kStatusBadIndex);
+  }
+}
+
+__global__ void k_max_count(const int64_t *count, int64_t n, int *out) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) atomicMax(out, (int)count[s]);
+}
+
+template <class T>
+a2c_status scan_exclusive(const T *in, int64_t *out, int64_t n, cudaStream_t st) {
+  size_t bytes = 0;
+  A2C_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, n, st));
+  void *tmp = nullptr;
+  A2C_CUDA(cudaMallocAsync(&tmp, bytes, st));
+  cudaError_t e = cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, n, st);
+  cudaFreeAsync(tmp, st);
+  A2C_CUDA(e);
+  return A2C_OK;
+}
+
+struct DevBuf {
+  void *p = nullptr;
+  cudaStream_t st;
+  explicit DevBuf(cudaStream_t s) : st(s) {}
+  ~DevBuf() {
+    if (p) cudaFreeAsync(p, st);
+  }
+};
+
+}  // namespace
+
+a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X) {
+  const int64_t N = c->N;
+  const a2c_gpp_params &p = c->p;
+  cudaStream_t st = c->stream;
+  GridArgs g{};
+  g.N = N;
+  g.nPd = p.nPd;
+  g.X = c->d_X;
+  g.rc = p.rc;
+  g.rc2 = p.rc * p.rc;
+  g.A75 = p.a_Pd * p.a_Pd * 0.75;
+  g.A125 = p.a_Pd * p.a_Pd * 1.25;
+  int64_t ncell = 1;
+  for (int d = 0; d < 3; ++d) {
+    g.periodic[d] = p.periodic[d] ? 1 : 0;
+    g.box[d] = p.box[d];
+    double ext;
+    if (g.periodic[d]) {
+      g.lo[d] = 0.0;
+      ext = p.box[d];
+    } else {
+      double lo = HUGE_VAL, hi = -HUGE_VAL;
+      for (int64_t s = 0; s < N; ++s) {
+        lo = std::min(lo, h_X[4 * s + d]);
+        hi = std::max(hi, h_X[4 * s + d]);
+      }
+      if (N == 0) lo = hi = 0.0;
+      g.lo[d] = lo;
+      ext = hi - lo;
+    }
+    int n = (int)std::floor(ext / (p.rc + 1e-6));
+    if (n < 1) n = 1;
+    if (n > 512) n = 512;
+    g.n[d] = n;
+    g.cs[d] = (ext > 0.0) ? ext / n : 1.0;
+    g.scan_all[d] = (g.periodic[d] && n < 3) || n < 3 ? 1 : 0;
+    ncell *= n;
+  }
+  A2C_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
+
+  DevBuf cell(st), ccount(st), cstart(st), cfill(st), items(st), counts(st), hh1c(st), maxc(st);
+  A2C_CUDA(cudaMallocAsync(&cell.p, sizeof(int) * std::max<int64_t>(N, 1), st));
+  A2C_CUDA(cudaMallocAsync(&ccount.p, sizeof(int) * (ncell + 1), st));
+  A2C_CUDA(cudaMallocAsync(&cstart.p, sizeof(int64_t) * (ncell + 1), st));
+  A2C_CUDA(cudaMallocAsync(&cfill.p, sizeof(int) * (ncell + 1), st));
+  A2C_CUDA(cudaMallocAsync(&items.p, sizeof(int) * std::max<int64_t>(N, 1), st));
+  A2C_CUDA(cudaMallocAsync(&counts.p, sizeof(int64_t) * (N + 1), st));
+  A2C_CUDA(cudaMallocAsync(&hh1c.p, sizeof(int64_t) * (p.nH + 1), st));
+  A2C_CUDA(cudaMallocAsync(&maxc.p, sizeof(int), st));
+  A2C_CUDA(cudaMemsetAsync(ccount.p, 0, sizeof(int) * (ncell + 1), st));
+  A2C_CUDA(cudaMemsetAsync(cfill.p, 0, sizeof(int) * (ncell + 1), st));
+  A2C_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int64_t) * (N + 1), st));
+  A2C_CUDA(cudaMemsetAsync(hh1c.p, 0, sizeof(int64_t) * (p.nH + 1), st));
+  A2C_CUDA(cudaMemsetAsync(maxc.p, 0, sizeof(int), st));
+  if (N > 0) {
+    k_cell_count<<<grid_for(N, 256), 256, 0, st>>>(g, (int *)cell.p, (int *)ccount.p);
+    A2C_CUDA(cudaGetLastError());
+  }
+  A2C_TRY(scan_exclusive((const int *)ccount.p, (int64_t *)cstart.p, ncell + 1, st));
+  if (N > 0) {
+    k_cell_fill<<<grid_for(N, 256), 256, 0, st>>>(g, (const int *)cell.p, (const int64_t *)cstart.p,
+                                                   (int *)cfill.p, (int *)items.p);
+    A2C_CUDA(cudaGetLastError());
+    k_nbr_count<<<grid_for(N, kBlock), kBlock, 0, st>>>(g, (const int64_t *)cstart.p, (const int *)items.p,
+                                                        (int64_t *)counts.p, c->d_npd, (int64_t *)hh1c.p,
+                                                        c->d_shell, c->d_status);
+    A2C_CUDA(cudaGetLastError());
+    k_max_count<<<grid_for(N, 256), 256, 0, st>>>((const int64_t *)counts.p, N, (int *)maxc.p);
+    A2C_CUDA(cudaGetLastError());
+  }
+  A2C_TRY(scan_exclusive((const int64_t *)counts.p, c->d_off, N + 1, st));
+  A2C_TRY(scan_exclusive((const int64_t *)hh1c.p, c->d_hh1_off, (int64_t)p.nH + 1, st));
+  int64_t total = 0, total1 = 0;
+  int maxn = 0, stat = 0;
+  A2C_CUDA(cudaMemcpyAsync(&total, c->d_off + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaMemcpyAsync(&total1, c->d_hh1_off + p.nH, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaMemcpyAsync(&maxn, maxc.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaMemcpyAsync(&stat, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaStreamSynchronize(st));
+  if (stat & kStatusOverflow) return A2C_ERR_NEIGHBOR_OVERFLOW;
+  if (total > c->nbr_cap) {
+    if (c->d_nbr) cudaFree(c->d_nbr);
+    c->d_nbr = nullptr;
+    c->nbr_cap = 0;
+    if (cudaMalloc(&c->d_nbr, sizeof(uint32_t) * std::max<int64_t>(total, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
+    c->nbr_cap = total;
+  }
+  if (total1 > c->hh1_cap) {
+    if (c->d_hh1) cudaFree(c->d_hh1);
+    c->d_hh1 = nullptr;
+    c->hh1_cap = 0;
+    if (cudaMalloc(&c->d_hh1, sizeof(int) * std::max<int64_t>(total1, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
+    c->hh1_cap = total1;
+  }
+  c->nbr_total = total;
+  c->hh1_total = total1;
+  c->max_neighbors = maxn;
+  if (N > 0) {
+    k_nbr_fill<<<grid_for(N, kBlock), kBlock, 0, st>>>(g, (const int64_t *)cstart.p, (const int *)items.p, c->d_off,
+                                                       c->d_nbr, c->d_hh1_off, c->d_hh1, c->d_status);
+    A2C_CUDA(cudaGetLastError());
+  }
+  A2C_CUDA(cudaMemcpyAsync(&stat, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaStreamSynchronize(st));
+  if (stat & kStatusBadIndex) return A2C_ERR_STATE;
+  return A2C_OK;
+}
+
+}  // namespace a2c

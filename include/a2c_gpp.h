@@ -1,0 +1,192 @@
+/*
+ * a2c_gpp.h -- C ABI of the GB300-native GPP-EAM evaluator for a2c's
+ * diffusive-molecular-dynamics hot path.
+ *
+ * Everything crosses this boundary as plain pointers, sizes and status codes;
+ * no C++ exception, CUDA type or torch type appears in a signature.  A
+ * context owns all device memory; host pointers are borrowed for the call.
+ * Calls on one context are single-host-thread; all device work runs on the
+ * context's stream.  Functions without the _device suffix take host
+ * pointers and return after the results are in host memory; the _device
+ * variants take device pointers and are stream-ordered.
+ *
+ * Layouts follow the reference:
+ *   X, G   4*(nPd+nH) doubles, AoS per site [qx, qy, qz, sigma], all Pd sites
+ *          then all H sites (minimizer.cpp:398-418, 464-473)
+ *   xH     nH doubles, H site occupancy (Pd sites carry an implicit 1)
+ *   lists  per-site neighbor indices local to the neighbor's species, as in
+ *          the reference's PdPd / PdH / HPd / HH / HH1 vectors
+ */
+#ifndef A2C_GPP_H
+#define A2C_GPP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  0 is success, as PetscErrorCode (minimizer.cpp:110). */
+typedef int a2c_status;
+enum {
+  A2C_OK = 0,
+  A2C_ERR_INVALID = 1,            /* bad argument or parameter */
+  A2C_ERR_CUDA = 2,               /* a CUDA runtime call failed */
+  A2C_ERR_NOMEM = 3,              /* device allocation failed */
+  A2C_ERR_NEIGHBOR_OVERFLOW = 4,  /* a site exceeded the neighbor capacity */
+  A2C_ERR_NONFINITE = 5,          /* NaN/Inf in an input or a result */
+  A2C_ERR_STATE = 6,              /* call order violated (e.g. no neighbors) */
+  A2C_ERR_TIMEOUT = 7,            /* a bounded device wait gave up */
+  A2C_ERR_NO_DEVICE = 8           /* no usable CUDA device */
+};
+
+/* Arithmetic forms of the evaluator. */
+enum {
+  A2C_FP64 = 0,  /* plain form: the reference's FP64 arithmetic and order */
+  A2C_MIXED = 1  /* FP32 pair quadrature, FP64 reductions and entropy terms */
+};
+
+/* Neighbor list ids for a2c_gpp_get_neighbors. */
+enum { A2C_LIST_PDPD = 0, A2C_LIST_PDH = 1, A2C_LIST_HPD = 2, A2C_LIST_HH = 3, A2C_LIST_HH1 = 4 };
+
+/* L-BFGS termination reasons, numbered like TaoConvergedReason. */
+enum {
+  A2C_CONVERGED_GATOL = 3,
+  A2C_CONTINUE = 0,
+  A2C_DIVERGED_MAXITS = -2,
+  A2C_DIVERGED_NAN = -4,
+  A2C_DIVERGED_MAXFCN = -5,
+  A2C_DIVERGED_LS_FAILURE = -6
+};
+
+/* Problem parameters.  The reference reads these from its input object
+ * (input.file.T0, eps, rc, a_Pd; QWp, coe_Pd, coe_H from the missing
+ * driver).  periodic[] and box[] enable the minimum-image extension, which
+ * the reference does not have. */
+typedef struct a2c_gpp_params {
+  int nPd, nH;
+  double T;          /* temperature [K] */
+  double QWp;        /* quadrature weight, 1/12 for the 12-point rule */
+  double eps;        /* finite-difference step of the EAM derivatives */
+  double rc;         /* neighbor cutoff [A] */
+  double a_Pd;       /* lattice constant for shell classification [A] */
+  double box[3];     /* periodic lengths [A] */
+  int periodic[3];
+  double coe_Pd[4];  /* correction coefficients of the chemical potential */
+  double coe_H[4];
+  int precision;     /* A2C_FP64 or A2C_MIXED */
+  int device;        /* CUDA device ordinal */
+} a2c_gpp_params;
+
+typedef struct a2c_lbfgs_params {
+  int m;            /* stored correction pairs */
+  int max_it;       /* iteration cap */
+  int max_fev;      /* objective-evaluation cap */
+  int max_ls;       /* backtracking steps per line search */
+  double gatol;     /* ||projected gradient||_2 tolerance (TAO gatol) */
+  double c1;        /* Armijo constant */
+  double init_step; /* max |component| of a steepest-descent step */
+  double sigma_lb;  /* lower bound on widths (minimizer.cpp:815, 822) */
+} a2c_lbfgs_params;
+
+typedef struct a2c_gpp_ctx a2c_gpp_ctx;
+
+/* Fills defaults: T=300, QWp=1/12, eps=1e-5, rc=5.35, a_Pd=3.89,
+ * coefficients 0, FP64, device 0, non-periodic. */
+void a2c_gpp_default_params(a2c_gpp_params *p);
+void a2c_lbfgs_default_params(a2c_lbfgs_params *p);
+const char *a2c_status_string(a2c_status s);
+
+/* Lifecycle.  Replaces Minimizer::Minimizer + Minimizer::initialize
+ * (minimizer.cpp:60-69, 484-546) and ~Minimizer (72-80). */
+a2c_status a2c_gpp_create(const a2c_gpp_params *p, a2c_gpp_ctx **out);
+a2c_status a2c_gpp_destroy(a2c_gpp_ctx *ctx);
+/* The context's CUDA stream, as a cudaStream_t cast to void*. */
+void *a2c_gpp_stream(a2c_gpp_ctx *ctx);
+a2c_status a2c_gpp_set_precision(a2c_gpp_ctx *ctx, int precision);
+
+/* H occupancy x0 used by every later call; replaces the x0 pointer swap of
+ * Minimizer::updateApplicationContext (minimizer.cpp:372-378). */
+a2c_status a2c_gpp_set_occupancy(a2c_gpp_ctx *ctx, const double *xH);
+a2c_status a2c_gpp_get_occupancy(a2c_gpp_ctx *ctx, double *xH);
+/* Stores X as the context's current state (used by chem_potential). */
+a2c_status a2c_gpp_set_state(a2c_gpp_ctx *ctx, const double *X);
+a2c_status a2c_gpp_get_state(a2c_gpp_ctx *ctx, double *X);
+
+/* Neighbor build from positions X: cell list, d^2 <= rc^2, self excluded,
+ * minimum image where periodic.  Replaces findNeighbors
+ * (neighbors.cpp:8-115) followed by Minimizer::findLocalNeighbors
+ * (minimizer.cpp:833-1144); the lists are held fixed until the next build,
+ * as in the reference.  max_neighbors receives the largest per-site count
+ * (the reference's maxNeib). */
+a2c_status a2c_gpp_build_neighbors(a2c_gpp_ctx *ctx, const double *X, int *max_neighbors);
+/* Sizes for a2c_gpp_get_neighbors: total entries of a list. */
+a2c_status a2c_gpp_neighbor_total(a2c_gpp_ctx *ctx, int list_id, int64_t *total);
+/* Export a list in the reference's form: offsets[n+1], idx[total] local to
+ * the neighbor species, each site's list sorted ascending. */
+a2c_status a2c_gpp_get_neighbors(a2c_gpp_ctx *ctx, int list_id, int64_t *offsets, int *idx);
+/* PdPdnum (minimizer.cpp:935-947): nPd x 3 shell counts. */
+a2c_status a2c_gpp_get_shell_counts(a2c_gpp_ctx *ctx, int *PdPdnum);
+
+/* Objective (free entropy) and gradient at X.  Replaces the TAO callback
+ * Minimizer::formFunctionAndGradient (minimizer.cpp:83-369); X also becomes
+ * the current state. */
+a2c_status a2c_gpp_eval(a2c_gpp_ctx *ctx, const double *X, double *f, double *G);
+a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG);
+/* Site electron densities of the last evaluation, all Pd then all H
+ * (electrondensity.cpp:12-56, the reference's recv_Pd / recv_H). */
+a2c_status a2c_gpp_get_density(a2c_gpp_ctx *ctx, double *rho);
+
+/* Variable bounds: q free, sigma >= 1e-6 (minimizer.cpp:804-830). */
+a2c_status a2c_gpp_bounds(a2c_gpp_ctx *ctx, double *lb, double *ub);
+
+/* Bound-constrained L-BFGS from X (in/out) on the device; replaces
+ * Minimizer::minimizeFreeEntropy + TaoSolve (minimizer.cpp:548-586).
+ * X becomes the current state.  reason follows TaoConvergedReason. */
+a2c_status a2c_gpp_minimize(a2c_gpp_ctx *ctx, double *X, const a2c_lbfgs_params *lp, double *fmin, int *iters,
+                            int *nfev, double *gnorm, int *reason);
+
+/* Occupancy gradient / chemical potential at the current state.  Replaces
+ * Minimizer::calculateChemicalPotential (minimizer.cpp:588-802); gamma and
+ * full_H are nH arrays, read and updated in place. */
+a2c_status a2c_gpp_chem_potential(a2c_gpp_ctx *ctx, double gamma_bd, double *gamma, int *full_H);
+
+/* Dirichlet condition on the listed H sites: gamma = gamma_bd, full_H = 1,
+ * x0 = xUb, applied to the context occupancy and to the caller's arrays.
+ * Replaces enforceBoundaryConditions (boundaryconditions.cpp:30-55). */
+a2c_status a2c_gpp_apply_dirichlet(a2c_gpp_ctx *ctx, const int *sites, int n, double gamma_bd, double xUb,
+                                   double *gamma, int *full_H);
+
+/* One explicit mean-field diffusion step over the first H shell from the
+ * context occupancy x0 into x (nH, in/out: sites with full_H == 1 keep the
+ * caller's value).  Replaces integrateDiffusion (integrate.cpp:9-87). */
+a2c_status a2c_gpp_diffuse(a2c_gpp_ctx *ctx, double dt, double nu, double Qm, double xLb, double xUb,
+                           const double *gamma, const int *full_H, double *x);
+
+/* Mean H fraction over all H sites and over sites not in HSurf.  Replaces
+ * calculateMacroResults (calculateresults.cpp:8-78). */
+a2c_status a2c_gpp_macro_results(a2c_gpp_ctx *ctx, const double *x, const int *HSurf, int nSurf, double *xH,
+                                 double *xHinterior);
+
+/* Seeded synthetic fcc Pd lattice with octahedral H sites (stand-in for the
+ * reference's SpaceInitializer lattice setup).  Site order: cells z, y, x,
+ * then basis; all Pd then all H.  Writes X (4N), xH (nH) and surface flags
+ * (nH; 1 where the unperturbed z is below 1e-6). */
+typedef struct a2c_lattice_spec {
+  int ncell[3];
+  double a;
+  int periodic[3];
+  double pos_std;          /* N(0, pos_std) per position component */
+  double sigma_lo, sigma_hi; /* sigma ~ U(lo, hi), or lo when hi <= lo */
+  int x_mode;              /* 0: x = x_center + U(-x_half, x_half); 1: nucleus */
+  double x_center, x_half;
+  double x_matrix, x_nucleus, nucleus_radius, interface_width;
+  double xLb, xUb;         /* clamp of the drawn occupancy */
+  uint64_t seed;
+} a2c_lattice_spec;
+a2c_status a2c_lattice_fcc(const a2c_lattice_spec *spec, double *X, double *xH, int *surface);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

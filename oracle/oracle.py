@@ -1,0 +1,329 @@
+"""ctypes binding of the CPU oracle (liba2c_oracle.so) and, where it was
+built, of the reference's own hot-path sources (_ref/liba2c_ref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, as the checker.  No product code imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "_build" / "liba2c_oracle.so"
+REF_SO = HERE / "_ref" / "liba2c_ref.so"
+REFERENCE_TREE = Path("/root/reference")
+
+ID_MASK = (1 << 27) - 1
+EAM_FUNCS = ["F_Pd", "F_Pd_deriv", "F_H", "F_H_deriv", "f_Pd", "f_Pd_deriv", "f_H", "f_H_deriv", "phi_Pd",
+             "phi_Pd_deriv", "phi_PdH", "phi_PdH_deriv", "phi_H", "phi_H_deriv"]
+
+P, D, I, I64 = C.c_void_p, C.c_double, C.c_int, C.c_int64
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile the oracle (and the reference-shim library when the reference
+    tree is present)."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    if ref is None:
+        ref = REFERENCE_TREE.is_dir()
+    if ref:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+
+
+class OrcParams(C.Structure):
+    _fields_ = [("nPd", C.c_int), ("nH", C.c_int), ("T", D), ("QWp", D), ("eps", D), ("rc", D), ("a_Pd", D),
+                ("box", D * 3), ("periodic", C.c_int * 3), ("coe_Pd", D * 4), ("coe_H", D * 4)]
+
+
+class OrcLbfgs(C.Structure):
+    _fields_ = [("m", C.c_int), ("max_it", C.c_int), ("max_fev", C.c_int), ("max_ls", C.c_int), ("gatol", D),
+                ("c1", D), ("init_step", D), ("sigma_lb", D)]
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+_olib = None
+_rlib = None
+
+
+def olib() -> C.CDLL:
+    global _olib
+    if _olib is None:
+        if not ORACLE_SO.exists():
+            build(ref=False)
+        L = C.CDLL(str(ORACLE_SO))
+        L.orc_eam.argtypes = [I, P, I64, D, P]
+        L.orc_neighbor_counts.argtypes = [C.POINTER(OrcParams), P, P, P]
+        L.orc_neighbor_fill.argtypes = [C.POINTER(OrcParams), P, P, P, P, P, P]
+        L.orc_eval.argtypes = [C.POINTER(OrcParams), P, P, P, P, I, I, C.POINTER(D), P, P, P]
+        L.orc_density.argtypes = [C.POINTER(OrcParams), P, P, P, P, I, P]
+        L.orc_chem_potential.argtypes = [C.POINTER(OrcParams), P, P, P, P, D, I, P, P]
+        L.orc_diffuse.argtypes = [I, P, P, P, P, P, D, D, D, D, D, D, P]
+        L.orc_dirichlet.argtypes = [P, I, D, D, P, P, P]
+        L.orc_dirichlet.restype = None
+        L.orc_macro_results.argtypes = [I, P, P, I, C.POINTER(D), C.POINTER(D)]
+        L.orc_macro_results.restype = None
+        L.orc_minimize.argtypes = [C.POINTER(OrcParams), P, P, P, P, C.POINTER(OrcLbfgs), I, C.POINTER(D),
+                                   C.POINTER(I), C.POINTER(I), C.POINTER(D), C.POINTER(I)]
+        _olib = L
+    return _olib
+
+
+def ref_available() -> bool:
+    return REF_SO.exists()
+
+
+def rlib() -> C.CDLL:
+    global _rlib
+    if _rlib is None:
+        if not REF_SO.exists():
+            raise RuntimeError("reference library not built (oracle/_ref); needs the reference tree")
+        L = C.CDLL(str(REF_SO))
+        L.ref_eam.argtypes = [I, P, I64, D, P]
+        L.ref_eval.argtypes = [I, I, D, D, D, D, D, P, P, P, P, P, C.POINTER(D), P, P]
+        L.ref_density.argtypes = [I, I, D, D, D, P, P, P, P, P]
+        L.ref_density.restype = None
+        L.ref_chem_potential.argtypes = [I, I, D, D, D, D, D, P, P, P, P, P, D, P, P]
+        L.ref_neighbors_run.argtypes = [I, I, D, D, P]
+        L.ref_neighbors_total.argtypes = [I]
+        L.ref_neighbors_total.restype = I64
+        L.ref_neighbors_get.argtypes = [I, P, P]
+        L.ref_neighbors_get.restype = None
+        L.ref_neighbors_maxneib.argtypes = [I]
+        L.ref_diffuse.argtypes = [I, P, P, P, P, P, D, D, D, D, D, D, P]
+        L.ref_dirichlet.argtypes = [I, P, I, D, D, P, P, P]
+        L.ref_macro_results.argtypes = [I, P, P, I, C.POINTER(D), C.POINTER(D)]
+        _rlib = L
+    return _rlib
+
+
+class Problem:
+    """Parameters shared by oracle calls."""
+
+    def __init__(self, nPd, nH, *, T=300.0, QWp=1.0 / 12.0, eps=1e-5, rc=5.35, a_Pd=3.89, box=(0, 0, 0),
+                 periodic=(0, 0, 0), coe_Pd=(0, 0, 0, 0), coe_H=(0, 0, 0, 0)):
+        p = OrcParams()
+        p.nPd, p.nH, p.T, p.QWp, p.eps, p.rc, p.a_Pd = nPd, nH, T, QWp, eps, rc, a_Pd
+        for d in range(3):
+            p.box[d] = float(box[d])
+            p.periodic[d] = int(bool(periodic[d]))
+        for k in range(4):
+            p.coe_Pd[k] = float(coe_Pd[k])
+            p.coe_H[k] = float(coe_H[k])
+        self.p = p
+        self.nPd, self.nH, self.N = nPd, nH, nPd + nH
+
+    @property
+    def coe(self) -> np.ndarray:
+        return np.array(list(self.p.coe_Pd) + list(self.p.coe_H), dtype=np.float64)
+
+
+def nthreads() -> int:
+    return int(os.environ.get("A2C_ORACLE_THREADS", os.cpu_count() or 1))
+
+
+# -- oracle ----------------------------------------------------------------
+def eam(which: int | str, x, eps=1e-5) -> np.ndarray:
+    if isinstance(which, str):
+        which = EAM_FUNCS.index(which)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    olib().orc_eam(which, _p(x), x.size, eps, _p(out))
+    return out
+
+
+def neighbors(pb: Problem, X):
+    """Oracle neighbor lists: (off, nbr, PdPdnum, hh1_off, hh1)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    cnt = np.zeros(pb.N, dtype=np.int64)
+    c1 = np.zeros(max(pb.nH, 1), dtype=np.int64)
+    assert olib().orc_neighbor_counts(C.byref(pb.p), _p(X), _p(cnt), _p(c1)) == 0
+    off = np.zeros(pb.N + 1, dtype=np.int64)
+    off[1:] = np.cumsum(cnt)
+    off1 = np.zeros(pb.nH + 1, dtype=np.int64)
+    off1[1:] = np.cumsum(c1[: pb.nH])
+    nbr = np.zeros(max(int(off[-1]), 1), dtype=np.uint32)
+    hh1 = np.zeros(max(int(off1[-1]), 1), dtype=np.int32)
+    shell = np.zeros(3 * max(pb.nPd, 1), dtype=np.int32)
+    assert olib().orc_neighbor_fill(C.byref(pb.p), _p(X), _p(off), _p(nbr), _p(shell), _p(off1), _p(hh1)) == 0
+    return off, nbr[: off[-1]], shell[: 3 * pb.nPd].reshape(pb.nPd, 3), off1, hh1[: off1[-1]]
+
+
+def evaluate(pb: Problem, X, xH, off, nbr, mode=1, threads=None):
+    """Oracle objective: (f, G, rho, Vsite)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    xH = np.ascontiguousarray(xH, dtype=np.float64)
+    G = np.empty(4 * pb.N)
+    rho = np.empty(pb.N)
+    Vs = np.empty(pb.N)
+    f = C.c_double()
+    assert olib().orc_eval(C.byref(pb.p), _p(X), _p(xH), _p(off), _p(nbr), mode, threads or nthreads(), C.byref(f),
+                           _p(G), _p(rho), _p(Vs)) == 0
+    return f.value, G, rho, Vs
+
+
+def density(pb: Problem, X, xH, off, nbr, threads=None):
+    rho = np.empty(pb.N)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    xH = np.ascontiguousarray(xH, dtype=np.float64)
+    assert olib().orc_density(C.byref(pb.p), _p(X), _p(xH), _p(off), _p(nbr), threads or nthreads(), _p(rho)) == 0
+    return rho
+
+
+def chem_potential(pb: Problem, X, xH, off, nbr, gamma_bd, gamma, full_H, threads=None):
+    g = np.ascontiguousarray(gamma, dtype=np.float64).copy()
+    fh = np.ascontiguousarray(full_H, dtype=np.int32).copy()
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    xH = np.ascontiguousarray(xH, dtype=np.float64)
+    assert olib().orc_chem_potential(C.byref(pb.p), _p(X), _p(xH), _p(off), _p(nbr), gamma_bd,
+                                     threads or nthreads(), _p(g), _p(fh)) == 0
+    return g, fh
+
+
+def diffuse(nH, x0, hh1_off, hh1, gamma, full_H, T, dt, nu, Qm, xLb, xUb, x):
+    x = np.ascontiguousarray(x, dtype=np.float64).copy()
+    args = [np.ascontiguousarray(a, dtype=t) for a, t in
+            ((x0, np.float64), (hh1_off, np.int64), (hh1, np.int32), (gamma, np.float64), (full_H, np.int32))]
+    assert olib().orc_diffuse(nH, *[_p(a) for a in args], T, dt, nu, Qm, xLb, xUb, _p(x)) == 0
+    return x
+
+
+def dirichlet(sites, gamma_bd, xUb, x0, gamma, full_H):
+    s = np.ascontiguousarray(sites, dtype=np.int32)
+    x0 = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    g = np.ascontiguousarray(gamma, dtype=np.float64).copy()
+    fh = np.ascontiguousarray(full_H, dtype=np.int32).copy()
+    olib().orc_dirichlet(_p(s), s.size, gamma_bd, xUb, _p(x0), _p(g), _p(fh))
+    return x0, g, fh
+
+
+def macro_results(x, HSurf):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    hs = np.ascontiguousarray(HSurf, dtype=np.int32)
+    a, b = C.c_double(), C.c_double()
+    olib().orc_macro_results(x.size, _p(x), _p(hs) if hs.size else None, hs.size, C.byref(a), C.byref(b))
+    return a.value, b.value
+
+
+def minimize(pb: Problem, X, xH, off, nbr, *, m=5, max_it=10000, max_fev=20000, max_ls=30, gatol=1e-6, c1=1e-4,
+             init_step=1e-2, sigma_lb=1e-6, threads=None):
+    lp = OrcLbfgs(m, max_it, max_fev, max_ls, gatol, c1, init_step, sigma_lb)
+    X = np.ascontiguousarray(X, dtype=np.float64).copy()
+    xH = np.ascontiguousarray(xH, dtype=np.float64)
+    f, it, nf, gn, why = C.c_double(), C.c_int(), C.c_int(), C.c_double(), C.c_int()
+    assert olib().orc_minimize(C.byref(pb.p), _p(X), _p(xH), _p(off), _p(nbr), C.byref(lp), threads or nthreads(),
+                               C.byref(f), C.byref(it), C.byref(nf), C.byref(gn), C.byref(why)) == 0
+    return dict(X=X, fmin=f.value, iters=it.value, nfev=nf.value, gnorm=gn.value, reason=why.value)
+
+
+# -- list conversions --------------------------------------------------------
+def split_lists(nPd, nH, off, nbr):
+    """Combined per-site lists -> reference lists {PdPd, PdH, HPd, HH} as
+    (offsets, local indices)."""
+    ids = (np.asarray(nbr, dtype=np.uint32) & ID_MASK).astype(np.int64)
+    out = {}
+    for name, lo, hi, pdn in (("PdPd", 0, nPd, True), ("PdH", 0, nPd, False), ("HPd", nPd, nPd + nH, True),
+                              ("HH", nPd, nPd + nH, False)):
+        o = [0]
+        v = []
+        for s in range(lo, hi):
+            seg = ids[off[s]:off[s + 1]]
+            seg = seg[seg < nPd] if pdn else seg[seg >= nPd] - nPd
+            v.extend(seg.tolist())
+            o.append(len(v))
+        out[name] = (np.array(o, dtype=np.int64), np.array(v, dtype=np.int32))
+    return out
+
+
+# -- reference (compiled from its own sources against single-rank shims) -----
+def ref_eam(which, x, eps=1e-5):
+    if isinstance(which, str):
+        which = EAM_FUNCS.index(which)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    rlib().ref_eam(which, _p(x), x.size, eps, _p(out))
+    return out
+
+
+def ref_evaluate(pb: Problem, X, xH, off, nbr):
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    xH = np.ascontiguousarray(xH, dtype=np.float64)
+    G = np.empty(4 * pb.N)
+    rho = np.empty(pb.N)
+    f = C.c_double()
+    p = pb.p
+    coe = pb.coe
+    assert rlib().ref_eval(p.nPd, p.nH, p.T, p.QWp, p.eps, p.rc, p.a_Pd, _p(coe), _p(X), _p(xH), _p(off), _p(nbr),
+                           C.byref(f), _p(G), _p(rho)) == 0
+    return f.value, G, rho
+
+
+def ref_density(pb: Problem, X, xH, off, nbr):
+    rho = np.empty(pb.N)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    xH = np.ascontiguousarray(xH, dtype=np.float64)
+    rlib().ref_density(pb.nPd, pb.nH, pb.p.QWp, pb.p.eps, pb.p.rc, _p(X), _p(xH), _p(off), _p(nbr), _p(rho))
+    return rho
+
+
+def ref_chem_potential(pb: Problem, X, xH, off, nbr, gamma_bd, gamma, full_H):
+    g = np.ascontiguousarray(gamma, dtype=np.float64).copy()
+    fh = np.ascontiguousarray(full_H, dtype=np.int32).copy()
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    xH = np.ascontiguousarray(xH, dtype=np.float64)
+    p = pb.p
+    coe = pb.coe
+    assert rlib().ref_chem_potential(p.nPd, p.nH, p.T, p.QWp, p.eps, p.rc, p.a_Pd, _p(coe), _p(X), _p(xH), _p(off),
+                                     _p(nbr), gamma_bd, _p(g), _p(fh)) == 0
+    return g, fh
+
+
+def ref_neighbors(pb: Problem, X):
+    """Reference findNeighbors + findLocalNeighbors: dict of lists in the
+    reference's own (KD-tree) order, PdPdnum, and the two maxNeib values."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    L = rlib()
+    assert L.ref_neighbors_run(pb.nPd, pb.nH, pb.p.rc, pb.p.a_Pd, _p(X)) == 0
+    out = {}
+    for lid, name, n in ((0, "PdPd", pb.nPd), (1, "PdH", pb.nPd), (2, "HPd", pb.nH), (3, "HH", pb.nH),
+                         (4, "HH1", pb.nH), (5, "PdPdnum", pb.nPd)):
+        tot = L.ref_neighbors_total(lid)
+        off = np.zeros(n + 1, dtype=np.int64)
+        idx = np.zeros(max(tot, 1), dtype=np.int32)
+        L.ref_neighbors_get(lid, _p(off), _p(idx))
+        out[name] = (off, idx[:tot])
+    out["maxNeib"] = (L.ref_neighbors_maxneib(0), L.ref_neighbors_maxneib(1))
+    return out
+
+
+def ref_diffuse(nH, x0, hh1_off, hh1, gamma, full_H, T, dt, nu, Qm, xLb, xUb, x):
+    x = np.ascontiguousarray(x, dtype=np.float64).copy()
+    args = [np.ascontiguousarray(a, dtype=t) for a, t in
+            ((x0, np.float64), (hh1_off, np.int64), (hh1, np.int32), (gamma, np.float64), (full_H, np.int32))]
+    assert rlib().ref_diffuse(nH, *[_p(a) for a in args], T, dt, nu, Qm, xLb, xUb, _p(x)) == 0
+    return x
+
+
+def ref_dirichlet(nH, sites, gamma_bd, xUb, x0, gamma, full_H):
+    s = np.ascontiguousarray(sites, dtype=np.int32)
+    x0 = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    g = np.ascontiguousarray(gamma, dtype=np.float64).copy()
+    fh = np.ascontiguousarray(full_H, dtype=np.int32).copy()
+    assert rlib().ref_dirichlet(nH, _p(s), s.size, gamma_bd, xUb, _p(x0), _p(g), _p(fh)) == 0
+    return x0, g, fh
+
+
+def ref_macro_results(x, HSurf):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    hs = np.ascontiguousarray(HSurf, dtype=np.int32)
+    a, b = C.c_double(), C.c_double()
+    assert rlib().ref_macro_results(x.size, _p(x), _p(hs) if hs.size else None, hs.size, C.byref(a),
+                                    C.byref(b)) == 0
+    return a.value, b.value
