@@ -98,6 +98,9 @@ class Gpp:
     def stream(self) -> int:
         return int(self._L.a2c_gpp_stream(self._h) or 0)
 
+    def synchronize(self) -> None:
+        N.check(self._L.a2c_gpp_synchronize(self._h), "a2c_gpp_synchronize")
+
     def set_precision(self, precision: int | str) -> None:
         if isinstance(precision, str):
             precision = {"fp64": A2C_FP64, "mixed": A2C_MIXED}[precision]
@@ -160,6 +163,13 @@ class Gpp:
         r = np.empty(self.N)
         N.check(self._L.a2c_gpp_get_density(self._h, N.ptr(r)), "a2c_gpp_get_density")
         return r
+
+    def eam(self, which: int, x) -> np.ndarray:
+        """Device FP64 EAM function `which` (0..13, as a2c_gpp_eam_eval)."""
+        x = _f64(x)
+        out = np.empty_like(x)
+        N.check(self._L.a2c_gpp_eam_eval(self._h, int(which), N.ptr(x), x.size, N.ptr(out)), "a2c_gpp_eam_eval")
+        return out
 
     def bounds(self) -> tuple[np.ndarray, np.ndarray]:
         lb, ub = np.empty(4 * self.N), np.empty(4 * self.N)

@@ -86,6 +86,7 @@ def lib() -> C.CDLL:
         "a2c_gpp_destroy": (I, [P]),
         "a2c_gpp_stream": (P, [P]),
         "a2c_gpp_set_precision": (I, [P, I]),
+        "a2c_gpp_synchronize": (I, [P]),
         "a2c_gpp_set_occupancy": (I, [P, P]),
         "a2c_gpp_get_occupancy": (I, [P, P]),
         "a2c_gpp_set_state": (I, [P, P]),
@@ -98,6 +99,7 @@ def lib() -> C.CDLL:
         "a2c_gpp_eval_device": (I, [P, P, P, P]),
         "a2c_gpp_get_density": (I, [P, P]),
         "a2c_gpp_bounds": (I, [P, P, P]),
+        "a2c_gpp_eam_eval": (I, [P, I, P, C.c_int64, P]),
         "a2c_gpp_minimize": (I, [P, P, C.POINTER(LbfgsParams), C.POINTER(D), C.POINTER(I), C.POINTER(I),
                                  C.POINTER(D), C.POINTER(I)]),
         "a2c_gpp_chem_potential": (I, [P, D, P, P]),
@@ -117,10 +119,10 @@ def lib() -> C.CDLL:
 def exported_symbols() -> list[str]:
     """Names of the C ABI functions this binding expects the library to export."""
     return ["a2c_gpp_default_params", "a2c_lbfgs_default_params", "a2c_status_string", "a2c_gpp_create",
-            "a2c_gpp_destroy", "a2c_gpp_stream", "a2c_gpp_set_precision", "a2c_gpp_set_occupancy",
+            "a2c_gpp_destroy", "a2c_gpp_stream", "a2c_gpp_set_precision", "a2c_gpp_synchronize", "a2c_gpp_set_occupancy",
             "a2c_gpp_get_occupancy", "a2c_gpp_set_state", "a2c_gpp_get_state", "a2c_gpp_build_neighbors",
             "a2c_gpp_neighbor_total", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
-            "a2c_gpp_eval_device", "a2c_gpp_get_density", "a2c_gpp_bounds", "a2c_gpp_minimize",
+            "a2c_gpp_eval_device", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
             "a2c_gpp_chem_potential", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",
             "a2c_lattice_fcc"]
 

@@ -204,6 +204,12 @@ a2c_status a2c_gpp_destroy(a2c_gpp_ctx *c) {
 
 void *a2c_gpp_stream(a2c_gpp_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
+a2c_status a2c_gpp_synchronize(a2c_gpp_ctx *c) {
+  if (!c) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  return finish(c);
+}
+
 a2c_status a2c_gpp_set_precision(a2c_gpp_ctx *c, int precision) {
   if (!c || (precision != A2C_FP64 && precision != A2C_MIXED)) return A2C_ERR_INVALID;
   c->p.precision = precision;
@@ -370,6 +376,21 @@ a2c_status a2c_gpp_get_density(a2c_gpp_ctx *c, double *rho) {
   if (!c->has_density) return A2C_ERR_STATE;
   DeviceGuard g(c->device);
   if (c->N > 0) A2C_CUDA(cudaMemcpyAsync(rho, c->d_rho, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+a2c_status a2c_gpp_eam_eval(a2c_gpp_ctx *c, int which, const double *in, int64_t n, double *out) {
+  if (!c || which < 0 || which > 13 || n < 0 || (n > 0 && (!in || !out))) return A2C_ERR_INVALID;
+  if (n == 0) return A2C_OK;
+  DeviceGuard g(c->device);
+  double *d = nullptr;
+  A2C_CUDA(cudaMallocAsync((void **)&d, sizeof(double) * 2 * n, c->stream));
+  a2c_status s = A2C_OK;
+  if (cudaMemcpyAsync(d, in, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream)) s = A2C_ERR_CUDA;
+  if (!s) s = launch_eam64(c, which, d, n, d + n);
+  if (!s && cudaMemcpyAsync(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream)) s = A2C_ERR_CUDA;
+  cudaFreeAsync(d, c->stream);
+  if (s) return s;
   return finish(c);
 }
 

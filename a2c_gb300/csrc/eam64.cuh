@@ -1,10 +1,13 @@
 // FP64 device restatement of the EAM Pd-H potential (potential.cpp:16-205,
 // Zhou et al. 2007), written in the reference's evaluation order so that the
-// plain form reproduces its bits.  Translation units including this header
+// plain form reproduces its bits.  exp is dd::fexp (0.5-ulp, the same bits
+// on host and device) and pow is dd::cr_pow (ddmath.cuh).  Translation units including this header
 // are compiled with -fmad=false: no multiply-add may be contracted into an
 // FMA, exactly as the reference's x86-64 build performs them.  The numeric
 // constants are the reference's; they define the potential.
 #pragma once
+
+#include "ddmath.cuh"
 
 namespace a2c {
 namespace eam64 {
@@ -25,12 +28,14 @@ __device__ __forceinline__ double F_Pd(double rho) {
   return y;
 }
 
-// potential.cpp:45-57
+// potential.cpp:45-57.  F_H is differentiated by a central difference, so
+// its three pow calls use the correctly rounded dd::cr_pow (a one-ulp pow
+// difference would otherwise become a ~1e-11 relative gradient error).
 __device__ __forceinline__ double F_H(double rho) {
   const double c = 0.000197047, d = 1.18860, a = 9.99780, b = 60.0155, eps1 = 0.0540638;
   const double u = rho + eps1;
-  double y = -c * (1.0 / (2.0 + d) * pow(u, 2.0 + d) - (a + b) / (1.0 + d) * pow(u, 1.0 + d) +
-                   a * b / d * pow(u, d));
+  double y = -c * (1.0 / (2.0 + d) * dd::cr_pow(u, 2.0 + d) - (a + b) / (1.0 + d) * dd::cr_pow(u, 1.0 + d) +
+                   a * b / d * dd::cr_pow(u, d));
   y = y - (-0.0296604) * rho;
   return y;
 }
@@ -50,15 +55,15 @@ __device__ __forceinline__ double f_Pd(double r) {
              r * (0.6676807403564453 + r * (-255.8965835571289 + r * (14673.409149169922 + -2.597301181336601e7 * ra)));
   const double r5 = r * 5.0;
   if (r5 <= 0.0) y = 0.0;
-  else if (r5 > 5.0) y = 0.001510569378297 * exp(-0.077976566126292 / 0.001510569378297 * (r5 - 5.0));
+  else if (r5 > 5.0) y = 0.001510569378297 * dd::fexp(-0.077976566126292 / 0.001510569378297 * (r5 - 5.0));
   return y;
 }
 
 // potential.cpp:105-119
 __device__ __forceinline__ double f_H(double r) {
   if (r <= 0.0) return 0.0;
-  if (r > 5.35) return 0.009986990526578 * exp(-0.013075667086408 / 0.009986990526578 * (r - 5.35));
-  return 11.0025 * exp(-1.30927 * r);
+  if (r > 5.35) return 0.009986990526578 * dd::fexp(-0.013075667086408 / 0.009986990526578 * (r - 5.35));
+  return 11.0025 * dd::fexp(-1.30927 * r);
 }
 
 // potential.cpp:126-155
@@ -75,24 +80,24 @@ __device__ __forceinline__ double phi_Pd(double r) {
   r = r * 5.0;
   y = y + (2 * 0.251546) * f_Pd(r);
   if (r <= 0.0) y = 0.0;
-  else if (r > 5.05) y = -0.016958780164980 * exp(0.089019679316328 / -0.016958780164980 * (r - 5.05));
+  else if (r > 5.05) y = -0.016958780164980 * dd::fexp(0.089019679316328 / -0.016958780164980 * (r - 5.05));
   return y;
 }
 
 // potential.cpp:162-177
 __device__ __forceinline__ double phi_PdH(double r) {
   if (r <= 0.0) return 0.0;
-  if (r > 5.35) return -3.353001113951400e-04 * exp(7.147062196813336e-04 / -3.353001113951400e-04 * (r - 5.35));
+  if (r > 5.35) return -3.353001113951400e-04 * dd::fexp(7.147062196813336e-04 / -3.353001113951400e-04 * (r - 5.35));
   const double D = 0.2494540, alpha = 4.82613, beta = 2.13158, r0 = 1.50964;
-  return D * (beta * exp(-alpha * (r - r0)) - alpha * exp(-beta * (r - r0)));
+  return D * (beta * dd::fexp(-alpha * (r - r0)) - alpha * dd::fexp(-beta * (r - r0)));
 }
 
 // potential.cpp:185-200
 __device__ __forceinline__ double phi_H(double r) {
   if (r <= 0.0) return 0.0;
-  if (r > 5.35) return -0.003702722457147 * exp(0.005465945471933 / -0.003702722457147 * (r - 5.35));
+  if (r > 5.35) return -0.003702722457147 * dd::fexp(0.005465945471933 / -0.003702722457147 * (r - 5.35));
   const double D = 0.0661496, alpha = 3.67263, beta = 1.47797, r0 = 2.51980;
-  return D * (beta * exp(-alpha * (r - r0)) - alpha * exp(-beta * (r - r0)));
+  return D * (beta * dd::fexp(-alpha * (r - r0)) - alpha * dd::fexp(-beta * (r - r0)));
 }
 
 // Central finite differences with step eps (potential.cpp:40, 59, 100, 121,

@@ -88,6 +88,7 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 // k_fp64.cu
 a2c_status launch_density64(a2c_gpp_ctx *c, const double *dX);
 a2c_status launch_gradient64(a2c_gpp_ctx *c, const double *dX, double *dG);
+a2c_status launch_eam64(a2c_gpp_ctx *c, int which, const double *d_in, int64_t n, double *d_out);
 a2c_status launch_chem64(a2c_gpp_ctx *c, const double *dX, double gamma_bd, double *d_send, const int *d_full);
 
 // k_misc.cu

@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(kBlock) k_gradient64(SiteArgs a) {
   a.G[4 * s + 2] = Fq[2] * cq;
   a.G[4 * s + 3] = Fs * cs - ce;
   a.Vs[s] = V;
-  a.Ss[s] = log(sigmai) * xi;
+  a.Ss[s] = dd::cr_log(sigmai) * xi;
   if (!isfinite(V) || !isfinite(Fs) || !isfinite(Fq[0] + Fq[1] + Fq[2])) atomicOr(a.status, kStatusNonfinite);
 }
 
@@ -304,7 +304,31 @@ __global__ void __launch_bounds__(kBlock) k_chem64(SiteArgs a, const double coeP
     for (int64_t u = mj; u < ej; ++u) sum = sum + (((xj * T) * coeH0) * coeH3) * a.occ[a.nbr[u] & kIdMask];
   }
   const double x0 = a.occ[s];
-  if (x0 > 0.0 && x0 < 1.0) send[h] = log(x0 / (1.0 - x0)) + sum / (kB * T);
+  if (x0 > 0.0 && x0 < 1.0) send[h] = dd::cr_log(x0 / (1.0 - x0)) + sum / (kB * T);
+}
+
+__global__ void k_eam64(int which, const double *in, int64_t n, double eps, double *out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = in[i];
+  double r;
+  switch (which) {
+    case 0: r = eam64::F_Pd(v); break;
+    case 1: r = eam64::F_Pd_d(v, eps); break;
+    case 2: r = eam64::F_H(v); break;
+    case 3: r = eam64::F_H_d(v, eps); break;
+    case 4: r = eam64::f_Pd(v); break;
+    case 5: r = eam64::f_Pd_d(v, eps); break;
+    case 6: r = eam64::f_H(v); break;
+    case 7: r = eam64::f_H_d(v, eps); break;
+    case 8: r = eam64::phi_Pd(v); break;
+    case 9: r = eam64::phi_Pd_d(v, eps); break;
+    case 10: r = eam64::phi_PdH(v); break;
+    case 11: r = eam64::phi_PdH_d(v, eps); break;
+    case 12: r = eam64::phi_H(v); break;
+    default: r = eam64::phi_H_d(v, eps); break;
+  }
+  out[i] = r;
 }
 
 SiteArgs site_args(a2c_gpp_ctx *c, const double *dX) {
@@ -344,6 +368,13 @@ a2c_status launch_gradient64(a2c_gpp_ctx *c, const double *dX, double *dG) {
   SiteArgs a = site_args(c, dX);
   a.G = dG;
   k_gradient64<<<grid_for(c->N, kBlock), kBlock, 0, c->stream>>>(a);
+  A2C_CUDA(cudaGetLastError());
+  return A2C_OK;
+}
+
+a2c_status launch_eam64(a2c_gpp_ctx *c, int which, const double *d_in, int64_t n, double *d_out) {
+  if (n <= 0) return A2C_OK;
+  k_eam64<<<grid_for(n, 256), 256, 0, c->stream>>>(which, d_in, n, c->p.eps, d_out);
   A2C_CUDA(cudaGetLastError());
   return A2C_OK;
 }

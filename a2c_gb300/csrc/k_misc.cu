@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "ddmath.cuh"
 #include "internal.cuh"
 
 namespace a2c {
@@ -108,12 +109,13 @@ __global__ void k_diffuse(const double *x0, const int64_t *hh1_off, const int *h
   if (i >= nH || full[i] == 1) return;
   const double xi = x0[i];
   double x_deriv = 0.0;
-  const double fi = gamma[i] - log(xi / (1.0 - xi));
+  // per-site logs and exps use the correctly rounded dd:: forms (cheap here)
+  const double fi = gamma[i] - dd::cr_log(xi / (1.0 - xi));
   for (int64_t t = hh1_off[i]; t < hh1_off[i + 1]; ++t) {
     const int j = hh1[t];
     const double xj = x0[j];
-    const double fj = gamma[j] - log(xj / (1.0 - xj));
-    x_deriv = x_deriv + (xj * (1.0 - xi) * exp(-(fi - fj) / 2.0) - xi * (1.0 - xj) * exp((fi - fj) / 2.0));
+    const double fj = gamma[j] - dd::cr_log(xj / (1.0 - xj));
+    x_deriv = x_deriv + (xj * (1.0 - xi) * dd::cr_exp(-(fi - fj) / 2.0) - xi * (1.0 - xj) * dd::cr_exp((fi - fj) / 2.0));
   }
   double v = xi + prefactor * x_deriv * dt;
   if (v < xLb) v = xLb;

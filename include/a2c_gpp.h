@@ -104,6 +104,8 @@ a2c_status a2c_gpp_destroy(a2c_gpp_ctx *ctx);
 /* The context's CUDA stream, as a cudaStream_t cast to void*. */
 void *a2c_gpp_stream(a2c_gpp_ctx *ctx);
 a2c_status a2c_gpp_set_precision(a2c_gpp_ctx *ctx, int precision);
+/* Waits for all work queued on the context's stream (for _device calls). */
+a2c_status a2c_gpp_synchronize(a2c_gpp_ctx *ctx);
 
 /* H occupancy x0 used by every later call; replaces the x0 pointer swap of
  * Minimizer::updateApplicationContext (minimizer.cpp:372-378). */
@@ -136,6 +138,13 @@ a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, d
 /* Site electron densities of the last evaluation, all Pd then all H
  * (electrondensity.cpp:12-56, the reference's recv_Pd / recv_H). */
 a2c_status a2c_gpp_get_density(a2c_gpp_ctx *ctx, double *rho);
+
+/* Known-answer access to the device EAM functions (potential.cpp:16-205):
+ * evaluates function `which` (0 F_Pd, 1 F_Pd_deriv, 2 F_H, 3 F_H_deriv,
+ * 4 f_Pd, 5 f_Pd_deriv, 6 f_H, 7 f_H_deriv, 8 phi_Pd, 9 phi_Pd_deriv,
+ * 10 phi_PdH, 11 phi_PdH_deriv, 12 phi_H, 13 phi_H_deriv) of the FP64 plain
+ * form on the context's device, host arrays in and out, step = params eps. */
+a2c_status a2c_gpp_eam_eval(a2c_gpp_ctx *ctx, int which, const double *in, int64_t n, double *out);
 
 /* Variable bounds: q free, sigma >= 1e-6 (minimizer.cpp:804-830). */
 a2c_status a2c_gpp_bounds(a2c_gpp_ctx *ctx, double *lb, double *ub);

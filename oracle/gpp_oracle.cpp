@@ -12,9 +12,65 @@
 #include <omp.h>
 #endif
 
+#include "../a2c_gb300/csrc/ddmath.cuh"
+
 namespace {
 
 const double kB = 8.6173324e-5;  // minimizer.cpp:92
+
+// Arithmetic mode.  0 (default): the reference's arithmetic -- the C
+// library's exp/pow/log and sequential sums; this mode is pinned bit for bit
+// to the reference's own sources.  1: the device's arithmetic -- the
+// portable exp/pow/log of ddmath.cuh (dd::fexp in the EAM functions,
+// dd::cr_pow, dd::cr_log, dd::cr_exp in the diffusion step) and the GPU's
+// fixed reduction tree for global sums and L-BFGS dot products; in this mode
+// the GPU plain form reproduces the oracle bit for bit.
+int g_arith = 0;
+inline double e_exp(double x) { return g_arith ? a2c::dd::fexp(x) : std::exp(x); }
+inline double e_pow(double u, double y) { return g_arith ? a2c::dd::cr_pow(u, y) : std::pow(u, y); }
+inline double x_log(double u) { return g_arith ? a2c::dd::cr_log(u) : std::log(u); }
+inline double d_exp(double x) { return g_arith ? a2c::dd::cr_exp(x) : std::exp(x); }
+
+// The GPU's deterministic reduction: `grid` blocks of 256 threads, thread t
+// of block b sums terms b*256+t, +grid*256, ... from 0.0; each warp then
+// combines lanes pairwise at strides 16, 8, 4, 2, 1 (lane 0's value is
+// kept); warp results 0..7 are combined the same way (zero-padded); a final
+// block of 256 threads sums the block partials strided by 256 and combines
+// them by the same tree.
+double warp_tree(double v[32]) {
+  for (int o = 16; o > 0; o >>= 1)
+    for (int i = 0; i < o; ++i) v[i] = v[i] + v[i + o];
+  return v[0];
+}
+double block_tree(const double lane[256]) {
+  double w[32] = {0.0};
+  for (int k = 0; k < 8; ++k) {
+    double v[32];
+    for (int i = 0; i < 32; ++i) v[i] = lane[32 * k + i];
+    w[k] = warp_tree(v);
+  }
+  return warp_tree(w);
+}
+template <class Term>
+double gpu_tree_sum(int64_t n, int maxgrid, Term term) {
+  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(maxgrid, (n + 255) / 256));
+  std::vector<double> part((size_t)grid);
+  double lane[256];
+  for (int64_t b = 0; b < grid; ++b) {
+    for (int t = 0; t < 256; ++t) {
+      double s = 0.0;
+      for (int64_t i = b * 256 + t; i < n; i += grid * 256) s += term(i);
+      lane[t] = s;
+    }
+    part[(size_t)b] = block_tree(lane);
+  }
+  for (int t = 0; t < 256; ++t) {
+    double s = 0.0;
+    for (int64_t i = t; i < grid; i += 256) s += part[(size_t)i];
+    lane[t] = s;
+  }
+  return block_tree(lane);
+}
 
 // --------------------------------------------------------------------------
 // Vec3D arithmetic, in the order of Vector3D.h:83 (norm), 281-286 (dot),
@@ -61,9 +117,9 @@ struct Eam {
   // potential.cpp:45-57
   double F_H(double rho) const {
     const double c = 0.000197047, d = 1.18860, a = 9.99780, b = 60.0155, eps1 = 0.0540638;
-    double y = -c * (1.0 / (2.0 + d) * std::pow(rho + eps1, 2.0 + d) -
-                     (a + b) / (1.0 + d) * std::pow(rho + eps1, 1.0 + d) +
-                     a * b / d * std::pow(rho + eps1, d));
+    double y = -c * (1.0 / (2.0 + d) * e_pow(rho + eps1, 2.0 + d) -
+                     (a + b) / (1.0 + d) * e_pow(rho + eps1, 1.0 + d) +
+                     a * b / d * e_pow(rho + eps1, d));
     const double Fprime = -0.0296604;
     y -= Fprime * rho;
     return y;
@@ -90,7 +146,7 @@ struct Eam {
     if (r * 5.0 <= 0.0)
       y = 0.0;
     else if (r * 5.0 > 5.0)
-      y = funRc * std::exp(funDerivRc / funRc * (r * 5.0 - 5.0));
+      y = funRc * e_exp(funDerivRc / funRc * (r * 5.0 - 5.0));
     return y;
   }
   double f_Pd_deriv(double r) const { return (f_Pd(r + eps) - f_Pd(r - eps)) / (2.0 * eps); }
@@ -100,8 +156,8 @@ struct Eam {
     const double funRc = 0.009986990526578, funDerivRc = -0.013075667086408;
     const double C = 11.0025, delta = 1.30927;
     if (r <= 0.0) return 0.0;
-    if (r > 5.35) return funRc * std::exp(funDerivRc / funRc * (r - 5.35));
-    return C * std::exp(-delta * r);
+    if (r > 5.35) return funRc * e_exp(funDerivRc / funRc * (r - 5.35));
+    return C * e_exp(-delta * r);
   }
   double f_H_deriv(double r) const { return (f_H(r + eps) - f_H(r - eps)) / (2.0 * eps); }
 
@@ -127,7 +183,7 @@ struct Eam {
     if (r <= 0.0)
       y = 0.0;
     else if (r > 5.05)
-      y = funRc * std::exp(funDerivRc / funRc * (r - 5.05));
+      y = funRc * e_exp(funDerivRc / funRc * (r - 5.05));
     return y;
   }
   double phi_Pd_deriv(double r) const { return (phi_Pd(r + eps) - phi_Pd(r - eps)) / (2.0 * eps); }
@@ -137,8 +193,8 @@ struct Eam {
     const double funRc = -3.353001113951400e-04, funDerivRc = 7.147062196813336e-04;
     const double D = 0.2494540, alpha = 4.82613, beta = 2.13158, r0 = 1.50964;
     if (r <= 0.0) return 0.0;
-    if (r > 5.35) return funRc * std::exp(funDerivRc / funRc * (r - 5.35));
-    return D * (beta * std::exp(-alpha * (r - r0)) - alpha * std::exp(-beta * (r - r0)));
+    if (r > 5.35) return funRc * e_exp(funDerivRc / funRc * (r - 5.35));
+    return D * (beta * e_exp(-alpha * (r - r0)) - alpha * e_exp(-beta * (r - r0)));
   }
   double phi_PdH_deriv(double r) const { return (phi_PdH(r + eps) - phi_PdH(r - eps)) / (2.0 * eps); }
 
@@ -147,8 +203,8 @@ struct Eam {
     const double funRc = -0.003702722457147, funDerivRc = 0.005465945471933;
     const double D = 0.0661496, alpha = 3.67263, beta = 1.47797, r0 = 2.51980;
     if (r <= 0.0) return 0.0;
-    if (r > 5.35) return funRc * std::exp(funDerivRc / funRc * (r - 5.35));
-    return D * (beta * std::exp(-alpha * (r - r0)) - alpha * std::exp(-beta * (r - r0)));
+    if (r > 5.35) return funRc * e_exp(funDerivRc / funRc * (r - 5.35));
+    return D * (beta * e_exp(-alpha * (r - r0)) - alpha * e_exp(-beta * (r - r0)));
   }
   double phi_H_deriv(double r) const { return (phi_H(r + eps) - phi_H(r - eps)) / (2.0 * eps); }
 };
@@ -326,7 +382,7 @@ void gradient_site(const Eam &eam, const Lists &L, const double *X, const double
     for (int c = 0; c < 3; ++c) Fq.v[c] *= 1.0 / T;   // minimizer.cpp:220-223
     Fs *= 1.0 / T * std::sqrt(2.0);
     Fs -= 3.0 * kB / sigmai;
-    *S += std::log(sigmai);
+    *S += x_log(sigmai);
   } else {
     *V += xi * eam.F_H(rhoi);
     for (int64_t t = b; t < m; ++t) {  // H-Pd, minimizer.cpp:234-256
@@ -365,7 +421,7 @@ void gradient_site(const Eam &eam, const Lists &L, const double *X, const double
     for (int c = 0; c < 3; ++c) Fq.v[c] *= 1.0 / T * xi;   // minimizer.cpp:282-285
     Fs *= 1.0 / T * std::sqrt(2.0) * xi;
     Fs -= 3.0 * kB / sigmai * xi;
-    *S += std::log(sigmai) * xi;
+    *S += x_log(sigmai) * xi;
   }
   G[4 * s] = Fq.v[0];
   G[4 * s + 1] = Fq.v[1];
@@ -409,9 +465,14 @@ int eval_impl(const orc_params *p, const double *X, const double *xH, const int6
       Vs[(size_t)s] = v;
       Ss[(size_t)s] = sg;
     }
-    for (int64_t s = 0; s < N; ++s) {
-      sum_V += Vs[(size_t)s];
-      sum_sigma += Ss[(size_t)s];
+    if (g_arith) {
+      sum_V = gpu_tree_sum(N, 1024, [&](int64_t i) { return Vs[(size_t)i]; });
+      sum_sigma = gpu_tree_sum(N, 1024, [&](int64_t i) { return Ss[(size_t)i]; });
+    } else {
+      for (int64_t s = 0; s < N; ++s) {
+        sum_V += Vs[(size_t)s];
+        sum_sigma += Ss[(size_t)s];
+      }
     }
     if (Vsite) std::memcpy(Vsite, Vs.data(), sizeof(double) * (size_t)N);
   }
@@ -553,6 +614,9 @@ void site_neighbors(const orc_params *p, const Grid &g, const double *X, int64_t
 }  // namespace
 
 extern "C" {
+
+void orc_set_arith(int mode) { g_arith = mode ? 1 : 0; }
+int orc_get_arith(void) { return g_arith; }
 
 void orc_eam(int which, const double *in, int64_t n, double eps, double *out) {
   Eam e{eps};
@@ -723,7 +787,7 @@ int orc_chem_potential(const orc_params *p, const double *X, const double *xH, c
       for (int64_t u = mj; u < off[jj + 1]; ++u) sum_Vx += xj * T * coe_H[0] * coe_H[3] * xall[nbr[u] & ID_MASK];
     }
     const double x0 = xH[i];
-    if (x0 > 0.0 && x0 < 1.0) send[(size_t)i] = std::log(x0 / (1.0 - x0)) + sum_Vx / (kB * T);
+    if (x0 > 0.0 && x0 < 1.0) send[(size_t)i] = x_log(x0 / (1.0 - x0)) + sum_Vx / (kB * T);
   }
   for (int i = 0; i < nH; ++i) {  // minimizer.cpp:793-800
     if (full_H[i] == 1) continue;
@@ -744,12 +808,12 @@ int orc_diffuse(int nH, const double *x0, const int64_t *hh1_off, const int *hh1
   for (int i = 0; i < nH; ++i) {
     if (full_H[i] == 1) continue;
     double x_deriv = 0.0;
-    const double fi = gamma[i] - std::log(x0[i] / (1.0 - x0[i]));
+    const double fi = gamma[i] - x_log(x0[i] / (1.0 - x0[i]));
     for (int64_t t = hh1_off[i]; t < hh1_off[i + 1]; ++t) {
       const int j = hh1[t];
-      const double fj = gamma[j] - std::log(x0[j] / (1.0 - x0[j]));
-      x_deriv += x0[j] * (1.0 - x0[i]) * std::exp(-(fi - fj) / 2.0) -
-                 x0[i] * (1.0 - x0[j]) * std::exp((fi - fj) / 2.0);
+      const double fj = gamma[j] - x_log(x0[j] / (1.0 - x0[j]));
+      x_deriv += x0[j] * (1.0 - x0[i]) * d_exp(-(fi - fj) / 2.0) -
+                 x0[i] * (1.0 - x0[j]) * d_exp((fi - fj) / 2.0);
     }
     send[(size_t)i] = x0[i] + prefactor * x_deriv * dt;
   }
@@ -799,6 +863,7 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
       if (v[(size_t)t] < lb) v[(size_t)t] = lb;
   };
   auto dotv = [&](const std::vector<double> &a, const std::vector<double> &b) {
+    if (g_arith) return gpu_tree_sum(n, 512, [&](int64_t t) { return a[(size_t)t] * b[(size_t)t]; });
     double s = 0.0;
     for (int64_t t = 0; t < n; ++t) s += a[(size_t)t] * b[(size_t)t];
     return s;
@@ -868,7 +933,10 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
       project(xn);
       if (F(xn, &fn, gn)) return 1;
       double dec = 0.0;
-      for (int64_t t = 0; t < n; ++t) dec += g[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]);
+      if (g_arith)
+        dec = gpu_tree_sum(n, 512, [&](int64_t t) { return g[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]); });
+      else
+        for (int64_t t = 0; t < n; ++t) dec += g[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]);
       if (std::isfinite(fn) && fn <= f + lp->c1 * dec) { ok = true; break; }
       alpha *= 0.5;
       if (nfev >= lp->max_fev) break;

@@ -58,6 +58,12 @@ typedef struct orc_lbfgs {
   double sigma_lb;  /* lower bound on widths */
 } orc_lbfgs;
 
+/* Arithmetic mode: 0 = the reference's (C library exp/pow/log, sequential
+ * sums; the default, pinned to the reference); 1 = the device's (portable
+ * exp/pow/log of a2c_gb300/csrc/ddmath.cuh and the GPU reduction tree). */
+void orc_set_arith(int mode);
+int orc_get_arith(void);
+
 /* EAM function by id (see gpp_oracle.cpp: 0..13), applied elementwise. */
 void orc_eam(int which, const double *in, int64_t n, double eps, double *out);
 

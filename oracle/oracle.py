@@ -59,6 +59,8 @@ def olib() -> C.CDLL:
         if not ORACLE_SO.exists():
             build(ref=False)
         L = C.CDLL(str(ORACLE_SO))
+        L.orc_set_arith.argtypes = [I]
+        L.orc_set_arith.restype = None
         L.orc_eam.argtypes = [I, P, I64, D, P]
         L.orc_neighbor_counts.argtypes = [C.POINTER(OrcParams), P, P, P]
         L.orc_neighbor_fill.argtypes = [C.POINTER(OrcParams), P, P, P, P, P, P]
@@ -74,6 +76,22 @@ def olib() -> C.CDLL:
                                    C.POINTER(I), C.POINTER(I), C.POINTER(D), C.POINTER(I)]
         _olib = L
     return _olib
+
+
+class arithmetic:
+    """Context manager selecting the oracle's arithmetic: "reference" (the C
+    library and sequential sums, pinned to the reference) or "device" (the
+    portable exp/pow/log and the GPU reduction tree)."""
+
+    def __init__(self, mode: str):
+        self.mode = {"reference": 0, "device": 1}[mode]
+
+    def __enter__(self):
+        olib().orc_set_arith(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        olib().orc_set_arith(0)
 
 
 def ref_available() -> bool:

@@ -1,0 +1,289 @@
+"""GPU parity of the FP64 plain form against the CPU oracle (which is itself
+pinned bit-for-bit to the reference's own sources in test_oracle_pin.py).
+
+Two comparisons per quantity:
+  * against the oracle in the reference's arithmetic (the C library's
+    exp/pow/log, sequential sums): objective and gradient to 1e-11 relative
+    (gradient in the 2-norm), the limit stated for the plain form -- a
+    one-ulp exp/pow difference is amplified ~1e5x by the reference's
+    finite-difference derivatives;
+  * against the oracle in the device's arithmetic (the same portable
+    exp/pow/log, the GPU's reduction tree): bit for bit, including whole
+    L-BFGS trajectories.
+Neighbor sets, shell counts and first-shell lists are bit-exact.
+"""
+import numpy as np
+import pytest
+
+import a2c_gb300 as A
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_F = 1e-11
+TOL_G = 1e-11
+
+CASES = {
+    # name: (ncell, periodic, pos_std, sigma range, x_center, x_half, seed)
+    "free3": ((3, 3, 3), (0, 0, 0), 0.02, (0.10, 0.10), 0.05, 0.01, 1),
+    "config1_6cube": ((6, 6, 6), (1, 1, 1), 0.02, (0.10, 0.10), 0.05, 0.01, 1),
+    "slab_4x5x6": ((4, 5, 6), (1, 1, 0), 0.03, (0.08, 0.14), 0.15, 0.15, 7),
+    "config2_16cube": ((16, 16, 16), (1, 1, 1), 0.03, (0.08, 0.14), 0.15, 0.15, 2),
+}
+
+
+def make(case):
+    ncell, per, ps, sg, xc, xh, seed = CASES[case]
+    X, xH, surf, box, nPd, nH = A.lattice_fcc(ncell, periodic=per, pos_std=ps, sigma=sg, x_center=xc, x_half=xh,
+                                             seed=seed)
+    pb = O.Problem(nPd, nH, box=box, periodic=per)
+    return X, xH, surf, box, per, nPd, nH, pb
+
+
+def gpp(nPd, nH, box, per, **kw):
+    return A.Gpp(nPd, nH, box=box, periodic=per, **kw)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_neighbor_sets_exact(gpu, case):
+    X, xH, surf, box, per, nPd, nH, pb = make(case)
+    off, nbr, shell, off1, hh1 = O.neighbors(pb, X)
+    want = O.split_lists(nPd, nH, off, nbr)
+    with gpp(nPd, nH, box, per) as g:
+        maxn = g.build_neighbors(X)
+        assert maxn == int(np.diff(off).max())
+        for lid, name in enumerate(("PdPd", "PdH", "HPd", "HH")):
+            go, gi = g.neighbors(lid)
+            wo, wi = want[name]
+            assert np.array_equal(go, wo), name
+            assert np.array_equal(gi, wi), name
+        go, gi = g.neighbors(4)
+        assert np.array_equal(go, off1) and np.array_equal(gi, hh1)
+        assert np.array_equal(g.shell_counts(), shell)
+
+
+def test_bulk_coordination(gpu):
+    """Perfect periodic fcc crystal: 42 same-species and 38 cross-species
+    neighbors within 5.35 A, 12 first-shell H neighbors, Pd shells 12/6/24."""
+    X, xH, _, box, nPd, nH = A.lattice_fcc(5, periodic=(1, 1, 1), pos_std=0.0, seed=3)
+    with gpp(nPd, nH, box, (1, 1, 1)) as g:
+        assert g.build_neighbors(X) == 80
+        for lid, n in ((0, 42), (1, 38), (2, 38), (3, 42)):
+            o, _ = g.neighbors(lid)
+            assert np.all(np.diff(o) == n)
+        o, _ = g.neighbors(4)
+        assert np.all(np.diff(o) == 12)
+        sh = g.shell_counts()
+        assert np.all(sh == np.array([12, 6, 24]))
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_objective_gradient_fp64(gpu, case):
+    X, xH, surf, box, per, nPd, nH, pb = make(case)
+    off, nbr, *_ = O.neighbors(pb, X)
+    f_ref, G_ref, rho_ref, _ = O.evaluate(pb, X, xH, off, nbr, mode=1)
+    with O.arithmetic("device"):
+        f_dev, G_dev, rho_dev, _ = O.evaluate(pb, X, xH, off, nbr, mode=1)
+    with gpp(nPd, nH, box, per) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        f, G = g.eval(X)
+        rho = g.density()
+    rel_f = abs(f - f_ref) / abs(f_ref)
+    rel_g = np.linalg.norm(G - G_ref) / np.linalg.norm(G_ref)
+    rel_rho = np.max(np.abs(rho - rho_ref) / np.maximum(np.abs(rho_ref), 1e-300))
+    print(f"{case}: vs reference arithmetic rel_f={rel_f:.3e} rel_G={rel_g:.3e} max_rel_rho={rel_rho:.3e}; "
+          f"vs device arithmetic: f {'==' if f == f_dev else '!='}, G equal {np.array_equal(G, G_dev)}, "
+          f"rho equal {np.array_equal(rho, rho_dev)}")
+    assert rel_rho < 1e-13
+    assert rel_f < TOL_F
+    assert rel_g < TOL_G
+    assert np.array_equal(rho, rho_dev)
+    assert np.array_equal(G, G_dev)
+    assert f == f_dev
+
+
+def test_eval_device_pointers(gpu):
+    """The stream-ordered device entry point gives the host entry point's
+    results bit for bit."""
+    import torch
+
+    X, xH, surf, box, per, nPd, nH, pb = make("slab_4x5x6")
+    with gpp(nPd, nH, box, per) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        f, G = g.eval(X)
+        dX = torch.tensor(X, device="cuda")
+        dG = torch.empty_like(dX)
+        df = torch.empty(1, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        g.eval_device(dX.data_ptr(), df.data_ptr(), dG.data_ptr())
+        g.synchronize()
+        assert df.item() == f
+        assert np.array_equal(dG.cpu().numpy(), G)
+
+
+def test_chem_potential_fp64(gpu):
+    X, xH, surf, box, per, nPd, nH, pb = make("slab_4x5x6")
+    pb2 = O.Problem(nPd, nH, box=box, periodic=per, coe_Pd=(0.3, 0.0, 0.02, -0.01), coe_H=(0.2, 0.01, -0.03, 0.004))
+    off, nbr, *_ = O.neighbors(pb2, X)
+    rng = np.random.default_rng(5)
+    gamma0 = rng.normal(size=nH)
+    full0 = (rng.random(nH) < 0.1).astype(np.int32)
+    xH = xH.copy()
+    xH[:5] = [0.0, 1.0, 0.99995, 0.5, 0.2]
+    g_ref, f_ref = O.chem_potential(pb2, X, xH, off, nbr, 2.5, gamma0, full0)
+    with O.arithmetic("device"):
+        g_dev, f_dev = O.chem_potential(pb2, X, xH, off, nbr, 2.5, gamma0, full0)
+    with gpp(nPd, nH, box, per, coe_Pd=(0.3, 0.0, 0.02, -0.01), coe_H=(0.2, 0.01, -0.03, 0.004)) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        gg, ff = g.chem_potential(2.5, gamma0, full0)
+    assert np.array_equal(ff, f_ref) and np.array_equal(ff, f_dev)
+    assert np.array_equal(gg, g_dev)
+    err = np.abs(gg - g_ref) / np.maximum(np.abs(g_ref), 1.0)
+    print(f"chem potential max rel err {err.max():.3e}")
+    assert err.max() < 1e-11
+
+
+def test_dirichlet_diffusion_macro(gpu):
+    X, xH, surf, box, per, nPd, nH, pb = make("slab_4x5x6")
+    off, nbr, shell, off1, hh1 = O.neighbors(pb, X)
+    sites = np.nonzero(surf)[0].astype(np.int32)
+    rng = np.random.default_rng(11)
+    gamma0 = rng.normal(size=nH) * 0.3
+    full0 = np.zeros(nH, dtype=np.int32)
+    x0_ref, g_ref, f_ref = O.dirichlet(sites, 4.0, 1 - 1e-16, xH, gamma0, full0)
+    T, dt, nu, Qm, xLb, xUb = 300.0, 1e-13, 1e13, 0.23, 1e-3, 1 - 1e-16
+    xprev = np.full(nH, 0.123)
+    x_ref = O.diffuse(nH, x0_ref, off1, hh1, g_ref, f_ref, T, dt, nu, Qm, xLb, xUb, xprev)
+    with O.arithmetic("device"):
+        x_dev = O.diffuse(nH, x0_ref, off1, hh1, g_ref, f_ref, T, dt, nu, Qm, xLb, xUb, xprev)
+    a_ref, b_ref = O.macro_results(x_ref, sites)
+    with gpp(nPd, nH, box, per) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        gg, ff = g.apply_dirichlet(sites, 4.0, 1 - 1e-16, gamma0, full0)
+        assert np.array_equal(ff, f_ref) and np.array_equal(gg, g_ref)
+        assert np.array_equal(g.occupancy(), x0_ref)
+        x = g.diffuse(dt, nu, Qm, xLb, xUb, gg, ff, xprev)
+        a, b = g.macro_results(x, sites)
+    assert np.array_equal(x[ff == 1], xprev[ff == 1])
+    assert np.array_equal(x, x_dev)
+    err = np.max(np.abs(x - x_ref))
+    print(f"diffusion max abs err {err:.3e}")
+    assert err < 1e-13
+    assert abs(a - a_ref) < 1e-13 and abs(b - b_ref) < 1e-13
+
+
+def test_diffusion_conserves_h(gpu):
+    """Without Dirichlet sites and with no clamp active, the hop flux is
+    antisymmetric: total H is conserved to rounding."""
+    X, xH, _, box, nPd, nH = A.lattice_fcc(6, periodic=(1, 1, 1), pos_std=0.02, x_center=0.3, x_half=0.2, seed=4)
+    with gpp(nPd, nH, box, (1, 1, 1)) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        gamma = np.log(xH / (1 - xH)) + 0.5 * np.sin(np.arange(nH))
+        x = g.diffuse(1e-14, 1e13, 0.23, 1e-6, 1 - 1e-16, gamma, np.zeros(nH, np.int32), xH)
+    assert abs(x.sum() - xH.sum()) < 1e-10 * xH.sum()
+    assert np.abs(x - xH).max() > 1e-6
+
+
+@pytest.mark.parametrize("case", ["free3", "config1_6cube"])
+def test_minimize_fp64_matches_oracle(gpu, case):
+    """The same projected L-BFGS on both sides in the same arithmetic: the
+    GPU reproduces the oracle's iterate sequence, so the converged state
+    matches to 1e-8 A (positions) and 1e-10 (widths) -- here bit for bit."""
+    X, xH, surf, box, per, nPd, nH, pb = make(case)
+    off, nbr, *_ = O.neighbors(pb, X)
+    kw = dict(m=5, max_it=400, gatol=1e-6)
+    with O.arithmetic("device"):
+        r_ref = O.minimize(pb, X, xH, off, nbr, **kw)
+    with gpp(nPd, nH, box, per) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        r = g.minimize(X, **kw)
+    print(f"oracle: it={r_ref['iters']} fev={r_ref['nfev']} f={r_ref['fmin']:.15e} reason={r_ref['reason']}; "
+          f"gpu: it={r.iters} fev={r.nfev} f={r.fmin:.15e} reason={r.reason}")
+    assert r_ref["reason"] == r.reason and r.reason in (3, -2)
+    assert r_ref["iters"] == r.iters and r_ref["nfev"] == r.nfev
+    dq = np.abs(r.X.reshape(-1, 4)[:, :3] - r_ref["X"].reshape(-1, 4)[:, :3]).max()
+    ds = np.abs(r.X.reshape(-1, 4)[:, 3] - r_ref["X"].reshape(-1, 4)[:, 3]).max()
+    print(f"max |dq|={dq:.3e} A, max |dsigma|={ds:.3e}")
+    assert dq < 1e-8 and ds < 1e-10
+    assert abs(r.fmin - r_ref["fmin"]) <= 1e-11 * abs(r_ref["fmin"])
+
+
+def test_error_paths(gpu):
+    X, xH, surf, box, per, nPd, nH, pb = make("free3")
+    with gpp(nPd, nH, box, per) as g:
+        with pytest.raises(A.A2CError) as e:
+            g.eval(X)
+        assert e.value.status == 6  # neighbors not built
+        g.build_neighbors(X)
+        Xb = X.copy()
+        Xb[7] = np.nan
+        with pytest.raises(A.A2CError) as e:
+            g.eval(Xb)
+        assert e.value.status == 5
+        with pytest.raises(A.A2CError) as e:
+            g.apply_dirichlet(np.array([nH + 3]), 1.0, 1.0, np.zeros(nH), np.zeros(nH, np.int32))
+        assert e.value.status == 1
+        f, G = g.eval(X)  # the context stays usable after rejected calls
+        assert np.isfinite(f)
+    with pytest.raises(A.A2CError):
+        A.Gpp(10, 10, box=(8.0, 8.0, 8.0), periodic=(1, 1, 1))  # box < 2 rc
+
+
+def test_isolated_and_empty(gpu):
+    """A site with no neighbors contributes F(0) and the width entropy only;
+    an empty problem evaluates to zero."""
+    X = np.array([0.0, 0.0, 0.0, 0.1, 20.0, 0.0, 0.0, 0.12])
+    xH = np.array([0.4])
+    pb = O.Problem(1, 1)
+    off, nbr, *_ = O.neighbors(pb, X)
+    f_ref, G_ref, _, _ = O.evaluate(pb, X, xH, off, nbr, mode=1, threads=1)
+    with A.Gpp(1, 1) as g:
+        g.set_occupancy(xH)
+        assert g.build_neighbors(X) == 0
+        f, G = g.eval(X)
+    assert abs(f - f_ref) <= 1e-12 * abs(f_ref)
+    assert np.allclose(G, G_ref, rtol=1e-12, atol=0)
+    with A.Gpp(0, 0) as g:
+        g.build_neighbors(np.zeros(0))
+        f, G = g.eval(np.zeros(0))
+        assert f == 0.0 and G.size == 0
+
+
+def test_eam_known_answers(gpu):
+    """Device EAM functions against the reference's own values
+    (golden_eam.npz, made by the reference's potential.cpp) and against the
+    oracle in the device arithmetic.  Against the oracle: bit for bit.
+    Against the reference: polynomial branches bit for bit; exp/pow branches
+    within a few ulp; the FD derivatives within the bound a few-ulp
+    difference of the differenced function gives, k * ulp(g) / (2 eps)."""
+    from pathlib import Path
+
+    gold = np.load(Path(__file__).resolve().parent / "golden" / "golden_eam.npz")
+    eps = 1e-5
+    with A.Gpp(1, 1) as g:
+        for w, name in enumerate(O.EAM_FUNCS):
+            x = gold["rho"] if name.startswith("F_") else gold["r"]
+            got = g.eam(w, x)
+            want = gold[name]
+            with O.arithmetic("device"):
+                assert np.array_equal(got, O.eam(w, x)), name
+            if name == "F_Pd":
+                assert np.array_equal(got, want), name
+            elif name.endswith("_deriv"):
+                base = O.eam(w - 1, x + eps)
+                bound = 8 * np.spacing(np.maximum(np.abs(base), np.abs(O.eam(w - 1, x - eps)))) / (2 * eps)
+                assert np.all(np.abs(got - want) <= bound + 1e-300), name
+            elif name == "F_H":  # three pows with cancellation: a pow ulp is many F_H ulps
+                assert np.max(np.abs(got - want) / np.abs(want)) < 1e-13, name
+            else:
+                ulps = np.abs(got - want) / np.spacing(np.maximum(np.abs(want), 1e-300))
+                assert np.max(ulps[np.abs(want) > 1e-300]) <= 2.0, name
+                if name in ("f_Pd", "phi_Pd"):  # polynomial branch: no libm call at all
+                    poly = (x > 0) & (x <= (5.0 if name == "f_Pd" else 4.5))
+                    assert np.array_equal(got[poly], want[poly]), name
