@@ -15,7 +15,7 @@ import numpy as np
 from . import _native as N
 from ._native import A2CError, A2C_FP64, A2C_MIXED  # noqa: F401
 
-__all__ = ["Gpp", "lattice_fcc", "A2CError", "A2C_FP64", "A2C_MIXED", "LbfgsResult"]
+__all__ = ["Gpp", "lattice_fcc", "peak_flops", "A2CError", "A2C_FP64", "A2C_MIXED", "LbfgsResult"]
 
 
 @dataclass
@@ -98,6 +98,9 @@ class Gpp:
     def stream(self) -> int:
         return int(self._L.a2c_gpp_stream(self._h) or 0)
 
+    def set_threads_per_site(self, tps: int) -> None:
+        N.check(self._L.a2c_gpp_set_threads_per_site(self._h, int(tps)), "a2c_gpp_set_threads_per_site")
+
     def synchronize(self) -> None:
         N.check(self._L.a2c_gpp_synchronize(self._h), "a2c_gpp_synchronize")
 
@@ -159,6 +162,13 @@ class Gpp:
         N.check(self._L.a2c_gpp_eval_device(self._h, C.c_void_p(dX), C.c_void_p(df), C.c_void_p(dG)),
                 "a2c_gpp_eval_device")
 
+    def profile_eval(self, dX: int, df: int, dG: int) -> np.ndarray:
+        """Stage durations [ms] of one evaluation: prep, pass 1, pass 2, reduce."""
+        ms = np.zeros(4, dtype=np.float32)
+        N.check(self._L.a2c_gpp_profile_eval(self._h, C.c_void_p(dX), C.c_void_p(df), C.c_void_p(dG), N.ptr(ms)),
+                "a2c_gpp_profile_eval")
+        return ms
+
     def density(self) -> np.ndarray:
         r = np.empty(self.N)
         N.check(self._L.a2c_gpp_get_density(self._h, N.ptr(r)), "a2c_gpp_get_density")
@@ -218,6 +228,15 @@ class Gpp:
         N.check(self._L.a2c_gpp_macro_results(self._h, N.ptr(x), N.ptr(hs) if hs.size else None, int(hs.size),
                                               C.byref(a), C.byref(b)), "a2c_gpp_macro_results")
         return a.value, b.value
+
+
+def peak_flops(precision: int | str = A2C_MIXED, device: int = 0) -> float:
+    """Measured FMA-pipe peak (flop/s) of FP32 ("mixed") or FP64 ("fp64")."""
+    if isinstance(precision, str):
+        precision = {"fp64": A2C_FP64, "mixed": A2C_MIXED, "fp32": A2C_MIXED}[precision]
+    v = C.c_double()
+    N.check(N.lib().a2c_gpp_peak_flops(int(device), int(precision), C.byref(v)), "a2c_gpp_peak_flops")
+    return v.value
 
 
 def lattice_fcc(ncell, *, a: float = 3.89, periodic=(1, 1, 1), pos_std: float = 0.0, sigma=(0.1, 0.1),

@@ -87,6 +87,7 @@ def lib() -> C.CDLL:
         "a2c_gpp_stream": (P, [P]),
         "a2c_gpp_set_precision": (I, [P, I]),
         "a2c_gpp_synchronize": (I, [P]),
+        "a2c_gpp_set_threads_per_site": (I, [P, I]),
         "a2c_gpp_set_occupancy": (I, [P, P]),
         "a2c_gpp_get_occupancy": (I, [P, P]),
         "a2c_gpp_set_state": (I, [P, P]),
@@ -97,6 +98,7 @@ def lib() -> C.CDLL:
         "a2c_gpp_get_shell_counts": (I, [P, P]),
         "a2c_gpp_eval": (I, [P, P, C.POINTER(D), P]),
         "a2c_gpp_eval_device": (I, [P, P, P, P]),
+        "a2c_gpp_profile_eval": (I, [P, P, P, P, P]),
         "a2c_gpp_get_density": (I, [P, P]),
         "a2c_gpp_bounds": (I, [P, P, P]),
         "a2c_gpp_eam_eval": (I, [P, I, P, C.c_int64, P]),
@@ -107,6 +109,7 @@ def lib() -> C.CDLL:
         "a2c_gpp_diffuse": (I, [P, D, D, D, D, D, P, P, P]),
         "a2c_gpp_macro_results": (I, [P, P, P, I, C.POINTER(D), C.POINTER(D)]),
         "a2c_lattice_fcc": (I, [C.POINTER(LatticeSpec), P, P, P]),
+        "a2c_gpp_peak_flops": (I, [I, I, C.POINTER(D)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -119,12 +122,13 @@ def lib() -> C.CDLL:
 def exported_symbols() -> list[str]:
     """Names of the C ABI functions this binding expects the library to export."""
     return ["a2c_gpp_default_params", "a2c_lbfgs_default_params", "a2c_status_string", "a2c_gpp_create",
-            "a2c_gpp_destroy", "a2c_gpp_stream", "a2c_gpp_set_precision", "a2c_gpp_synchronize", "a2c_gpp_set_occupancy",
+            "a2c_gpp_destroy", "a2c_gpp_stream", "a2c_gpp_set_precision", "a2c_gpp_synchronize",
+            "a2c_gpp_set_threads_per_site", "a2c_gpp_set_occupancy",
             "a2c_gpp_get_occupancy", "a2c_gpp_set_state", "a2c_gpp_get_state", "a2c_gpp_build_neighbors",
             "a2c_gpp_neighbor_total", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
-            "a2c_gpp_eval_device", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
+            "a2c_gpp_eval_device", "a2c_gpp_profile_eval", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
             "a2c_gpp_chem_potential", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",
-            "a2c_lattice_fcc"]
+            "a2c_lattice_fcc", "a2c_gpp_peak_flops"]
 
 
 class A2CError(RuntimeError):

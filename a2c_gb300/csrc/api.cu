@@ -23,14 +23,19 @@ a2c_status cuda_status(cudaError_t e) {
   }
 }
 
-a2c_status eval_device_impl(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG) {
+a2c_status eval_device_impl(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev) {
   if (!c->has_neighbors) return A2C_ERR_STATE;
   if (c->p.precision == A2C_MIXED) {
-    A2C_TRY(mixed_eval(c, dX, d_f, dG));
+    A2C_TRY(mixed_eval(c, dX, d_f, dG, ev));
   } else {
+    if (ev) cudaEventRecord(ev[0], c->stream);
+    if (ev) cudaEventRecord(ev[1], c->stream);
     A2C_TRY(launch_density64(c, dX));
+    if (ev) cudaEventRecord(ev[2], c->stream);
     A2C_TRY(launch_gradient64(c, dX, dG));
+    if (ev) cudaEventRecord(ev[3], c->stream);
     A2C_TRY(reduce_objective(c, d_f));
+    if (ev) cudaEventRecord(ev[4], c->stream);
   }
   c->has_density = (c->p.precision != A2C_MIXED);
   return A2C_OK;
@@ -204,6 +209,12 @@ a2c_status a2c_gpp_destroy(a2c_gpp_ctx *c) {
 
 void *a2c_gpp_stream(a2c_gpp_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
+a2c_status a2c_gpp_set_threads_per_site(a2c_gpp_ctx *c, int tps) {
+  if (!c) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  return mixed_set_threads_per_site(c, tps);
+}
+
 a2c_status a2c_gpp_synchronize(a2c_gpp_ctx *c) {
   if (!c) return A2C_ERR_INVALID;
   DeviceGuard g(c->device);
@@ -355,6 +366,20 @@ a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *c, const double *dX, double *df, dou
     A2C_CUDA(cudaMemcpyAsync(c->d_X, dX, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToDevice, c->stream));
   c->has_state = true;
   return A2C_OK;
+}
+
+a2c_status a2c_gpp_profile_eval(a2c_gpp_ctx *c, const double *dX, double *df, double *dG, float *stage_ms) {
+  if (!c || (!dX && c->N > 0) || !df || (!dG && c->N > 0) || !stage_ms) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  cudaEvent_t ev[5];
+  for (auto &e : ev) A2C_CUDA(cudaEventCreate(&e));
+  a2c_status s = eval_device_impl(c, dX, df, dG, ev);
+  if (!s && cudaEventSynchronize(ev[4]) != cudaSuccess) s = A2C_ERR_CUDA;
+  for (int k = 0; k < 4 && !s; ++k)
+    if (cudaEventElapsedTime(&stage_ms[k], ev[k], ev[k + 1]) != cudaSuccess) s = A2C_ERR_CUDA;
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (s) return s;
+  return check_status_word(c);
 }
 
 a2c_status a2c_gpp_eval(a2c_gpp_ctx *c, const double *X, double *f, double *G) {

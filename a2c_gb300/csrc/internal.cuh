@@ -107,8 +107,12 @@ a2c_status check_status_word(a2c_gpp_ctx *c);
 a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X);
 
 // k_mixed.cu
-a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG);
+// ev: optional 5 events recorded before the first launch and after each
+// stage (prep, pass 1, pass 2, reduction) on the context's stream
+a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev = nullptr);
 void mixed_free(a2c_gpp_ctx *c);
+a2c_status mixed_set_threads_per_site(a2c_gpp_ctx *c, int tps);
+int mixed_threads_per_site(a2c_gpp_ctx *c);
 
 // lbfgs.cu
 a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp, double *fmin, int *iters,
@@ -116,6 +120,6 @@ a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp
 void lbfgs_free(a2c_gpp_ctx *c);
 
 // api.cu
-a2c_status eval_device_impl(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG);
+a2c_status eval_device_impl(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev = nullptr);
 
 }  // namespace a2c

@@ -1,7 +1,460 @@
-// Mixed-precision evaluator (placeholder until the FP32 kernels land).
+// Mixed-precision evaluator: FP32 pair quadrature with compensated per-site
+// sums; FP64 for the per-site finish, the global free-entropy reduction and
+// everything the L-BFGS touches.  Same mathematics as minimizer.cpp:83-369
+// (pass 1: electrondensity.cpp:20-49) with analytic derivatives in place of
+// the reference's central differences.
+//
+// Layout per evaluation (k_prep): every site becomes one int4 -- its
+// position as three 32-bit fixed-point coordinates (unit S/2^32 with S the
+// periodic box length, or 64 A in a free direction) and sigma as FP32 bits.
+// The integer difference of two coordinates, taken modulo 2^32, is the
+// minimum-image difference exactly, so no FP64 arithmetic and no image
+// decoding happen per neighbor; converting it to FP32 costs one rounding.
+//
+// Quadrature in closed form: point k moves coordinate m = k/2 mod 3 of atom i
+// (k < 6) or of atom j (k >= 6) by u = sqrt(6) sigma, so with the pair
+// vector D, |r_k|^2 = (|D|^2 + u^2) +- 2 D_m u: one FMA per point.  The
+// gradient sums reduce to per-pair scalars (sum of c_k, per-coordinate
+// u-weighted differences), multiplied by D once per neighbor.
+//
+// Functions: f_Pd and phi_Pd from the FP32 cubic Hermite tables of
+// tables.cpp (their polynomial forms cancel catastrophically in FP32);
+// f_H, phi_PdH, phi_H analytically with ex2.approx (their exponential tails
+// beyond 5.35 A are C1 continuations, selected branch-free); F and F' per
+// site from FP32 Hermite tables in rho.
+//
+// Mapping: TPS threads per site (1, 2, 4 or 8), each taking every TPS-th
+// neighbor, first among the Pd then among the H neighbors (so the lanes of a
+// warp evaluate the same pair type together), combined by shuffles.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "internal.cuh"
 
 namespace a2c {
-a2c_status mixed_eval(a2c_gpp_ctx *, const double *, double *, double *) { return A2C_ERR_INVALID; }
-void mixed_free(a2c_gpp_ctx *) {}
+
+void build_pair_table(double r0, double h, int n, std::vector<float> &out);
+void build_embed_table(int species, double h, int n, std::vector<float> &out);
+
+struct Mixed {
+  int64_t N = 0;
+  int4 *P = nullptr;        // per site: fixed-point x, y, z; sigma (FP32 bits)
+  float *occ = nullptr;     // per site occupancy (1 for Pd)
+  float2 *FF = nullptr;     // per site (F'(rho), F(rho))
+  float4 *tabPair = nullptr;  // per r interval: f_Pd cubic, phi_Pd cubic
+  float4 *tabEmb = nullptr;   // per rho interval: F_Pd cubics, then F_H cubics
+  int tps = 0;                // threads per site (0 = choose)
+};
+
+namespace {
+
+constexpr double kTabR0 = 1.0;
+constexpr double kTabInvH = 320.0;
+constexpr int kTabN = 2240;  // r in [1, 8)
+constexpr double kEmbInvH = 64.0;
+constexpr int kEmbN = 4096;  // rho in [0, 64)
+constexpr int kBlock = 256;
+
+struct MixArgs {
+  int64_t N;
+  int nPd;
+  float W;
+  float sc[3];  // metres of one fixed-point unit per dimension [A]
+  const int4 *P;
+  const float *occ;
+  const int64_t *off;
+  const uint32_t *nbr;
+  const int *npd;
+  const float4 *tabPair;
+  const float4 *tabEmb;
+  float2 *FF;
+  double *G, *Vs, *Ss;
+  double T;
+};
+
+__device__ __forceinline__ float ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rsq(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ void kahan(float &s, float &c, float v) {
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+__device__ __forceinline__ float3 pair_vec(const MixArgs &a, int4 pi, int4 pj) {  // q_i - q_j
+  return make_float3((float)(int)((unsigned)pi.x - (unsigned)pj.x) * a.sc[0],
+                     (float)(int)((unsigned)pi.y - (unsigned)pj.y) * a.sc[1],
+                     (float)(int)((unsigned)pi.z - (unsigned)pj.z) * a.sc[2]);
+}
+
+__device__ __forceinline__ float hv(float4 c, float t) { return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x); }
+__device__ __forceinline__ float hd(float4 c, float t) { return fmaf(fmaf(3.0f * c.w, t, 2.0f * c.z), t, c.y); }
+
+__device__ __forceinline__ int tab_index(float s, float &t) {
+  float x = (s - (float)kTabR0) * (float)kTabInvH;
+  x = fminf(fmaxf(x, 0.0f), (float)kTabN - 0.5f);
+  const int i = (int)x;
+  t = x - (float)i;
+  return i;
+}
+
+// f_H(r) = C exp(-delta r) (potential.cpp:105-119; its tail is the same
+// exponential); written as A 2^(K (r - 3.5)) to keep the argument small.
+constexpr float kFH_A = (float)(11.0025 * 0.010229853702006403);  // C e^{-3.5 delta}
+constexpr float kFH_K = (float)(-1.30927 * 1.4426950408889634);
+constexpr float kFH_D = -1.30927f;
+__device__ __forceinline__ float fH(float s) { return kFH_A * ex2(kFH_K * (s - 3.5f)); }
+
+// phi_PdH / phi_H (potential.cpp:162-200): D(b e^{-a(r-r0)} - a e^{-b(r-r0)})
+// for r <= 5.35, funRc e^{k(r-5.35)} beyond; value and derivative.
+struct Morse {
+  float A1, K1, R1, A2, K2, R2, rc, At, Kt;
+};
+__device__ __forceinline__ void morse(const Morse &m, float s, float &v, float &d) {
+  const bool tail = s > m.rc;
+  const float A1 = tail ? 0.0f : m.A1, A2 = tail ? m.At : m.A2;
+  const float K1 = m.K1, K2 = tail ? m.Kt : m.K2, R2 = tail ? m.rc : m.R2;
+  const float e1 = A1 * ex2(K1 * (s - m.R1)), e2 = A2 * ex2(K2 * (s - R2));
+  v = e1 + e2;
+  d = (e1 * K1 + e2 * K2) * 0.6931471805599453f;
+}
+#define LOG2E 1.4426950408889634
+__constant__ Morse kPdH = {(float)(0.2494540 * 2.13158), (float)(-4.82613 * LOG2E), 1.50964f,
+                           (float)(-0.2494540 * 4.82613), (float)(-2.13158 * LOG2E), 1.50964f, 5.35f,
+                           (float)-3.353001113951400e-04,
+                           (float)(7.147062196813336e-04 / -3.353001113951400e-04 * LOG2E)};
+__constant__ Morse kHH = {(float)(0.0661496 * 1.47797), (float)(-3.67263 * LOG2E), 2.51980f,
+                          (float)(-0.0661496 * 3.67263), (float)(-1.47797 * LOG2E), 2.51980f, 5.35f,
+                          (float)-0.003702722457147, (float)(0.005465945471933 / -0.003702722457147 * LOG2E)};
+#undef LOG2E
+
+constexpr float kSqrt6 = 2.449489742783178f;
+constexpr float kSqrt3 = 1.7320508075688772f;
+
+// The four squared radii of coordinate c for the pair (D, ui, uj):
+// atom i moved by +ui, -ui; atom j moved by -uj, +uj (r = q_i - q_j).
+#define A2C_RADII(c, Dc)                                  \
+  const float bi = 2.0f * (Dc) * ui, bj = 2.0f * (Dc) * uj; \
+  const float s2[4] = {Ai + bi, Ai - bi, Aj - bj, Aj + bj};
+
+// ---------------------------------------------------------------- pass 1
+template <int TPS>
+__global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t s = g / TPS;
+  const int lane = (int)(g % TPS);
+  const bool live = s < a.N;
+  float acc = 0.0f, cmp = 0.0f;
+  if (live) {
+    const int4 pi = a.P[s];
+    const float ui = kSqrt6 * __int_as_float(pi.w), ui2 = ui * ui;
+    const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
+    for (int64_t t = b + lane; t < m; t += TPS) {  // Pd neighbors: f_Pd
+      const int64_t j = a.nbr[t] & kIdMask;
+      const int4 pj = a.P[j];
+      const float3 D = pair_vec(a, pi, pj);
+      const float uj = kSqrt6 * __int_as_float(pj.w);
+      const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
+      const float Ai = D2 + ui2, Aj = fmaf(uj, uj, D2);
+      float part = 0.0f;
+      const float Dv[3] = {D.x, D.y, D.z};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        A2C_RADII(c, Dv[c])
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float r = s2[q] * rsq(s2[q]);
+          float tt;
+          const int i = tab_index(r, tt);
+          part += hv(__ldg(&a.tabPair[2 * i]), tt);
+        }
+      }
+      kahan(acc, cmp, part);
+    }
+    for (int64_t t = m + lane; t < e; t += TPS) {  // H neighbors: x_j f_H
+      const int64_t j = a.nbr[t] & kIdMask;
+      const int4 pj = a.P[j];
+      const float3 D = pair_vec(a, pi, pj);
+      const float uj = kSqrt6 * __int_as_float(pj.w);
+      const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
+      const float Ai = D2 + ui2, Aj = fmaf(uj, uj, D2);
+      float part = 0.0f;
+      const float Dv[3] = {D.x, D.y, D.z};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        A2C_RADII(c, Dv[c])
+#pragma unroll
+        for (int q = 0; q < 4; ++q) part += fH(s2[q] * rsq(s2[q]));
+      }
+      kahan(acc, cmp, part * a.occ[j]);
+    }
+  }
+  float tot = acc;
+#pragma unroll
+  for (int o = TPS / 2; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  if (live && lane == 0) {
+    const float rho = tot * a.W;
+    const bool iPd = s < a.nPd;
+    float x = fminf(fmaxf(rho * (float)kEmbInvH, 0.0f), (float)kEmbN - 0.5f);
+    const int i = (int)x;
+    const float tt = x - (float)i;
+    const float4 c = __ldg(&a.tabEmb[(iPd ? 0 : kEmbN) + i]);
+    a.FF[s] = make_float2(hd(c, tt) * (float)kEmbInvH, hv(c, tt));
+  }
+}
+
+// ---------------------------------------------------------------- pass 2
+// Per pair: c_k = g(s_k)/s_k with g = F'_A(rho_i) f'_B + F'_B(rho_j) f'_A +
+// phi'_AB; the pair's gradient contributions are
+//   sum_k c_k r_k = D * sum_k c_k + e_m * sum over the points moving m of c_k delta_k
+//   sigma part    = sqrt(3) sum_m [ D_m (c_{+i} - c_{-i}) + ui (c_{+i} + c_{-i}) ]
+// scaled by W x_j; the energy is 0.5 W x_i x_j sum_k phi(s_k).
+struct PairAcc {
+  float csum, e[3], sig, v;
+};
+
+template <int TYPE>  // 0 Pd-Pd, 1 Pd i / H j, 2 H i / Pd j, 3 H-H
+__device__ __forceinline__ void pair_terms(const MixArgs &a, float Fa, float Fb, float3 D, float ui, float uj,
+                                           PairAcc &p) {
+  const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
+  const float Ai = fmaf(ui, ui, D2), Aj = fmaf(uj, uj, D2);
+  const float Dv[3] = {D.x, D.y, D.z};
+  p.csum = 0.0f;
+  p.sig = 0.0f;
+  p.v = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    A2C_RADII(c, Dv[c])
+    float ck[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float is = rsq(s2[q]);
+      const float r = s2[q] * is;
+      float g, phi;
+      if (TYPE == 0) {
+        float tt;
+        const int i = tab_index(r, tt);
+        const float4 cf = __ldg(&a.tabPair[2 * i]), cp = __ldg(&a.tabPair[2 * i + 1]);
+        g = fmaf(Fa + Fb, hd(cf, tt), hd(cp, tt)) * (float)kTabInvH;
+        phi = hv(cp, tt);
+      } else if (TYPE == 3) {
+        const float fh = fH(r);
+        float dphi;
+        morse(kHH, r, phi, dphi);
+        g = fmaf((Fa + Fb) * kFH_D, fh, dphi);
+      } else {
+        float tt;
+        const int i = tab_index(r, tt);
+        const float fpd = hd(__ldg(&a.tabPair[2 * i]), tt) * (float)kTabInvH;
+        const float fhd = fH(r) * kFH_D;
+        float dphi;
+        morse(kPdH, r, phi, dphi);
+        g = (TYPE == 1) ? fmaf(Fa, fhd, fmaf(Fb, fpd, dphi)) : fmaf(Fa, fpd, fmaf(Fb, fhd, dphi));
+      }
+      ck[q] = g * is;
+      p.v += phi;
+    }
+    const float cpi = ck[0], cmi = ck[1], cmj = ck[2], cpj = ck[3];
+    p.csum += (cpi + cmi) + (cmj + cpj);
+    p.e[c] = fmaf(ui, cpi - cmi, uj * (cpj - cmj));
+    p.sig = fmaf(Dv[c], cpi - cmi, fmaf(ui, cpi + cmi, p.sig));
+  }
+}
+
+struct SiteAcc {
+  float s[5], c[5];  // Fq x, y, z, Fsigma, V  with Kahan compensations
+};
+
+__device__ __forceinline__ void add_pair(SiteAcc &A, const PairAcc &p, float3 D, float wx, float vx) {
+  kahan(A.s[0], A.c[0], wx * fmaf(D.x, p.csum, p.e[0]));
+  kahan(A.s[1], A.c[1], wx * fmaf(D.y, p.csum, p.e[1]));
+  kahan(A.s[2], A.c[2], wx * fmaf(D.z, p.csum, p.e[2]));
+  kahan(A.s[3], A.c[3], wx * p.sig);
+  kahan(A.s[4], A.c[4], vx * p.v);
+}
+
+template <int TPS>
+__global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t s = g / TPS;
+  const int lane = (int)(g % TPS);
+  const bool live = s < a.N;
+  SiteAcc A;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) A.s[k] = A.c[k] = 0.0f;
+  float xi = 0.0f, sigi = 1.0f;
+  float2 ffi = make_float2(0.0f, 0.0f);
+  if (live) {
+    const int4 pi = a.P[s];
+    sigi = __int_as_float(pi.w);
+    const float ui = kSqrt6 * sigi;
+    xi = a.occ[s];
+    ffi = a.FF[s];
+    const bool iPd = s < a.nPd;
+    const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
+    const float hw = 0.5f * a.W * xi;
+    for (int64_t t = b + lane; t < m; t += TPS) {  // Pd neighbors
+      const int64_t j = a.nbr[t] & kIdMask;
+      const int4 pj = a.P[j];
+      const float3 D = pair_vec(a, pi, pj);
+      const float uj = kSqrt6 * __int_as_float(pj.w);
+      const float Fb = a.FF[j].x;
+      PairAcc p;
+      if (iPd) pair_terms<0>(a, ffi.x, Fb, D, ui, uj, p);
+      else pair_terms<2>(a, ffi.x, Fb, D, ui, uj, p);
+      add_pair(A, p, D, a.W, hw);
+    }
+    for (int64_t t = m + lane; t < e; t += TPS) {  // H neighbors
+      const int64_t j = a.nbr[t] & kIdMask;
+      const int4 pj = a.P[j];
+      const float3 D = pair_vec(a, pi, pj);
+      const float uj = kSqrt6 * __int_as_float(pj.w);
+      const float Fb = a.FF[j].x;
+      const float xj = a.occ[j];
+      PairAcc p;
+      if (iPd) pair_terms<1>(a, ffi.x, Fb, D, ui, uj, p);
+      else pair_terms<3>(a, ffi.x, Fb, D, ui, uj, p);
+      add_pair(A, p, D, a.W * xj, hw * xj);
+    }
+  }
+  double tot[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    float v = A.s[k] - A.c[k];
+#pragma unroll
+    for (int o = TPS / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    tot[k] = (double)v;
+  }
+  if (live && lane == 0) {
+    const double x = xi, sg = sigi, invT = 1.0 / a.T;
+    a.G[4 * s] = tot[0] * (invT * x);
+    a.G[4 * s + 1] = tot[1] * (invT * x);
+    a.G[4 * s + 2] = tot[2] * (invT * x);
+    a.G[4 * s + 3] = tot[3] * (1.7320508075688772 * 1.4142135623730951 * invT * x) - 3.0 * kB / sg * x;
+    a.Vs[s] = x * (double)ffi.y + tot[4];
+    a.Ss[s] = (double)logf(sigi) * x;
+  }
+}
+
+__global__ void k_prep(const double *X, const double *occ, int64_t N, double k0, double k1, double k2, int4 *P,
+                       float *occf) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  const long long u0 = __double2ll_rn(X[4 * s] * k0);
+  const long long u1 = __double2ll_rn(X[4 * s + 1] * k1);
+  const long long u2 = __double2ll_rn(X[4 * s + 2] * k2);
+  P[s] = make_int4((int)(unsigned)u0, (int)(unsigned)u1, (int)(unsigned)u2, __float_as_int((float)X[4 * s + 3]));
+  occf[s] = (float)occ[s];
+}
+
+template <int TPS>
+void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev) {
+  const int64_t threads = a.N * TPS;
+  const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
+  k_rho_mixed<TPS><<<grid, kBlock, 0, st>>>(a);
+  if (ev) cudaEventRecord(ev[2], st);
+  k_grad_mixed<TPS><<<grid, kBlock, 0, st>>>(a);
+  if (ev) cudaEventRecord(ev[3], st);
+}
+
+a2c_status ensure_mixed(a2c_gpp_ctx *c) {
+  if (c->mixed && c->mixed->N == c->N) return A2C_OK;
+  mixed_free(c);
+  Mixed *M = new Mixed;
+  c->mixed = M;
+  M->N = c->N;
+  const int64_t n = std::max<int64_t>(c->N, 1);
+  if (cudaMalloc(&M->P, sizeof(int4) * n) != cudaSuccess || cudaMalloc(&M->occ, sizeof(float) * n) != cudaSuccess ||
+      cudaMalloc(&M->FF, sizeof(float2) * n) != cudaSuccess ||
+      cudaMalloc(&M->tabPair, sizeof(float4) * 2 * kTabN) != cudaSuccess ||
+      cudaMalloc(&M->tabEmb, sizeof(float4) * 2 * kEmbN) != cudaSuccess)
+    return A2C_ERR_NOMEM;
+  std::vector<float> pair, embPd, embH;
+  build_pair_table(kTabR0, 1.0 / kTabInvH, kTabN, pair);
+  build_embed_table(0, 1.0 / kEmbInvH, kEmbN, embPd);
+  build_embed_table(1, 1.0 / kEmbInvH, kEmbN, embH);
+  A2C_CUDA(cudaMemcpyAsync(M->tabPair, pair.data(), sizeof(float) * pair.size(), cudaMemcpyHostToDevice, c->stream));
+  A2C_CUDA(cudaMemcpyAsync(M->tabEmb, embPd.data(), sizeof(float) * embPd.size(), cudaMemcpyHostToDevice, c->stream));
+  A2C_CUDA(cudaMemcpyAsync(M->tabEmb + kEmbN, embH.data(), sizeof(float) * embH.size(), cudaMemcpyHostToDevice,
+                           c->stream));
+  A2C_CUDA(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+  return A2C_OK;
+}
+
+}  // namespace
+
+void mixed_free(a2c_gpp_ctx *c) {
+  Mixed *M = c->mixed;
+  if (!M) return;
+  for (void *p : {(void *)M->P, (void *)M->occ, (void *)M->FF, (void *)M->tabPair, (void *)M->tabEmb})
+    if (p) cudaFree(p);
+  delete M;
+  c->mixed = nullptr;
+}
+
+int mixed_threads_per_site(a2c_gpp_ctx *c) { return (c->mixed && c->mixed->tps) ? c->mixed->tps : 0; }
+
+a2c_status mixed_set_threads_per_site(a2c_gpp_ctx *c, int tps) {
+  if (tps != 0 && tps != 1 && tps != 2 && tps != 4 && tps != 8) return A2C_ERR_INVALID;
+  A2C_TRY(ensure_mixed(c));
+  c->mixed->tps = tps;
+  return A2C_OK;
+}
+
+a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev) {
+  A2C_TRY(ensure_mixed(c));
+  Mixed *M = c->mixed;
+  const int64_t N = c->N;
+  MixArgs a{};
+  a.N = N;
+  a.nPd = c->p.nPd;
+  a.W = (float)c->p.QWp;
+  double k[3];
+  for (int d = 0; d < 3; ++d) {
+    const double S = c->p.periodic[d] ? c->p.box[d] : 64.0;  // free direction: any span > 2 x neighbor reach
+    k[d] = 4294967296.0 / S;
+    a.sc[d] = (float)(S / 4294967296.0);
+  }
+  a.P = M->P;
+  a.occ = M->occ;
+  a.off = c->d_off;
+  a.nbr = c->d_nbr;
+  a.npd = c->d_npd;
+  a.tabPair = M->tabPair;
+  a.tabEmb = M->tabEmb;
+  a.FF = M->FF;
+  a.G = dG;
+  a.Vs = c->d_Vs;
+  a.Ss = c->d_Ss;
+  a.T = c->p.T;
+  if (ev) cudaEventRecord(ev[0], c->stream);
+  if (N > 0) {
+    k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ);
+    A2C_CUDA(cudaGetLastError());
+    if (ev) cudaEventRecord(ev[1], c->stream);
+    int tps = M->tps ? M->tps : (N < 152 * 2048 ? 4 : 1);
+    switch (tps) {
+      case 1: launch_pair_kernels<1>(a, c->stream, ev); break;
+      case 2: launch_pair_kernels<2>(a, c->stream, ev); break;
+      case 4: launch_pair_kernels<4>(a, c->stream, ev); break;
+      default: launch_pair_kernels<8>(a, c->stream, ev); break;
+    }
+    A2C_CUDA(cudaGetLastError());
+  } else if (ev) {
+    for (int k2 = 1; k2 < 4; ++k2) cudaEventRecord(ev[k2], c->stream);
+  }
+  A2C_TRY(reduce_objective(c, d_f));
+  if (ev) cudaEventRecord(ev[4], c->stream);
+  return A2C_OK;
+}
+
 }  // namespace a2c

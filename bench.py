@@ -1,0 +1,393 @@
+#!/usr/bin/env python
+"""GPP-EAM objective+gradient throughput on GB300 (atom-evals/s).
+
+Workload: the evaluator-throughput configuration -- an fcc Pd lattice of
+32x32x32 cells with its octahedral H sites (131,072 Pd + 131,072 H =
+262,144 sites), periodic in x, y, z, positions perturbed by N(0, 0.03 A),
+sigma ~ U(0.08, 0.14) A, occupancy ~ U(0, 0.3) clamped to >= 1e-3, T = 300 K,
+seeded synthetic data generated in-process.  One step = one objective +
+gradient evaluation (both quadrature passes and the free-entropy reduction)
+at a fixed state; one atom-eval = one site's contribution.
+
+Headline `value`: the mixed-precision form (FP32 pair quadrature,
+compensated per-site sums, FP64 reductions), device-resident inputs, CUDA
+events on the evaluator's stream, L2 (129 MB) flushed by writing a 256 MB
+buffer before every step.  Also reported: the FP64 plain form, the errors of
+the mixed form against it, `e2e` through the public host-pointer entry
+point a2c_gpp_eval (pinned host input and output copied every step), the
+roofline of the dominant kernel (pass 2), the CPU oracle as a baseline, and
+the SM clocks sampled during the timed region.
+
+Multi-GPU (torchrun): every rank evaluates its own replica (weak scaling, no
+data-path collective); `value` is the sum over ranks of atom-evals divided
+by the slowest rank's device time.
+
+--impl reference times the reference's CPU algorithm (the oracle port with
+the reference's redundant finite-difference calls, all host threads) on a
+bounded 12x12x12-cell sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GPP-EAM objective+grad atom-evals/s & time-to-minimum, mixed vs FP64 on GB300"
+UNIT = "atom-evals/s"
+WORKLOAD = dict(ncell=32, periodic=(1, 1, 1), pos_std=0.03, sigma=(0.08, 0.14), x_center=0.15, x_half=0.15, seed=2)
+
+
+def config_dict(extra=None):
+    c = {"workload": "evaluator throughput: fcc Pd 32x32x32 cells + octahedral H, periodic, 262,144 sites, "
+                     "N(0,0.03 A) positions, sigma~U(0.08,0.14) A, x~U(0,0.3), T=300 K",
+         "sites": 262144, "quadrature_points": 12, "cutoff_A": 5.35, "l2": "flushed (256 MB write) before each step"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return json.loads(p.read_text())
+    except Exception:
+        return {}
+
+
+def cpu_sample(threads: int, seconds: float = 10.0, max_evals: int = 50):
+    """The oracle (reference arithmetic, the reference's redundant FD calls)
+    on a 12x12x12-cell sample drawn like the workload; returns (atom-evals/s,
+    evals, sites)."""
+    import a2c_gb300 as A
+    from oracle import oracle as O
+
+    w = dict(WORKLOAD, ncell=12)
+    X, xH, _, box, nPd, nH = A.lattice_fcc(w["ncell"], periodic=w["periodic"], pos_std=w["pos_std"],
+                                           sigma=w["sigma"], x_center=w["x_center"], x_half=w["x_half"],
+                                           seed=w["seed"])
+    pb = O.Problem(nPd, nH, box=box, periodic=w["periodic"])
+    off, nbr, *_ = O.neighbors(pb, X)
+    O.evaluate(pb, X, xH, off, nbr, mode=1, threads=threads)  # warm-up
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_evals and (time.perf_counter() - t0) < seconds:
+        O.evaluate(pb, X, xH, off, nbr, mode=1, threads=threads)
+        n += 1
+    dt = time.perf_counter() - t0
+    return (nPd + nH) * n / dt, n, nPd + nH
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+
+    O.build(ref=False)
+    threads = os.cpu_count() or 1
+    w = dict(WORKLOAD, ncell=12)
+    import a2c_gb300 as A
+
+    X, xH, _, box, nPd, nH = A.lattice_fcc(w["ncell"], periodic=w["periodic"], pos_std=w["pos_std"],
+                                           sigma=w["sigma"], x_center=w["x_center"], x_half=w["x_half"],
+                                           seed=w["seed"])
+    pb = O.Problem(nPd, nH, box=box, periodic=w["periodic"])
+    off, nbr, *_ = O.neighbors(pb, X)
+    for _ in range(args.warmup):
+        O.evaluate(pb, X, xH, off, nbr, mode=1, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.evaluate(pb, X, xH, off, nbr, mode=1, threads=threads)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = (nPd + nH) * args.steps / tot
+    sample = (f"{w['ncell']}x{w['ncell']}x{w['ncell']}-cell sample ({nPd + nH} sites) of the workload, "
+              f"one objective+gradient evaluation per step")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict({"sample_sites": nPd + nH}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference's CPU path: the oracle restatement (bit-exact with the reference's own "
+                    "sources where those compile) with its redundant FD calls, OpenMP over sites"}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import a2c_gb300 as A
+    from a2c_gb300 import flop_model
+    from a2c_gb300 import _native as NATIVE
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = local
+    w = WORKLOAD
+    X, xH, _, box, nPd, nH = A.lattice_fcc(w["ncell"], periodic=w["periodic"], pos_std=w["pos_std"],
+                                           sigma=w["sigma"], x_center=w["x_center"], x_half=w["x_half"],
+                                           seed=w["seed"] + rank)
+    Ns = nPd + nH
+    g = A.Gpp(nPd, nH, box=box, periodic=w["periodic"], precision="mixed", device=dev)
+    g.set_occupancy(xH)
+    g.build_neighbors(X)
+    tot = {k: 0 for k in ("PdPd", "PdH", "HPd", "HH")}
+    for lid, k in enumerate(tot):
+        o, _ = g.neighbors(lid)
+        tot[k] = int(o[-1])
+    fl = flop_model.flops(tot["PdPd"], tot["PdH"], tot["HPd"], tot["HH"], Ns)
+    n_entries = sum(tot.values())
+
+    stream = torch.cuda.ExternalStream(g.stream, device=dev)
+    dX = torch.tensor(X, device=dev)
+    dG = torch.empty_like(dX)
+    df = torch.empty(1, dtype=torch.float64, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    torch.cuda.synchronize()
+
+    def step_profiled():
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        return g.profile_eval(dX.data_ptr(), df.data_ptr(), dG.data_ptr())
+
+    # autotune the threads-per-site mapping of the mixed kernels
+    tune = {}
+    for tps in (1, 2, 4, 8):
+        g.set_threads_per_site(tps)
+        step_profiled()
+        tune[tps] = min(float(np.sum(step_profiled())) for _ in range(3))
+    best = min(tune, key=tune.get)
+    g.set_threads_per_site(best)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def timed(nsteps, nwarm):
+        for _ in range(nwarm):
+            step_profiled()
+        barrier()
+        torch.cuda.synchronize()
+        stages = []
+        for _ in range(nsteps):
+            stages.append(step_profiled())
+        torch.cuda.synchronize()
+        barrier()
+        return np.array(stages)
+
+    with ClockSampler(dev) as clk:
+        st_mixed = timed(args.steps, args.warmup)
+    clocks = clk.summary()
+    f_mixed = df.item()
+    G_mixed = dG.cpu().numpy()
+
+    # FP64 plain form on the same state
+    g.set_precision("fp64")
+    st_64 = timed(args.fp64_steps, 1)
+    f_64 = df.item()
+    G_64 = dG.cpu().numpy()
+    g.set_precision("mixed")
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        import torch.distributed as dist
+
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    dev_time_mixed = max_over_ranks(float(st_mixed.sum()) * 1e-3)
+    dev_time_64 = max_over_ranks(float(st_64.sum()) * 1e-3)
+    value = world * Ns * args.steps / dev_time_mixed
+    value_64 = world * Ns * args.fp64_steps / dev_time_64
+
+    # end to end through the public host-pointer entry point
+    Xp = torch.empty(4 * Ns, dtype=torch.float64, pin_memory=True)
+    Xp.numpy()[:] = X
+    Gp = torch.empty(4 * Ns, dtype=torch.float64, pin_memory=True)
+    fbuf = np.zeros(1)
+    L = NATIVE.lib()
+    import ctypes as C
+
+    fval = C.c_double()
+
+    def e2e_step():
+        NATIVE.check(L.a2c_gpp_eval(g.handle, C.c_void_p(Xp.data_ptr()), C.byref(fval), C.c_void_p(Gp.data_ptr())),
+                     "a2c_gpp_eval")
+
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e2e_step()
+    e2e_t = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_time = max_over_ranks(sum(e2e_t))
+    fbuf[0] = fval.value
+    e2e_value = world * Ns * args.steps / e2e_time
+
+    # roofline of the dominant kernel (pass 2) from the timed steps
+    pass2_ms = float(np.mean(st_mixed[:, 2]))
+    pass1_ms = float(np.mean(st_mixed[:, 1]))
+    peak32 = A.peak_flops("fp32", dev)
+    peak64 = A.peak_flops("fp64", dev)
+    ach = fl["pass2"] / (pass2_ms * 1e-3)
+    pass2_64_ms = float(np.mean(st_64[:, 2]))
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get("k_grad_mixed_bytes_per_launch")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "fp32", "kernel": f"k_grad_mixed<{best}> (pass 2)", "achieved": ach / 1e12,
+                "peak": peak32 / 1e12, "unit": "TFLOP/s", "frac": ach / peak32,
+                "peak_source": "measured in this run: FP32 FMA-chain kernel (a2c_gpp_peak_flops); "
+                               "MEASURED_PEAKS.json holds only HBM and bf16-tensor peaks and no tensor core "
+                               "is used here",
+                "flops_per_launch": fl["pass2"], "traffic": traffic,
+                "hbm_frac": (flop_model.algorithmic_bytes(Ns, n_entries) / ((pass1_ms + pass2_ms) * 1e-3)) /
+                            (measured_peaks().get("hbm_gbs", 6800.0) * 1e9),
+                "pass1": {"ms": pass1_ms, "achieved_tflops": fl["pass1"] / (pass1_ms * 1e-3) / 1e12},
+                "fp64_plain_pass2": {"ms": pass2_64_ms, "achieved_tflops": fl["pass2"] / (pass2_64_ms * 1e-3) / 1e12,
+                                     "peak_tflops": peak64 / 1e12,
+                                     "frac": fl["pass2"] / (pass2_64_ms * 1e-3) / peak64}}
+
+    rel_f = abs(f_mixed - f_64) / abs(f_64)
+    rel_g = float(np.linalg.norm(G_mixed - G_64) / np.linalg.norm(G_64))
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, n, sites = cpu_sample(threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"12x12x12-cell sample ({sites} sites) of the workload, {n} evaluations, "
+                         f"oracle with the reference's arithmetic and redundant FD calls, OpenMP"}
+
+    g.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dev_time_mixed * 1e3 / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": config_dict({"parallelism": f"replicas x{world}", "threads_per_site": best,
+                                       "autotune_ms": tune}),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * 4 * Ns,
+                        "d2h_bytes_per_step": 8 * 4 * Ns + 8},
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "gpu_launches": 5 * args.steps,
+                "fp64_plain": {"value": value_64, "unit": UNIT, "steps": args.fp64_steps,
+                               "ms_per_step": dev_time_64 * 1e3 / args.fp64_steps},
+                "mixed_over_fp64": value / value_64,
+                "mixed_error_vs_fp64": {"free_entropy_rel": rel_f, "gradient_rel_2norm": rel_g},
+                "stages_ms_mixed": {"prep": float(np.mean(st_mixed[:, 0])), "pass1": pass1_ms, "pass2": pass2_ms,
+                                    "reduce": float(np.mean(st_mixed[:, 3]))}}
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -104,6 +104,11 @@ a2c_status a2c_gpp_destroy(a2c_gpp_ctx *ctx);
 /* The context's CUDA stream, as a cudaStream_t cast to void*. */
 void *a2c_gpp_stream(a2c_gpp_ctx *ctx);
 a2c_status a2c_gpp_set_precision(a2c_gpp_ctx *ctx, int precision);
+/* Threads per site of the mixed-precision kernels: 1, 2, 4 or 8, or 0 to
+ * let the library choose (the autotuner in a2c_gb300/autotune.py measures
+ * the candidates and sets the fastest). */
+a2c_status a2c_gpp_set_threads_per_site(a2c_gpp_ctx *ctx, int tps);
+
 /* Waits for all work queued on the context's stream (for _device calls). */
 a2c_status a2c_gpp_synchronize(a2c_gpp_ctx *ctx);
 
@@ -135,6 +140,11 @@ a2c_status a2c_gpp_get_shell_counts(a2c_gpp_ctx *ctx, int *PdPdnum);
  * the current state. */
 a2c_status a2c_gpp_eval(a2c_gpp_ctx *ctx, const double *X, double *f, double *G);
 a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG);
+/* Profiling aid: one stream-ordered evaluation on device pointers with CUDA
+ * events between its launches; stage_ms[4] receives the durations of the
+ * state preparation, pass 1 (densities), pass 2 (energy and gradient) and
+ * the objective reduction.  Waits for completion. */
+a2c_status a2c_gpp_profile_eval(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG, float *stage_ms);
 /* Site electron densities of the last evaluation, all Pd then all H
  * (electrondensity.cpp:12-56, the reference's recv_Pd / recv_H). */
 a2c_status a2c_gpp_get_density(a2c_gpp_ctx *ctx, double *rho);
@@ -176,6 +186,11 @@ a2c_status a2c_gpp_diffuse(a2c_gpp_ctx *ctx, double dt, double nu, double Qm, do
  * calculateMacroResults (calculateresults.cpp:8-78). */
 a2c_status a2c_gpp_macro_results(a2c_gpp_ctx *ctx, const double *x, const int *HSurf, int nSurf, double *xH,
                                  double *xHinterior);
+
+/* Measured peak of the FP64 (precision A2C_FP64) or FP32 (A2C_MIXED) FMA
+ * pipe of a device, in flop/s: the roofline denominator for the evaluator's
+ * compute-bound kernels (no reference counterpart; a measurement aid). */
+a2c_status a2c_gpp_peak_flops(int device, int precision, double *flops_per_s);
 
 /* Seeded synthetic fcc Pd lattice with octahedral H sites (stand-in for the
  * reference's SpaceInitializer lattice setup).  Site order: cells z, y, x,

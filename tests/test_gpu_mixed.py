@@ -1,0 +1,74 @@
+"""Mixed-precision form (FP32 pair quadrature, compensated per-site sums,
+FP64 finish and reductions) against the FP64 oracle.
+
+Stated bounds: free entropy within 1e-6 relative of the FP64 oracle; the
+gradient within 1e-4 in the 2-norm relative (FP32 rounding of terms that
+cancel in the net per-site force); densities-derived quantities are checked
+through the objective.  Every threads-per-site mapping gives the same
+result to FP32 rounding.
+"""
+import numpy as np
+import pytest
+
+import a2c_gb300 as A
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_F = 1e-6
+TOL_G = 1e-4
+
+CASES = {
+    "free3": ((3, 3, 3), (0, 0, 0), 0.02, (0.10, 0.10), 0.05, 0.01, 1),
+    "config1_6cube": ((6, 6, 6), (1, 1, 1), 0.02, (0.10, 0.10), 0.05, 0.01, 1),
+    "slab_4x5x6": ((4, 5, 6), (1, 1, 0), 0.03, (0.08, 0.14), 0.15, 0.15, 7),
+    "config2_16cube": ((16, 16, 16), (1, 1, 1), 0.03, (0.08, 0.14), 0.15, 0.15, 2),
+}
+
+
+def make(case):
+    ncell, per, ps, sg, xc, xh, seed = CASES[case]
+    X, xH, surf, box, nPd, nH = A.lattice_fcc(ncell, periodic=per, pos_std=ps, sigma=sg, x_center=xc, x_half=xh,
+                                             seed=seed)
+    return X, xH, box, per, nPd, nH, O.Problem(nPd, nH, box=box, periodic=per)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_mixed_objective_gradient(gpu, case):
+    X, xH, box, per, nPd, nH, pb = make(case)
+    off, nbr, *_ = O.neighbors(pb, X)
+    f_ref, G_ref, _, _ = O.evaluate(pb, X, xH, off, nbr, mode=1)
+    with A.Gpp(nPd, nH, box=box, periodic=per, precision="mixed") as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        res = {}
+        for tps in (1, 2, 4, 8):
+            g.set_threads_per_site(tps)
+            res[tps] = g.eval(X)
+    for tps, (f, G) in res.items():
+        rel_f = abs(f - f_ref) / abs(f_ref)
+        rel_g = np.linalg.norm(G - G_ref) / np.linalg.norm(G_ref)
+        print(f"{case} tps={tps}: rel_f={rel_f:.3e} rel_G={rel_g:.3e}")
+        assert rel_f < TOL_F
+        assert rel_g < TOL_G
+
+
+def test_mixed_minimize_close_to_fp64(gpu):
+    """Mixed-precision L-BFGS (FP64 vector algebra) converges to the FP64
+    minimum: free entropy within 1e-6 relative, positions within 1e-4 A."""
+    X, xH, box, per, nPd, nH, pb = make("config1_6cube")
+    kw = dict(m=5, max_it=2000, gatol=1e-6)
+    with A.Gpp(nPd, nH, box=box, periodic=per) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        r64 = g.minimize(X, **kw)
+        g.set_precision("mixed")
+        rmx = g.minimize(X, **dict(kw, gatol=2e-6))
+        g.set_precision("fp64")
+        f_at_mixed, _ = g.eval(rmx.X)
+    dq = np.abs(rmx.X.reshape(-1, 4)[:, :3] - r64.X.reshape(-1, 4)[:, :3]).max()
+    print(f"fp64: it={r64.iters} f={r64.fmin:.12e} reason={r64.reason}; mixed: it={rmx.iters} f={rmx.fmin:.12e} "
+          f"reason={rmx.reason}; fp64 objective at the mixed minimum {f_at_mixed:.12e}; max|dq|={dq:.2e}")
+    assert r64.reason == 3
+    assert abs(f_at_mixed - r64.fmin) <= 1e-6 * abs(r64.fmin)
+    assert dq < 1e-4
