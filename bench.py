@@ -373,6 +373,36 @@ def run_ours(args):
     return 0
 
 
+def run_profile_case(args):
+    """A small case for ncu captures: a 40x40x40-cell lattice (512,000
+    sites; neighbor lists ~165 MB, larger than the 129 MB L2), `--steps`
+    mixed evaluations then one FP64 plain evaluation, untimed."""
+    import torch
+
+    import a2c_gb300 as A
+
+    w = dict(WORKLOAD, ncell=args.case_cells)
+    X, xH, _, box, nPd, nH = A.lattice_fcc(w["ncell"], periodic=w["periodic"], pos_std=w["pos_std"],
+                                           sigma=w["sigma"], x_center=w["x_center"], x_half=w["x_half"],
+                                           seed=w["seed"])
+    with A.Gpp(nPd, nH, box=box, periodic=w["periodic"], precision="mixed") as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        dX = torch.tensor(X, device="cuda")
+        dG = torch.empty_like(dX)
+        df = torch.empty(1, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            g.eval_device(dX.data_ptr(), df.data_ptr(), dG.data_ptr())
+        g.synchronize()
+        if args.fp64_steps > 0:
+            g.set_precision("fp64")
+            g.eval_device(dX.data_ptr(), df.data_ptr(), dG.data_ptr())
+            g.synchronize()
+    print(json.dumps({"case": "profile", "sites": nPd + nH, "f": df.item()}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -381,7 +411,12 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--case", choices=["bench", "profile"], default="bench",
+                    help="profile: the small untimed case used for ncu captures")
+    ap.add_argument("--case-cells", type=int, default=40)
     args = ap.parse_args()
+    if args.case == "profile":
+        return run_profile_case(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
