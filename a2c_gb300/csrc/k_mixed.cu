@@ -28,6 +28,7 @@
 // warp evaluate the same pair type together), combined by shuffles.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "internal.cuh"
@@ -458,3 +459,172 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
 }
 
 }  // namespace a2c
+
+// ---------------------------------------------------------------------------
+// Allocation-free evaluation: a2c_gpp_eval_mixed_noalloc.
+//
+// For callers that cannot allocate device memory at evaluation time -- a
+// host code whose device memory is owned by another allocator (a PETSc or
+// solver-framework callback running under its own memory pool), or work
+// recorded into a CUDA graph by a driver that forbids allocation while it
+// records -- this entry point evaluates the mixed-precision form with all of
+// its scratch in one file-scope device array of fixed size instead of
+// memory from cudaMalloc.  Every GPU that loads the library holds the array
+// (about 5.8 MB) until the process exits.
+// ---------------------------------------------------------------------------
+namespace a2c {
+
+void build_pair_table_raw(double r0, double h, int n, float *out);
+void build_embed_table_raw(int species, double h, int n, float *out);
+
+namespace {
+
+constexpr int64_t kNaMaxSites = 131072;  // the largest problem the fixed scratch holds
+constexpr int kNaRedGrid = 1024, kNaRedBlock = 256;
+// byte offsets of the scratch regions, each a multiple of 256
+constexpr size_t kNaP = 0;
+constexpr size_t kNaOcc = kNaP + 16 * (size_t)kNaMaxSites;
+constexpr size_t kNaFF = kNaOcc + 4 * (size_t)kNaMaxSites;
+constexpr size_t kNaVs = kNaFF + 8 * (size_t)kNaMaxSites;
+constexpr size_t kNaSs = kNaVs + 8 * (size_t)kNaMaxSites;
+constexpr size_t kNaPart = kNaSs + 8 * (size_t)kNaMaxSites;
+constexpr size_t kNaTabPair = kNaPart + 8 * 2 * (size_t)kNaRedGrid;
+constexpr size_t kNaTabEmb = kNaTabPair + 16 * 2 * (size_t)kTabN;
+constexpr size_t kNaBytes = kNaTabEmb + 16 * 2 * (size_t)kEmbN;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+// Host side: the device address of the array, looked up once per device.
+constexpr int kNaMaxDevices = 64;
+unsigned char *g_na_base[kNaMaxDevices] = {};
+std::mutex g_na_mutex;
+float g_na_pair_host[8 * kTabN];
+float g_na_emb_host[2 * 4 * kEmbN];
+bool g_na_host_ready = false;
+
+// Set-up on the current device: resolve the array's device address and
+// load the constant function tables into it.  Runs on a device's first call.
+a2c_status na_setup(int dev, unsigned char **base) {
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  if (dev < 0 || dev >= kNaMaxDevices) return A2C_ERR_INVALID;
+  if (g_na_base[dev]) {
+    *base = g_na_base[dev];
+    return A2C_OK;
+  }
+  void *ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (!g_na_host_ready) {
+    build_pair_table_raw(kTabR0, 1.0 / kTabInvH, kTabN, g_na_pair_host);
+    build_embed_table_raw(0, 1.0 / kEmbInvH, kEmbN, g_na_emb_host);
+    build_embed_table_raw(1, 1.0 / kEmbInvH, kEmbN, g_na_emb_host + 4 * kEmbN);
+    g_na_host_ready = true;
+  }
+  unsigned char *b = (unsigned char *)ptr;
+  e = cudaMemcpy(b + kNaTabPair, g_na_pair_host, sizeof(g_na_pair_host), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b + kNaTabEmb, g_na_emb_host, sizeof(g_na_emb_host), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_status(e);
+  g_na_base[dev] = b;
+  *base = b;
+  return A2C_OK;
+}
+
+__device__ __forceinline__ double na_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double na_block_sum(double v, double *sh) {
+  v = na_warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  v = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
+  if (w == 0) v = na_warp_sum(v);
+  __syncthreads();
+  return v;
+}
+// The objective reduction (the same fixed-partition tree as the context path)
+__global__ void __launch_bounds__(kNaRedBlock) k_na_partial(const double *a, const double *b, int64_t n, double *pa,
+                                                             double *pb) {
+  __shared__ double sh[kNaRedBlock / 32];
+  double sa = 0.0, sb = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    sa += a[i];
+    sb += b[i];
+  }
+  sa = na_block_sum(sa, sh);
+  sb = na_block_sum(sb, sh);
+  if (threadIdx.x == 0) {
+    pa[blockIdx.x] = sa;
+    pb[blockIdx.x] = sb;
+  }
+}
+__global__ void __launch_bounds__(kNaRedBlock) k_na_final(const double *pa, const double *pb, int np, double T,
+                                                           double *f) {
+  __shared__ double sh[kNaRedBlock / 32];
+  double sa = 0.0, sb = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    sa += pa[i];
+    sb += pb[i];
+  }
+  sa = na_block_sum(sa, sh);
+  sb = na_block_sum(sb, sh);
+  if (threadIdx.x == 0) *f = 1.0 / T * sa - 3.0 * kB * sb;
+}
+
+}  // namespace
+}  // namespace a2c
+
+extern "C" a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *c, const double *dX, double *df, double *dG) {
+  using namespace a2c;
+  if (!c || !df || (c->N > 0 && (!dX || !dG))) return A2C_ERR_INVALID;
+  if (c->N > kNaMaxSites) return A2C_ERR_INVALID;  // larger than the fixed scratch array
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_status(e);
+  unsigned char *base = nullptr;
+  A2C_TRY(na_setup(c->device, &base));
+  const int64_t N = c->N;
+  MixArgs a{};
+  a.N = N;
+  a.nPd = c->p.nPd;
+  a.W = (float)c->p.QWp;
+  double k[3];
+  for (int d = 0; d < 3; ++d) {
+    const double S = c->p.periodic[d] ? c->p.box[d] : 64.0;
+    k[d] = 4294967296.0 / S;
+    a.sc[d] = (float)(S / 4294967296.0);
+  }
+  a.P = (const int4 *)(base + kNaP);
+  a.occ = (const float *)(base + kNaOcc);
+  a.off = c->d_off;
+  a.nbr = c->d_nbr;
+  a.npd = c->d_npd;
+  a.tabPair = (const float4 *)(base + kNaTabPair);
+  a.tabEmb = (const float4 *)(base + kNaTabEmb);
+  a.FF = (float2 *)(base + kNaFF);
+  a.G = dG;
+  a.Vs = (double *)(base + kNaVs);
+  a.Ss = (double *)(base + kNaSs);
+  a.T = c->p.T;
+  double *pa = (double *)(base + kNaPart), *pb = pa + kNaRedGrid;
+  // No region needs clearing: every word a kernel reads was written earlier
+  // in this call (P, occupancy, F/F', energy partials, block partials).
+  if (N > 0) {
+    k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], (int4 *)(base + kNaP),
+                                                     (float *)(base + kNaOcc));
+    const int tps = (c->mixed && c->mixed->tps) ? c->mixed->tps : (N < 152 * 2048 ? 4 : 1);
+    switch (tps) {
+      case 1: launch_pair_kernels<1>(a, c->stream, nullptr); break;
+      case 2: launch_pair_kernels<2>(a, c->stream, nullptr); break;
+      case 4: launch_pair_kernels<4>(a, c->stream, nullptr); break;
+      default: launch_pair_kernels<8>(a, c->stream, nullptr); break;
+    }
+  }
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(kNaRedGrid, (N + kNaRedBlock - 1) / kNaRedBlock));
+  k_na_partial<<<grid, kNaRedBlock, 0, c->stream>>>(a.Vs, a.Ss, N, pa, pb);
+  k_na_final<<<1, kNaRedBlock, 0, c->stream>>>(pa, pb, grid, c->p.T, df);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? A2C_OK : cuda_status(e);
+}

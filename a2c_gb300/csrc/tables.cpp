@@ -121,3 +121,27 @@ void build_embed_table(int species, double h, int n, std::vector<float> &out) {
 }
 
 }  // namespace a2c
+
+namespace a2c {
+
+// The same tables written into caller-provided arrays (8n and 4n floats),
+// with no heap allocation.
+void build_pair_table_raw(double r0, double h, int n, float *out) {
+  for (int i = 0; i < n; ++i) {
+    const double xa = r0 + h * i, xb = r0 + h * (i + 1), mid = r0 + h * (i + 0.5);
+    tables::hermite(tables::f_Pd({xa, 1.0}, mid), tables::f_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i]);
+    tables::hermite(tables::phi_Pd({xa, 1.0}, mid), tables::phi_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i + 4]);
+  }
+}
+
+void build_embed_table_raw(int species, double h, int n, float *out) {
+  for (int i = 0; i < n; ++i) {
+    const tables::Dual a = {h * i, 1.0}, b = {h * (i + 1), 1.0};
+    if (species == 0)
+      tables::hermite(tables::F_Pd(a), tables::F_Pd(b), h, &out[(size_t)4 * i]);
+    else
+      tables::hermite(tables::F_H(a), tables::F_H(b), h, &out[(size_t)4 * i]);
+  }
+}
+
+}  // namespace a2c

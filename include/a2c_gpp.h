@@ -140,6 +140,23 @@ a2c_status a2c_gpp_get_shell_counts(a2c_gpp_ctx *ctx, int *PdPdnum);
  * the current state. */
 a2c_status a2c_gpp_eval(a2c_gpp_ctx *ctx, const double *X, double *f, double *G);
 a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG);
+/* Mixed-precision objective and gradient that allocates no device memory,
+ * for callers that cannot call cudaMalloc while they evaluate: a host code
+ * whose device memory belongs to another allocator (a solver framework's
+ * callback running inside its own memory pool) or work being recorded by a
+ * driver that forbids allocation during recording.  It has no counterpart
+ * in the reference.  Inputs dX (4N doubles) and outputs df (1 double), dG
+ * (4N doubles) are device pointers; the context supplies the neighbor lists
+ * (build them first) and the occupancy.  All scratch lives in one fixed
+ * device array of about 5.8 MB that every GPU loading the library keeps until
+ * the process exits, so problems above 131,072 sites are rejected with
+ * A2C_ERR_INVALID.  The first call on a device finds the array's address
+ * and loads constant tables into it (synchronous copies): make that first
+ * call before any stream capture.  Calls share the array and it keeps the
+ * last call's contents; nothing in it needs clearing, but calls that
+ * overlap on the GPU (two streams, two contexts on one device) race.
+ * Stream-ordered on the context's stream, like a2c_gpp_eval_device. */
+a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG);
 /* Profiling aid: one stream-ordered evaluation on device pointers with CUDA
  * events between its launches; stage_ms[4] receives the durations of the
  * state preparation, pass 1 (densities), pass 2 (energy and gradient) and
