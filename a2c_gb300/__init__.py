@@ -26,6 +26,9 @@ class LbfgsResult:
     nfev: int
     gnorm: float
     reason: int
+    mixed_iters: int = 0
+    fp64_iters: int = 0
+    mixed_gnorm: float = 0.0
 
 
 def _f64(a, n=None) -> np.ndarray:
@@ -195,7 +198,9 @@ class Gpp:
         f, it, nfev, gn, why = C.c_double(), C.c_int(), C.c_int(), C.c_double(), C.c_int()
         N.check(self._L.a2c_gpp_minimize(self._h, N.ptr(X), C.byref(lp), C.byref(f), C.byref(it), C.byref(nfev),
                                          C.byref(gn), C.byref(why)), "a2c_gpp_minimize")
-        return LbfgsResult(X, f.value, it.value, nfev.value, gn.value, why.value)
+        mi, fi, mg = C.c_int(), C.c_int(), C.c_double()
+        N.check(self._L.a2c_gpp_minimize_stats(self._h, C.byref(mi), C.byref(fi), C.byref(mg)), "a2c_gpp_minimize_stats")
+        return LbfgsResult(X, f.value, it.value, nfev.value, gn.value, why.value, mi.value, fi.value, mg.value)
 
     # -- occupancy dynamics --------------------------------------------------
     def chem_potential(self, gamma_bd: float, gamma, full_H) -> tuple[np.ndarray, np.ndarray]:

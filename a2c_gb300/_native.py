@@ -28,6 +28,7 @@ A2C_MIXED = 1
 LIST_PDPD, LIST_PDH, LIST_HPD, LIST_HH, LIST_HH1 = range(5)
 
 CONVERGED_GATOL = 3
+CONVERGED_STALLED = 6
 DIVERGED_MAXITS = -2
 DIVERGED_NAN = -4
 DIVERGED_MAXFCN = -5
@@ -48,6 +49,7 @@ class LbfgsParams(C.Structure):
     _fields_ = [
         ("m", C.c_int), ("max_it", C.c_int), ("max_fev", C.c_int), ("max_ls", C.c_int),
         ("gatol", C.c_double), ("c1", C.c_double), ("init_step", C.c_double), ("sigma_lb", C.c_double),
+        ("f_noise", C.c_double), ("polish", C.c_int), ("stall_window", C.c_int), ("stall_rtol", C.c_double),
     ]
 
 
@@ -105,6 +107,7 @@ def lib() -> C.CDLL:
         "a2c_gpp_minimize": (I, [P, P, C.POINTER(LbfgsParams), C.POINTER(D), C.POINTER(I), C.POINTER(I),
                                  C.POINTER(D), C.POINTER(I)]),
         "a2c_gpp_chem_potential": (I, [P, D, P, P]),
+        "a2c_gpp_minimize_stats": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(D)]),
         "a2c_gpp_apply_dirichlet": (I, [P, P, I, D, D, P, P]),
         "a2c_gpp_diffuse": (I, [P, D, D, D, D, D, P, P, P]),
         "a2c_gpp_macro_results": (I, [P, P, P, I, C.POINTER(D), C.POINTER(D)]),
@@ -127,7 +130,7 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_get_occupancy", "a2c_gpp_set_state", "a2c_gpp_get_state", "a2c_gpp_build_neighbors",
             "a2c_gpp_neighbor_total", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
             "a2c_gpp_eval_device", "a2c_gpp_profile_eval", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
-            "a2c_gpp_chem_potential", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",
+            "a2c_gpp_chem_potential", "a2c_gpp_minimize_stats", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",
             "a2c_lattice_fcc", "a2c_gpp_peak_flops"]
 
 

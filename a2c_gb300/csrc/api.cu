@@ -128,6 +128,10 @@ void a2c_lbfgs_default_params(a2c_lbfgs_params *p) {
   p->c1 = 1.0e-4;
   p->init_step = 1.0e-2;
   p->sigma_lb = 1.0e-6;
+  p->f_noise = 0.0;
+  p->polish = 1;
+  p->stall_window = 50;
+  p->stall_rtol = 0.0;
 }
 
 const char *a2c_status_string(a2c_status s) {
@@ -445,6 +449,14 @@ a2c_status a2c_gpp_minimize(a2c_gpp_ctx *c, double *X, const a2c_lbfgs_params *l
   c->has_density = false;
   if (c->N > 0) A2C_CUDA(cudaMemcpyAsync(X, c->d_X, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToHost, c->stream));
   return finish(c);
+}
+
+a2c_status a2c_gpp_minimize_stats(a2c_gpp_ctx *c, int *mixed_iters, int *fp64_iters, double *mixed_gnorm) {
+  if (!c) return A2C_ERR_INVALID;
+  if (mixed_iters) *mixed_iters = c->last_mixed_iters;
+  if (fp64_iters) *fp64_iters = c->last_fp64_iters;
+  if (mixed_gnorm) *mixed_gnorm = c->last_mixed_gnorm;
+  return A2C_OK;
 }
 
 a2c_status a2c_gpp_chem_potential(a2c_gpp_ctx *c, double gamma_bd, double *gamma, int *full_H) {

@@ -66,6 +66,8 @@ struct a2c_gpp_ctx {
   int64_t h_pinned_n;
   a2c::Mixed *mixed;
   a2c::Lbfgs *lbfgs;
+  int last_mixed_iters, last_fp64_iters;
+  double last_mixed_gnorm;
 };
 
 namespace a2c {

@@ -7,8 +7,16 @@
 //   d  = -H pg by the two-loop recursion over the last m pairs, H0 =
 //        (s.y / y.y) I; zero on the active set; with no pairs (or if d is
 //        not a descent direction) d = -pg * init_step / max|pg|
-//   backtracking projected Armijo search from alpha = 1, halving
+//   backtracking projected Armijo search from alpha = 1, halving; when the
+//   objective change is below its noise level (|f_new - f| <= f_noise |f|)
+//   the step is accepted by the derivative form of the Armijo test,
+//   g_new.s <= (2 c1 - 1) g.s, exact for a quadratic (the approximate-Wolfe
+//   idea of Hager and Zhang, 2005) -- this keeps the mixed-precision form,
+//   whose objective carries FP32 rounding noise, converging on its gradient
 //   pair (s, y) kept when s.y > 2^-52 y.y
+// Mixed precision with `polish`: when the mixed phase stops (gatol reached
+// on the mixed gradient, or a failed line search), the iteration continues
+// from the same point and memory with FP64 evaluations until gatol.
 // All vector algebra is FP64 with fixed-partition (deterministic) block
 // reductions; the objective is whichever form the context evaluates.
 #include <algorithm>
@@ -190,6 +198,20 @@ __global__ void __launch_bounds__(kBlock) k_pair(const double *x, const double *
   }
 }
 
+// part = g_new . (xn - x)
+__global__ void __launch_bounds__(kBlock) k_dot_step(const double *gn, const double *xn, const double *x, int64_t n,
+                                                      double *part) {
+  __shared__ double sh[kBlock / 32];
+  double s = 0.0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    s += gn[t] * (xn[t] - x[t]);
+  s = bred<false>(s, sh);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s;
+    part[2 * blockIdx.x + 1] = 0.0;
+  }
+}
+
 __global__ void k_project(double *x, int64_t n, double lb) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
     if ((t & 3) == 3 && x[t] < lb) x[t] = lb;
@@ -249,96 +271,139 @@ a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp
 
   A2C_CUDA(cudaMemcpyAsync(L->x, dX, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   k_project<<<gr, kBlock, 0, st>>>(L->x, n, lb);
+  const int saved_precision = c->p.precision;
   int fev = 0;
-  A2C_TRY(eval_device_impl(c, L->x, L->f, L->g));
-  ++fev;
-  double f;
-  A2C_TRY(fetch(L->f, &f, 1));
+  double f = 0.0;
   // pairs occupy slots head-1, ..., head-npairs (mod m+1); slot head is free,
   // so a rejected pair never overwrites a live one
   std::vector<double> rhoS(ring, 0.0);
   int npairs = 0, head = 0, it = 0, why = 0;
   double gnorm = 0.0;
-  while (true) {
-    k_projgrad<<<gr, kBlock, 0, st>>>(L->x, L->g, L->pg, n, lb, part);
-    k_final_sum_max<<<1, kBlock, 0, st>>>(part, gr, scal);
-    double sm[2];
-    A2C_TRY(fetch(scal, sm, 2));
-    gnorm = std::sqrt(sm[0]);
-    const double amax = sm[1];
-    if (!std::isfinite(f) || !std::isfinite(gnorm)) { why = A2C_DIVERGED_NAN; break; }
-    if (gnorm <= lp->gatol) { why = A2C_CONVERGED_GATOL; break; }
-    if (it >= lp->max_it) { why = A2C_DIVERGED_MAXITS; break; }
-    if (fev >= lp->max_fev) { why = A2C_DIVERGED_MAXFCN; break; }
-    auto steepest = [&]() { k_scale<<<gr, kBlock, 0, st>>>(L->pg, -lp->init_step / amax, L->d, n); };
-    if (npairs == 0) {
-      steepest();
-    } else {
-      // two-loop recursion; alpha_j kept in scal[4 + j]
-      A2C_CUDA(cudaMemcpyAsync(L->d, L->pg, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-      for (int k = 0; k < npairs; ++k) {
-        const int sl = ((head - 1 - k) % ring + ring) % ring;
-        dot2(L->S + (size_t)sl * n, L->d, nullptr, nullptr, scal + 2);
-        k_scale<<<1, 1, 0, st>>>(scal + 2, rhoS[sl], scal + 4 + sl, 1);  // alpha = rho (s . q)
-        k_axpy_dev<<<gr, kBlock, 0, st>>>(L->d, L->Y + (size_t)sl * n, scal + 4 + sl, 1.0, n);
+  c->last_mixed_iters = c->last_fp64_iters = 0;
+  c->last_mixed_gnorm = 0.0;
+
+  std::vector<double> fhist;  // f after each accepted iteration of the phase
+  auto phase = [&](double f_noise, double stall_rtol) -> a2c_status {
+    fhist.clear();
+    A2C_TRY(eval_device_impl(c, L->x, L->f, L->g));
+    ++fev;
+    A2C_TRY(fetch(L->f, &f, 1));
+    while (true) {
+      k_projgrad<<<gr, kBlock, 0, st>>>(L->x, L->g, L->pg, n, lb, part);
+      k_final_sum_max<<<1, kBlock, 0, st>>>(part, gr, scal);
+      double sm[2];
+      A2C_TRY(fetch(scal, sm, 2));
+      gnorm = std::sqrt(sm[0]);
+      const double amax = sm[1];
+      if (!std::isfinite(f) || !std::isfinite(gnorm)) { why = A2C_DIVERGED_NAN; break; }
+      if (gnorm <= lp->gatol) { why = A2C_CONVERGED_GATOL; break; }
+      if (it >= lp->max_it) { why = A2C_DIVERGED_MAXITS; break; }
+      if (fev >= lp->max_fev) { why = A2C_DIVERGED_MAXFCN; break; }
+      auto steepest = [&]() { k_scale<<<gr, kBlock, 0, st>>>(L->pg, -lp->init_step / amax, L->d, n); };
+      if (npairs == 0) {
+        steepest();
+      } else {
+        // two-loop recursion; alpha_j kept in scal[4 + j]
+        A2C_CUDA(cudaMemcpyAsync(L->d, L->pg, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        for (int k = 0; k < npairs; ++k) {
+          const int sl = ((head - 1 - k) % ring + ring) % ring;
+          dot2(L->S + (size_t)sl * n, L->d, nullptr, nullptr, scal + 2);
+          k_scale<<<1, 1, 0, st>>>(scal + 2, rhoS[sl], scal + 4 + sl, 1);  // alpha = rho (s . q)
+          k_axpy_dev<<<gr, kBlock, 0, st>>>(L->d, L->Y + (size_t)sl * n, scal + 4 + sl, 1.0, n);
+        }
+        const int nw = ((head - 1) % ring + ring) % ring;
+        double sy_yy[2];
+        dot2(L->S + (size_t)nw * n, L->Y + (size_t)nw * n, L->Y + (size_t)nw * n, L->Y + (size_t)nw * n, scal + 2);
+        A2C_TRY(fetch(scal + 2, sy_yy, 2));
+        k_scale<<<gr, kBlock, 0, st>>>(L->d, sy_yy[0] / sy_yy[1], L->d, n);
+        for (int k = npairs - 1; k >= 0; --k) {
+          const int sl = ((head - 1 - k) % ring + ring) % ring;
+          dot2(L->Y + (size_t)sl * n, L->d, nullptr, nullptr, scal + 2);
+          k_axpy_ab<<<gr, kBlock, 0, st>>>(L->d, L->S + (size_t)sl * n, scal + 4 + sl, scal + 2, rhoS[sl], n);
+        }
+        k_neg_mask<<<gr, kBlock, 0, st>>>(L->d, L->x, L->g, n, lb);
       }
-      const int nw = ((head - 1) % ring + ring) % ring;
-      double sy_yy[2];
-      dot2(L->S + (size_t)nw * n, L->Y + (size_t)nw * n, L->Y + (size_t)nw * n, L->Y + (size_t)nw * n, scal + 2);
-      A2C_TRY(fetch(scal + 2, sy_yy, 2));
-      k_scale<<<gr, kBlock, 0, st>>>(L->d, sy_yy[0] / sy_yy[1], L->d, n);
-      for (int k = npairs - 1; k >= 0; --k) {
-        const int sl = ((head - 1 - k) % ring + ring) % ring;
-        dot2(L->Y + (size_t)sl * n, L->d, nullptr, nullptr, scal + 2);
-        k_axpy_ab<<<gr, kBlock, 0, st>>>(L->d, L->S + (size_t)sl * n, scal + 4 + sl, scal + 2, rhoS[sl], n);
-      }
-      k_neg_mask<<<gr, kBlock, 0, st>>>(L->d, L->x, L->g, n, lb);
-    }
-    double gd[2];
-    dot2(L->g, L->d, nullptr, nullptr, scal + 2);
-    A2C_TRY(fetch(scal + 2, gd, 1));
-    if (!(gd[0] < 0.0)) {
-      npairs = 0;
-      head = 0;
-      steepest();
-    }
-    double alpha = 1.0, fn = 0.0;
-    bool ok = false;
-    for (int ls = 0; ls < lp->max_ls; ++ls) {
-      k_trial<<<gr, kBlock, 0, st>>>(L->x, L->d, L->g, alpha, lb, L->xn, n, part);
-      k_final_sum2<<<1, kBlock, 0, st>>>(part, gr, scal + 2);
-      A2C_TRY(eval_device_impl(c, L->xn, L->fn, L->gn));
-      ++fev;
-      double v[2];
-      A2C_TRY(fetch(scal + 2, v, 1));
-      A2C_TRY(fetch(L->fn, &fn, 1));
-      if (std::isfinite(fn) && fn <= f + lp->c1 * v[0]) { ok = true; break; }
-      alpha *= 0.5;
-      if (fev >= lp->max_fev) break;
-    }
-    if (!ok) {
-      if (npairs > 0 && fev < lp->max_fev) {
+      double gd[2];
+      dot2(L->g, L->d, nullptr, nullptr, scal + 2);
+      A2C_TRY(fetch(scal + 2, gd, 1));
+      if (!(gd[0] < 0.0)) {
         npairs = 0;
         head = 0;
-        continue;
+        steepest();
       }
-      why = (fev >= lp->max_fev) ? A2C_DIVERGED_MAXFCN : A2C_DIVERGED_LS_FAILURE;
-      break;
+      double alpha = 1.0, fn = 0.0;
+      bool ok = false;
+      for (int ls = 0; ls < lp->max_ls; ++ls) {
+        k_trial<<<gr, kBlock, 0, st>>>(L->x, L->d, L->g, alpha, lb, L->xn, n, part);
+        k_final_sum2<<<1, kBlock, 0, st>>>(part, gr, scal + 2);
+        A2C_TRY(eval_device_impl(c, L->xn, L->fn, L->gn));
+        ++fev;
+        double v[2];
+        A2C_TRY(fetch(scal + 2, v, 1));
+        A2C_TRY(fetch(L->fn, &fn, 1));
+        if (std::isfinite(fn) && fn <= f + lp->c1 * v[0]) { ok = true; break; }
+        if (std::isfinite(fn) && std::fabs(fn - f) <= f_noise * std::fabs(f)) {
+          double dn[2];
+          k_dot_step<<<gr, kBlock, 0, st>>>(L->gn, L->xn, L->x, n, part);
+          k_final_sum2<<<1, kBlock, 0, st>>>(part, gr, scal + 2);
+          A2C_TRY(fetch(scal + 2, dn, 1));
+          if (dn[0] <= (2.0 * lp->c1 - 1.0) * v[0]) { ok = true; break; }
+        }
+        alpha *= 0.5;
+        if (fev >= lp->max_fev) break;
+      }
+      if (!ok) {
+        if (npairs > 0 && fev < lp->max_fev) {
+          npairs = 0;
+          head = 0;
+          continue;
+        }
+        why = (fev >= lp->max_fev) ? A2C_DIVERGED_MAXFCN : A2C_DIVERGED_LS_FAILURE;
+        break;
+      }
+      k_pair<<<gr, kBlock, 0, st>>>(L->x, L->xn, L->g, L->gn, L->S + (size_t)head * n, L->Y + (size_t)head * n, n,
+                                    part);
+      k_final_sum2<<<1, kBlock, 0, st>>>(part, gr, scal + 2);
+      double sy[2];
+      A2C_TRY(fetch(scal + 2, sy, 2));
+      if (sy[0] > 2.220446049250313e-16 * sy[1]) {
+        rhoS[head] = 1.0 / sy[0];
+        head = (head + 1) % ring;
+        if (npairs < m) ++npairs;
+      }
+      std::swap(L->x, L->xn);
+      std::swap(L->g, L->gn);
+      f = fn;
+      ++it;
+      fhist.push_back(f);
+      const int W = lp->stall_window;
+      if (W > 0 && (int)fhist.size() > W && fhist[fhist.size() - 1 - W] - f <= stall_rtol * std::fabs(f)) {
+        why = A2C_CONVERGED_STALLED;
+        break;
+      }
     }
-    k_pair<<<gr, kBlock, 0, st>>>(L->x, L->xn, L->g, L->gn, L->S + (size_t)head * n, L->Y + (size_t)head * n, n, part);
-    k_final_sum2<<<1, kBlock, 0, st>>>(part, gr, scal + 2);
-    double sy[2];
-    A2C_TRY(fetch(scal + 2, sy, 2));
-    if (sy[0] > 2.220446049250313e-16 * sy[1]) {
-      rhoS[head] = 1.0 / sy[0];
-      head = (head + 1) % ring;
-      if (npairs < m) ++npairs;
+    return A2C_OK;
+  };
+
+  a2c_status st_run;
+  if (saved_precision == A2C_MIXED) {
+    st_run = phase(lp->f_noise > 0.0 ? lp->f_noise : 1.0e-7, lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-10);
+    c->last_mixed_iters = it;
+    c->last_mixed_gnorm = gnorm;
+    if (st_run == A2C_OK && lp->polish &&
+        (why == A2C_CONVERGED_GATOL || why == A2C_DIVERGED_LS_FAILURE || why == A2C_CONVERGED_STALLED)) {
+      c->p.precision = A2C_FP64;
+      const int it0 = it;
+      st_run = phase(lp->f_noise > 0.0 ? lp->f_noise : 1.0e-14, lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-14);
+      c->last_fp64_iters = it - it0;
+      c->p.precision = saved_precision;
     }
-    std::swap(L->x, L->xn);
-    std::swap(L->g, L->gn);
-    f = fn;
-    ++it;
+  } else {
+    st_run = phase(lp->f_noise > 0.0 ? lp->f_noise : 1.0e-14, lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-14);
+    c->last_fp64_iters = it;
   }
+  c->p.precision = saved_precision;
+  A2C_TRY(st_run);
   A2C_CUDA(cudaMemcpyAsync(dX, L->x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   A2C_CUDA(cudaStreamSynchronize(st));
   *fmin = f;

@@ -58,6 +58,31 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(v: float, world: int, device=None) -> float:
+    """The slowest rank's value (device time) -- the only collective: it is
+    timing bookkeeping, not part of the evaluator's data path."""
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(sites_per_rank: int, steps: int, world: int, max_time_s: float) -> float:
+    """Replicas (weak scaling): every rank evaluates its own lattice of
+    `sites_per_rank` sites `steps` times; atom-evals of all ranks divided by
+    the slowest rank's time."""
+    return world * sites_per_rank * steps / max_time_s
+
+
+def replica_seed(base: int, rank: int) -> int:
+    """Each rank draws an independent replica of the workload."""
+    return base + rank
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -144,6 +169,57 @@ def cpu_sample(threads: int, seconds: float = 10.0, max_evals: int = 50):
     return (nPd + nH) * n / dt, n, nPd + nH
 
 
+def nucleus_lattice(cells: int, seed: int = 3):
+    """The mixed-minimization workload drawn at `cells`^3 cells: a spherical
+    hydride nucleus (x = 0.60) with a 5 A tanh interface in an x = 0.02
+    matrix, radius 80 A at 64^3 cells scaled with the box; N(0, 0.02 A)
+    positions, sigma = 0.10 A, periodic, T = 300 K."""
+    import a2c_gb300 as A
+
+    return A.lattice_fcc(cells, periodic=(1, 1, 1), pos_std=0.02, sigma=(0.1, 0.1), x_mode=1, x_matrix=0.02,
+                         x_nucleus=0.60, nucleus_radius=80.0 * cells / 64.0, interface_width=5.0, x_half=0.0,
+                         seed=seed)
+
+
+def time_to_minimum(cells: int, gatol: float, device: int):
+    """Wall time of a2c_gpp_minimize to gatol in FP64 and in mixed precision
+    (mixed phase then FP64 polish), and the mixed result's distance from the
+    FP64 minimum."""
+    import numpy as np
+
+    import a2c_gb300 as A
+
+    X, xH, _, box, nPd, nH = nucleus_lattice(cells)
+    out = {"cells": cells, "sites": nPd + nH, "gatol": gatol}
+    with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), device=device) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        g.eval(X)  # warm-up (lazy set-up of both forms)
+        g.set_precision("mixed")
+        g.eval(X)
+        g.set_precision("fp64")
+        t0 = time.perf_counter()
+        r64 = g.minimize(X, gatol=gatol, max_it=20000, max_fev=40000)
+        t64 = time.perf_counter() - t0
+        g.set_precision("mixed")
+        t0 = time.perf_counter()
+        rmx = g.minimize(X, gatol=gatol, max_it=20000, max_fev=40000)
+        tmx = time.perf_counter() - t0
+        g.set_precision("fp64")
+        f_at_mixed, _ = g.eval(rmx.X)
+    dq = float(np.abs(rmx.X.reshape(-1, 4)[:, :3] - r64.X.reshape(-1, 4)[:, :3]).max())
+    ds = float(np.abs(rmx.X.reshape(-1, 4)[:, 3] - r64.X.reshape(-1, 4)[:, 3]).max())
+    out.update({"fp64": {"seconds": t64, "iters": r64.iters, "nfev": r64.nfev, "reason": r64.reason,
+                         "gnorm": r64.gnorm, "f": r64.fmin},
+                "mixed": {"seconds": tmx, "iters": rmx.iters, "mixed_iters": rmx.mixed_iters,
+                          "fp64_polish_iters": rmx.fp64_iters, "mixed_phase_gnorm": rmx.mixed_gnorm,
+                          "nfev": rmx.nfev, "reason": rmx.reason, "gnorm": rmx.gnorm},
+                "speedup": t64 / tmx,
+                "mixed_vs_fp64": {"free_entropy_rel": abs(f_at_mixed - r64.fmin) / abs(r64.fmin),
+                                  "max_position_A": dq, "max_sigma_A": ds}})
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -202,7 +278,7 @@ def run_ours(args):
     w = WORKLOAD
     X, xH, _, box, nPd, nH = A.lattice_fcc(w["ncell"], periodic=w["periodic"], pos_std=w["pos_std"],
                                            sigma=w["sigma"], x_center=w["x_center"], x_half=w["x_half"],
-                                           seed=w["seed"] + rank)
+                                           seed=replica_seed(w["seed"], rank))
     Ns = nPd + nH
     g = A.Gpp(nPd, nH, box=box, periodic=w["periodic"], precision="mixed", device=dev)
     g.set_occupancy(xH)
@@ -266,19 +342,10 @@ def run_ours(args):
     G_64 = dG.cpu().numpy()
     g.set_precision("mixed")
 
-    def max_over_ranks(v):
-        if world == 1:
-            return v
-        import torch.distributed as dist
-
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    dev_time_mixed = max_over_ranks(float(st_mixed.sum()) * 1e-3)
-    dev_time_64 = max_over_ranks(float(st_64.sum()) * 1e-3)
-    value = world * Ns * args.steps / dev_time_mixed
-    value_64 = world * Ns * args.fp64_steps / dev_time_64
+    dev_time_mixed = max_over_ranks(float(st_mixed.sum()) * 1e-3, world, dev)
+    dev_time_64 = max_over_ranks(float(st_64.sum()) * 1e-3, world, dev)
+    value = whole_job_value(Ns, args.steps, world, dev_time_mixed)
+    value_64 = whole_job_value(Ns, args.fp64_steps, world, dev_time_64)
 
     # end to end through the public host-pointer entry point
     Xp = torch.empty(4 * Ns, dtype=torch.float64, pin_memory=True)
@@ -306,9 +373,9 @@ def run_ours(args):
         t0 = time.perf_counter()
         e2e_step()
         e2e_t.append(time.perf_counter() - t0)
-    e2e_time = max_over_ranks(sum(e2e_t))
+    e2e_time = max_over_ranks(sum(e2e_t), world, dev)
     fbuf[0] = fval.value
-    e2e_value = world * Ns * args.steps / e2e_time
+    e2e_value = whole_job_value(Ns, args.steps, world, e2e_time)
 
     # roofline of the dominant kernel (pass 2) from the timed steps
     pass2_ms = float(np.mean(st_mixed[:, 2]))
@@ -349,6 +416,9 @@ def run_ours(args):
                          f"oracle with the reference's arithmetic and redundant FD calls, OpenMP"}
 
     g.close()
+    ttm = None
+    if world == 1 and args.ttm_cells > 0:
+        ttm = time_to_minimum(args.ttm_cells, 1e-6, dev)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_time_mixed * 1e3 / args.steps, "higher_is_better": True,
@@ -364,7 +434,8 @@ def run_ours(args):
                 "mixed_over_fp64": value / value_64,
                 "mixed_error_vs_fp64": {"free_entropy_rel": rel_f, "gradient_rel_2norm": rel_g},
                 "stages_ms_mixed": {"prep": float(np.mean(st_mixed[:, 0])), "pass1": pass1_ms, "pass2": pass2_ms,
-                                    "reduce": float(np.mean(st_mixed[:, 3]))}}
+                                    "reduce": float(np.mean(st_mixed[:, 3]))},
+                "time_to_minimum": ttm}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
@@ -411,12 +482,17 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
-    ap.add_argument("--case", choices=["bench", "profile"], default="bench",
+    ap.add_argument("--ttm-cells", type=int, default=12,
+                    help="time-to-minimum leg on a cells^3 nucleus lattice (0 = skip; 64 = the full 2,097,152 sites)")
+    ap.add_argument("--case", choices=["bench", "profile", "ttm"], default="bench",
                     help="profile: the small untimed case used for ncu captures")
     ap.add_argument("--case-cells", type=int, default=40)
     args = ap.parse_args()
     if args.case == "profile":
         return run_profile_case(args)
+    if args.case == "ttm":
+        print(json.dumps({"time_to_minimum": time_to_minimum(args.ttm_cells, 1e-6, dist_env()[2])}))
+        return 0
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -52,6 +52,7 @@ enum { A2C_LIST_PDPD = 0, A2C_LIST_PDH = 1, A2C_LIST_HPD = 2, A2C_LIST_HH = 3, A
 /* L-BFGS termination reasons, numbered like TaoConvergedReason. */
 enum {
   A2C_CONVERGED_GATOL = 3,
+  A2C_CONVERGED_STALLED = 6, /* no objective progress (like TAO's steptol) */
   A2C_CONTINUE = 0,
   A2C_DIVERGED_MAXITS = -2,
   A2C_DIVERGED_NAN = -4,
@@ -87,6 +88,14 @@ typedef struct a2c_lbfgs_params {
   double c1;        /* Armijo constant */
   double init_step; /* max |component| of a steepest-descent step */
   double sigma_lb;  /* lower bound on widths (minimizer.cpp:815, 822) */
+  double f_noise;   /* relative objective noise: a step whose |f change| is
+                       below f_noise*|f| is accepted by the derivative form of
+                       the Armijo test; 0 = 1e-14 (FP64) or 1e-7 (mixed) */
+  int polish;       /* mixed precision: after the mixed phase stops, continue
+                       with FP64 evaluations to gatol (1) or not (0) */
+  int stall_window; /* stop (A2C_CONVERGED_STALLED) when f fell by no more
+                       than stall_rtol*|f| over this many iterations */
+  double stall_rtol;/* 0 = 1e-14 (FP64) or 1e-10 (mixed phase) */
 } a2c_lbfgs_params;
 
 typedef struct a2c_gpp_ctx a2c_gpp_ctx;
@@ -175,6 +184,9 @@ a2c_status a2c_gpp_eam_eval(a2c_gpp_ctx *ctx, int which, const double *in, int64
 
 /* Variable bounds: q free, sigma >= 1e-6 (minimizer.cpp:804-830). */
 a2c_status a2c_gpp_bounds(a2c_gpp_ctx *ctx, double *lb, double *ub);
+
+/* Iterations of the last a2c_gpp_minimize spent in each precision. */
+a2c_status a2c_gpp_minimize_stats(a2c_gpp_ctx *ctx, int *mixed_iters, int *fp64_iters, double *mixed_gnorm);
 
 /* Bound-constrained L-BFGS from X (in/out) on the device; replaces
  * Minimizer::minimizeFreeEntropy + TaoSolve (minimizer.cpp:548-586).

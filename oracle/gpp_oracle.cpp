@@ -857,6 +857,9 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
   if (!check_params(p) || !lp || lp->m < 1) return 1;
   const int64_t n = 4 * ((int64_t)p->nPd + p->nH);
   const double lb = lp->sigma_lb;
+  const double f_noise = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-14;
+  const double stall_rtol = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-14;
+  std::vector<double> fhist;  // f after each accepted iteration
   auto is_sig = [](int64_t t) { return (t & 3) == 3; };
   auto project = [&](std::vector<double> &v) {
     for (int64_t t = 3; t < n; t += 4)
@@ -938,6 +941,16 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
       else
         for (int64_t t = 0; t < n; ++t) dec += g[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]);
       if (std::isfinite(fn) && fn <= f + lp->c1 * dec) { ok = true; break; }
+      // objective change within its noise: the derivative form of the
+      // Armijo test, g_new.s <= (2 c1 - 1) g.s (exact for a quadratic)
+      if (std::isfinite(fn) && std::fabs(fn - f) <= f_noise * std::fabs(f)) {
+        double dn = 0.0;
+        if (g_arith)
+          dn = gpu_tree_sum(n, 512, [&](int64_t t) { return gn[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]); });
+        else
+          for (int64_t t = 0; t < n; ++t) dn += gn[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]);
+        if (dn <= (2.0 * lp->c1 - 1.0) * dec) { ok = true; break; }
+      }
       alpha *= 0.5;
       if (nfev >= lp->max_fev) break;
     }
@@ -967,6 +980,12 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
     g.swap(gn);
     f = fn;
     ++it;
+    fhist.push_back(f);
+    const int W = lp->stall_window;
+    if (W > 0 && (int)fhist.size() > W && fhist[fhist.size() - 1 - W] - f <= stall_rtol * std::fabs(f)) {
+      why = 6;
+      break;
+    }
   }
   std::memcpy(X, x.data(), sizeof(double) * (size_t)n);
   *fmin = f;

@@ -56,6 +56,9 @@ typedef struct orc_lbfgs {
   double c1;        /* Armijo constant */
   double init_step; /* max |displacement| of the first (steepest) step */
   double sigma_lb;  /* lower bound on widths */
+  double f_noise;   /* relative objective noise for the derivative Armijo form; 0 = 1e-14 */
+  int stall_window; /* stop (6) when f fell by <= stall_rtol*|f| over this many iterations */
+  double stall_rtol;/* 0 = 1e-14 */
 } orc_lbfgs;
 
 /* Arithmetic mode: 0 = the reference's (C library exp/pow/log, sequential

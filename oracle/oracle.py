@@ -42,7 +42,8 @@ class OrcParams(C.Structure):
 
 class OrcLbfgs(C.Structure):
     _fields_ = [("m", C.c_int), ("max_it", C.c_int), ("max_fev", C.c_int), ("max_ls", C.c_int), ("gatol", D),
-                ("c1", D), ("init_step", D), ("sigma_lb", D)]
+                ("c1", D), ("init_step", D), ("sigma_lb", D), ("f_noise", D), ("stall_window", C.c_int),
+                ("stall_rtol", D)]
 
 
 def _p(a):
@@ -231,8 +232,8 @@ def macro_results(x, HSurf):
 
 
 def minimize(pb: Problem, X, xH, off, nbr, *, m=5, max_it=10000, max_fev=20000, max_ls=30, gatol=1e-6, c1=1e-4,
-             init_step=1e-2, sigma_lb=1e-6, threads=None):
-    lp = OrcLbfgs(m, max_it, max_fev, max_ls, gatol, c1, init_step, sigma_lb)
+             init_step=1e-2, sigma_lb=1e-6, f_noise=0.0, stall_window=50, stall_rtol=0.0, threads=None):
+    lp = OrcLbfgs(m, max_it, max_fev, max_ls, gatol, c1, init_step, sigma_lb, f_noise, stall_window, stall_rtol)
     X = np.ascontiguousarray(X, dtype=np.float64).copy()
     xH = np.ascontiguousarray(xH, dtype=np.float64)
     f, it, nf, gn, why = C.c_double(), C.c_int(), C.c_int(), C.c_double(), C.c_int()

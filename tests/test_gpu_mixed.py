@@ -54,8 +54,13 @@ def test_mixed_objective_gradient(gpu, case):
 
 
 def test_mixed_minimize_close_to_fp64(gpu):
-    """Mixed-precision L-BFGS (FP64 vector algebra) converges to the FP64
-    minimum: free entropy within 1e-6 relative, positions within 1e-4 A."""
+    """Mixed-precision L-BFGS (FP32 evaluator, FP64 vector algebra) reaches
+    the FP64 minimum.  Without polish it stops at the mixed gradient's noise
+    floor; with polish (the default) it finishes with FP64 evaluations to
+    gatol.  Bounds: free entropy within 1e-6 relative of the FP64 minimum;
+    positions within 1e-3 A -- the resolution gatol = 1e-6 leaves on this
+    lattice: two FP64 runs that differ only in the last bit of exp end 2e-4 A
+    apart (measured with the oracle)."""
     X, xH, box, per, nPd, nH, pb = make("config1_6cube")
     kw = dict(m=5, max_it=2000, gatol=1e-6)
     with A.Gpp(nPd, nH, box=box, periodic=per) as g:
@@ -63,12 +68,18 @@ def test_mixed_minimize_close_to_fp64(gpu):
         g.build_neighbors(X)
         r64 = g.minimize(X, **kw)
         g.set_precision("mixed")
-        rmx = g.minimize(X, **dict(kw, gatol=2e-6))
+        rmx = g.minimize(X, **kw)
+        rraw = g.minimize(X, **dict(kw, polish=0))
         g.set_precision("fp64")
-        f_at_mixed, _ = g.eval(rmx.X)
+        f_at_mixed, G_at_mixed = g.eval(rmx.X)
+        f_at_raw, _ = g.eval(rraw.X)
     dq = np.abs(rmx.X.reshape(-1, 4)[:, :3] - r64.X.reshape(-1, 4)[:, :3]).max()
-    print(f"fp64: it={r64.iters} f={r64.fmin:.12e} reason={r64.reason}; mixed: it={rmx.iters} f={rmx.fmin:.12e} "
-          f"reason={rmx.reason}; fp64 objective at the mixed minimum {f_at_mixed:.12e}; max|dq|={dq:.2e}")
-    assert r64.reason == 3
+    dq_raw = np.abs(rraw.X.reshape(-1, 4)[:, :3] - r64.X.reshape(-1, 4)[:, :3]).max()
+    print(f"fp64: it={r64.iters} f={r64.fmin:.12e} reason={r64.reason}; mixed+polish: it={rmx.iters} "
+          f"(mixed {rmx.mixed_iters}, fp64 {rmx.fp64_iters}, mixed |g| {rmx.mixed_gnorm:.2e}) reason={rmx.reason} "
+          f"max|dq|={dq:.2e}; mixed only: it={rraw.iters} reason={rraw.reason} |g|={rraw.gnorm:.2e} "
+          f"max|dq|={dq_raw:.2e} rel df={abs(f_at_raw - r64.fmin) / abs(r64.fmin):.1e}")
+    assert r64.reason == 3 and rmx.reason == 3
     assert abs(f_at_mixed - r64.fmin) <= 1e-6 * abs(r64.fmin)
-    assert dq < 1e-4
+    assert abs(f_at_raw - r64.fmin) <= 1e-6 * abs(r64.fmin)
+    assert dq < 1e-3
