@@ -18,7 +18,10 @@
 // u-weighted differences), multiplied by D once per neighbor.
 //
 // Functions: f_Pd and phi_Pd from the FP32 cubic Hermite tables of
-// tables.cpp (their polynomial forms cancel catastrophically in FP32);
+// tables.cpp (their polynomial forms cancel catastrophically in FP32), held
+// in shared memory: the kernels are persistent, each block loads the 30 KB
+// of tables once and then walks many sites -- from global memory the
+// data-dependent table gathers (28 sectors per request) saturated the L1;
 // f_H, phi_PdH, phi_H analytically with ex2.approx (their exponential tails
 // beyond 5.35 A are C1 continuations, selected branch-free); F and F' per
 // site from FP32 Hermite tables in rho.
@@ -43,7 +46,8 @@ struct Mixed {
   int4 *P = nullptr;        // per site: fixed-point x, y, z; sigma (FP32 bits)
   float *occ = nullptr;     // per site occupancy (1 for Pd)
   float2 *FF = nullptr;     // per site (F'(rho), F(rho))
-  float4 *tabPair = nullptr;  // per r interval: f_Pd cubic, phi_Pd cubic
+  float4 *tabPair = nullptr;  // kTabN f_Pd cubics, then kTabN phi_Pd cubics
+  int grid_cap[9] = {};       // persistent grid size per threads-per-site
   float4 *tabEmb = nullptr;   // per rho interval: F_Pd cubics, then F_H cubics
   int tps = 0;                // threads per site (0 = choose)
 };
@@ -51,8 +55,8 @@ struct Mixed {
 namespace {
 
 constexpr double kTabR0 = 1.0;
-constexpr double kTabInvH = 320.0;
-constexpr int kTabN = 2240;  // r in [1, 8)
+constexpr double kTabInvH = 160.0;
+constexpr int kTabN = 960;  // r in [1, 7): knots on the 5.0 / 5.05 A branch points
 constexpr double kEmbInvH = 64.0;
 constexpr int kEmbN = 4096;  // rho in [0, 64)
 constexpr int kBlock = 256;
@@ -147,21 +151,60 @@ constexpr float kSqrt3 = 1.7320508075688772f;
   const float bi = 2.0f * (Dc) * ui, bj = 2.0f * (Dc) * uj; \
   const float s2[4] = {Ai + bi, Ai - bi, Aj - bj, Aj + bj};
 
+
+// Walks neighbor entries begin, begin+step, ... < end with the loads of the
+// next neighbor (its entry one step further ahead) issued before the current
+// one is computed: the entry -> state -> arithmetic chain is otherwise a
+// dependent global-load latency per neighbor (the dominant stall).
+template <bool OCC, bool FP, class Body>
+__device__ __forceinline__ void walk_neighbors(const MixArgs &a, int64_t begin, int64_t end, int step, Body body) {
+  int64_t t = begin;
+  if (t >= end) return;
+  int64_t j0 = __ldg(&a.nbr[t]) & kIdMask;
+  int4 p0 = __ldg(&a.P[j0]);
+  float x0 = OCC ? __ldg(&a.occ[j0]) : 1.0f;
+  float f0 = FP ? __ldg(&a.FF[j0].x) : 0.0f;
+  int64_t t1 = t + step;
+  uint32_t e1 = (t1 < end) ? __ldg(&a.nbr[t1]) : 0u;
+  for (; t < end; t += step) {
+    const int64_t t2 = t1 + step;
+    int4 p1 = p0;
+    float x1 = x0, f1 = f0;
+    uint32_t e2 = 0u;
+    if (t1 < end) {
+      const int64_t j1 = e1 & kIdMask;
+      p1 = __ldg(&a.P[j1]);
+      if (OCC) x1 = __ldg(&a.occ[j1]);
+      if (FP) f1 = __ldg(&a.FF[j1].x);
+    }
+    if (t2 < end) e2 = __ldg(&a.nbr[t2]);
+    body(p0, x0, f0);
+    p0 = p1;
+    x0 = x1;
+    f0 = f1;
+    e1 = e2;
+    t1 = t2;
+  }
+}
+
 // ---------------------------------------------------------------- pass 1
 template <int TPS>
 __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t s = g / TPS;
-  const int lane = (int)(g % TPS);
+  __shared__ float4 sF[kTabN];
+  for (int i = threadIdx.x; i < kTabN; i += blockDim.x) sF[i] = __ldg(&a.tabPair[i]);
+  __syncthreads();
+  constexpr int kSitesPerBlock = kBlock / TPS;
+  for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < a.N;
+       base += (int64_t)gridDim.x * kSitesPerBlock) {
+  const int64_t s = base + threadIdx.x / TPS;
+  const int lane = (int)(threadIdx.x % TPS);
   const bool live = s < a.N;
   float acc = 0.0f, cmp = 0.0f;
   if (live) {
     const int4 pi = a.P[s];
     const float ui = kSqrt6 * __int_as_float(pi.w), ui2 = ui * ui;
     const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
-    for (int64_t t = b + lane; t < m; t += TPS) {  // Pd neighbors: f_Pd
-      const int64_t j = a.nbr[t] & kIdMask;
-      const int4 pj = a.P[j];
+    walk_neighbors<false, false>(a, b + lane, m, TPS, [&](int4 pj, float, float) {  // Pd neighbors: f_Pd
       const float3 D = pair_vec(a, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
@@ -176,14 +219,12 @@ __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
           const float r = s2[q] * rsq(s2[q]);
           float tt;
           const int i = tab_index(r, tt);
-          part += hv(__ldg(&a.tabPair[2 * i]), tt);
+          part += hv(sF[i], tt);
         }
       }
       kahan(acc, cmp, part);
-    }
-    for (int64_t t = m + lane; t < e; t += TPS) {  // H neighbors: x_j f_H
-      const int64_t j = a.nbr[t] & kIdMask;
-      const int4 pj = a.P[j];
+    });
+    walk_neighbors<true, false>(a, m + lane, e, TPS, [&](int4 pj, float xj, float) {  // H neighbors: x_j f_H
       const float3 D = pair_vec(a, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
@@ -196,8 +237,8 @@ __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) part += fH(s2[q] * rsq(s2[q]));
       }
-      kahan(acc, cmp, part * a.occ[j]);
-    }
+      kahan(acc, cmp, part * xj);
+    });
   }
   float tot = acc;
 #pragma unroll
@@ -210,6 +251,7 @@ __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
     const float tt = x - (float)i;
     const float4 c = __ldg(&a.tabEmb[(iPd ? 0 : kEmbN) + i]);
     a.FF[s] = make_float2(hd(c, tt) * (float)kEmbInvH, hv(c, tt));
+  }
   }
 }
 
@@ -224,8 +266,8 @@ struct PairAcc {
 };
 
 template <int TYPE>  // 0 Pd-Pd, 1 Pd i / H j, 2 H i / Pd j, 3 H-H
-__device__ __forceinline__ void pair_terms(const MixArgs &a, float Fa, float Fb, float3 D, float ui, float uj,
-                                           PairAcc &p) {
+__device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, float Fa, float Fb, float3 D, float ui,
+                                           float uj, PairAcc &p) {
   const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
   const float Ai = fmaf(ui, ui, D2), Aj = fmaf(uj, uj, D2);
   const float Dv[3] = {D.x, D.y, D.z};
@@ -244,7 +286,7 @@ __device__ __forceinline__ void pair_terms(const MixArgs &a, float Fa, float Fb,
       if (TYPE == 0) {
         float tt;
         const int i = tab_index(r, tt);
-        const float4 cf = __ldg(&a.tabPair[2 * i]), cp = __ldg(&a.tabPair[2 * i + 1]);
+        const float4 cf = sF[i], cp = sP[i];
         g = fmaf(Fa + Fb, hd(cf, tt), hd(cp, tt)) * (float)kTabInvH;
         phi = hv(cp, tt);
       } else if (TYPE == 3) {
@@ -255,7 +297,7 @@ __device__ __forceinline__ void pair_terms(const MixArgs &a, float Fa, float Fb,
       } else {
         float tt;
         const int i = tab_index(r, tt);
-        const float fpd = hd(__ldg(&a.tabPair[2 * i]), tt) * (float)kTabInvH;
+        const float fpd = hd(sF[i], tt) * (float)kTabInvH;
         const float fhd = fH(r) * kFH_D;
         float dphi;
         morse(kPdH, r, phi, dphi);
@@ -285,9 +327,17 @@ __device__ __forceinline__ void add_pair(SiteAcc &A, const PairAcc &p, float3 D,
 
 template <int TPS>
 __global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t s = g / TPS;
-  const int lane = (int)(g % TPS);
+  __shared__ float4 sF[kTabN], sP[kTabN];
+  for (int i = threadIdx.x; i < kTabN; i += blockDim.x) {
+    sF[i] = __ldg(&a.tabPair[i]);
+    sP[i] = __ldg(&a.tabPair[kTabN + i]);
+  }
+  __syncthreads();
+  constexpr int kSitesPerBlock = kBlock / TPS;
+  for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < a.N;
+       base += (int64_t)gridDim.x * kSitesPerBlock) {
+  const int64_t s = base + threadIdx.x / TPS;
+  const int lane = (int)(threadIdx.x % TPS);
   const bool live = s < a.N;
   SiteAcc A;
 #pragma unroll
@@ -303,29 +353,22 @@ __global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
     const bool iPd = s < a.nPd;
     const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
     const float hw = 0.5f * a.W * xi;
-    for (int64_t t = b + lane; t < m; t += TPS) {  // Pd neighbors
-      const int64_t j = a.nbr[t] & kIdMask;
-      const int4 pj = a.P[j];
+    walk_neighbors<false, true>(a, b + lane, m, TPS, [&](int4 pj, float, float Fb) {  // Pd neighbors
       const float3 D = pair_vec(a, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
-      const float Fb = a.FF[j].x;
       PairAcc p;
-      if (iPd) pair_terms<0>(a, ffi.x, Fb, D, ui, uj, p);
-      else pair_terms<2>(a, ffi.x, Fb, D, ui, uj, p);
+      if (iPd) pair_terms<0>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+      else pair_terms<2>(sF, sP, ffi.x, Fb, D, ui, uj, p);
       add_pair(A, p, D, a.W, hw);
-    }
-    for (int64_t t = m + lane; t < e; t += TPS) {  // H neighbors
-      const int64_t j = a.nbr[t] & kIdMask;
-      const int4 pj = a.P[j];
+    });
+    walk_neighbors<true, true>(a, m + lane, e, TPS, [&](int4 pj, float xj, float Fb) {  // H neighbors
       const float3 D = pair_vec(a, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
-      const float Fb = a.FF[j].x;
-      const float xj = a.occ[j];
       PairAcc p;
-      if (iPd) pair_terms<1>(a, ffi.x, Fb, D, ui, uj, p);
-      else pair_terms<3>(a, ffi.x, Fb, D, ui, uj, p);
+      if (iPd) pair_terms<1>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+      else pair_terms<3>(sF, sP, ffi.x, Fb, D, ui, uj, p);
       add_pair(A, p, D, a.W * xj, hw * xj);
-    }
+    });
   }
   double tot[5];
 #pragma unroll
@@ -344,6 +387,7 @@ __global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
     a.Vs[s] = x * (double)ffi.y + tot[4];
     a.Ss[s] = (double)logf(sigi) * x;
   }
+  }
 }
 
 __global__ void k_prep(const double *X, const double *occ, int64_t N, double k0, double k1, double k2, int4 *P,
@@ -357,13 +401,24 @@ __global__ void k_prep(const double *X, const double *occ, int64_t N, double k0,
   occf[s] = (float)occ[s];
 }
 
+// Persistent grids: as many blocks as fit on the device at once (occupancy
+// query, cached per kernel), capped by the work.
 template <int TPS>
 void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev) {
-  const int64_t threads = a.N * TPS;
-  const unsigned grid = (unsigned)((threads + kBlock - 1) / kBlock);
-  k_rho_mixed<TPS><<<grid, kBlock, 0, st>>>(a);
+  static int cap[2] = {0, 0};
+  if (!cap[0]) {
+    int dev = 0, sms = 0, b0 = 0, b1 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_rho_mixed<TPS>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_grad_mixed<TPS>, kBlock, 0);
+    cap[0] = std::max(1, sms * b0);
+    cap[1] = std::max(1, sms * b1);
+  }
+  const int64_t need = (a.N * TPS + kBlock - 1) / kBlock;
+  k_rho_mixed<TPS><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[0])), kBlock, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
-  k_grad_mixed<TPS><<<grid, kBlock, 0, st>>>(a);
+  k_grad_mixed<TPS><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[1])), kBlock, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[3], st);
 }
 
@@ -379,8 +434,13 @@ a2c_status ensure_mixed(a2c_gpp_ctx *c) {
       cudaMalloc(&M->tabPair, sizeof(float4) * 2 * kTabN) != cudaSuccess ||
       cudaMalloc(&M->tabEmb, sizeof(float4) * 2 * kEmbN) != cudaSuccess)
     return A2C_ERR_NOMEM;
-  std::vector<float> pair, embPd, embH;
-  build_pair_table(kTabR0, 1.0 / kTabInvH, kTabN, pair);
+  std::vector<float> inter, pair((size_t)8 * kTabN), embPd, embH;
+  build_pair_table(kTabR0, 1.0 / kTabInvH, kTabN, inter);
+  for (int i = 0; i < kTabN; ++i)  // interleaved (f, phi) per interval -> all f cubics, then all phi cubics
+    for (int k = 0; k < 4; ++k) {
+      pair[(size_t)4 * i + k] = inter[(size_t)8 * i + k];
+      pair[(size_t)4 * (kTabN + i) + k] = inter[(size_t)8 * i + 4 + k];
+    }
   build_embed_table(0, 1.0 / kEmbInvH, kEmbN, embPd);
   build_embed_table(1, 1.0 / kEmbInvH, kEmbN, embH);
   A2C_CUDA(cudaMemcpyAsync(M->tabPair, pair.data(), sizeof(float) * pair.size(), cudaMemcpyHostToDevice, c->stream));
@@ -515,7 +575,13 @@ a2c_status na_setup(int dev, unsigned char **base) {
   cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
   if (e != cudaSuccess) return cuda_status(e);
   if (!g_na_host_ready) {
-    build_pair_table_raw(kTabR0, 1.0 / kTabInvH, kTabN, g_na_pair_host);
+    static float inter[8 * kTabN];
+    build_pair_table_raw(kTabR0, 1.0 / kTabInvH, kTabN, inter);
+    for (int i = 0; i < kTabN; ++i)  // all f cubics, then all phi cubics
+      for (int k = 0; k < 4; ++k) {
+        g_na_pair_host[4 * i + k] = inter[8 * i + k];
+        g_na_pair_host[4 * (kTabN + i) + k] = inter[8 * i + 4 + k];
+      }
     build_embed_table_raw(0, 1.0 / kEmbInvH, kEmbN, g_na_emb_host);
     build_embed_table_raw(1, 1.0 / kEmbInvH, kEmbN, g_na_emb_host + 4 * kEmbN);
     g_na_host_ready = true;

@@ -459,6 +459,8 @@ def run_profile_case(args):
     with A.Gpp(nPd, nH, box=box, periodic=w["periodic"], precision="mixed") as g:
         g.set_occupancy(xH)
         g.build_neighbors(X)
+        if args.case_tps:
+            g.set_threads_per_site(args.case_tps)
         dX = torch.tensor(X, device="cuda")
         dG = torch.empty_like(dX)
         df = torch.empty(1, dtype=torch.float64, device="cuda")
@@ -487,6 +489,7 @@ def main():
     ap.add_argument("--case", choices=["bench", "profile", "ttm"], default="bench",
                     help="profile: the small untimed case used for ncu captures")
     ap.add_argument("--case-cells", type=int, default=40)
+    ap.add_argument("--case-tps", type=int, default=0, help="threads per site in the profile case (0 = library)")
     args = ap.parse_args()
     if args.case == "profile":
         return run_profile_case(args)
