@@ -15,7 +15,7 @@ import numpy as np
 from . import _native as N
 from ._native import A2CError, A2C_FP64, A2C_MIXED  # noqa: F401
 
-__all__ = ["Gpp", "lattice_fcc", "peak_flops", "A2CError", "A2C_FP64", "A2C_MIXED", "LbfgsResult"]
+__all__ = ["Gpp", "lattice_fcc", "peak_flops", "restart_write", "restart_read", "A2CError", "A2C_FP64", "A2C_MIXED", "LbfgsResult"]
 
 
 @dataclass
@@ -226,6 +226,31 @@ class Gpp:
                 "a2c_gpp_diffuse")
         return xo
 
+    def dmd_run(self, X, xH, gamma, full_H, bd_sites, surf_sites, nsteps: int, *, dt: float, nu: float, Qm: float,
+                x_bd: float, gamma_bd: float, xLb: float = 1e-3, xUb: float = 1.0 - 1e-16, **lbfgs) -> dict:
+        """nsteps DMD outer steps on the device (a2c_gpp_dmd_run)."""
+        dp = N.DmdParams()
+        self._L.a2c_lbfgs_default_params(C.byref(dp.lbfgs))
+        for k, v in lbfgs.items():
+            setattr(dp.lbfgs, k, v)
+        dp.dt, dp.nu, dp.Qm, dp.xLb, dp.xUb, dp.x_bd, dp.gamma_bd = dt, nu, Qm, xLb, xUb, x_bd, gamma_bd
+        X = _f64(X, 4 * self.N).copy()
+        xH = _f64(xH, self.nH).copy()
+        g = _f64(gamma, self.nH).copy()
+        fh = _i32(full_H, self.nH).copy()
+        bd = _i32(bd_sites)
+        sf = _i32(surf_sites)
+        out = {k: np.zeros(max(nsteps, 1)) for k in ("xH_mean", "xH_interior", "fmin")}
+        its = np.zeros(max(nsteps, 1), dtype=np.int32)
+        N.check(self._L.a2c_gpp_dmd_run(self._h, N.ptr(X), N.ptr(xH), N.ptr(g), N.ptr(fh),
+                                        N.ptr(bd) if bd.size else None, int(bd.size),
+                                        N.ptr(sf) if sf.size else None, int(sf.size), C.byref(dp), int(nsteps),
+                                        N.ptr(out["xH_mean"]), N.ptr(out["xH_interior"]), N.ptr(out["fmin"]),
+                                        N.ptr(its)), "a2c_gpp_dmd_run")
+        res = {k: v[:nsteps] for k, v in out.items()}
+        res.update(X=X, xH=xH, gamma=g, full_H=fh, iters=its[:nsteps])
+        return res
+
     def macro_results(self, x, HSurf) -> tuple[float, float]:
         x = _f64(x, self.nH)
         hs = _i32(HSurf)
@@ -233,6 +258,22 @@ class Gpp:
         N.check(self._L.a2c_gpp_macro_results(self._h, N.ptr(x), N.ptr(hs) if hs.size else None, int(hs.size),
                                               C.byref(a), C.byref(b)), "a2c_gpp_macro_results")
         return a.value, b.value
+
+
+def restart_write(path: str, nPd: int, nH: int, X, xH, gamma, full_H, step: int = 0, time: float = 0.0) -> None:
+    """Restart file in the format the reference's readResults reads."""
+    N.check(N.lib().a2c_restart_write(str(path).encode(), nPd, nH, N.ptr(_f64(X, 4 * (nPd + nH))),
+                                      N.ptr(_f64(xH, nH)), N.ptr(_f64(gamma, nH)), N.ptr(_i32(full_H, nH)),
+                                      int(step), float(time)), "a2c_restart_write")
+
+
+def restart_read(path: str, nPd: int, nH: int, xLb: float = 1e-3, xUb: float = 1.0 - 1e-16):
+    """(X, xH, gamma, full_H) from a restart file (x clamped to [xLb, xUb])."""
+    X, xH, g = np.empty(4 * (nPd + nH)), np.empty(nH), np.empty(nH)
+    fh = np.empty(nH, dtype=np.int32)
+    N.check(N.lib().a2c_restart_read(str(path).encode(), nPd, nH, xLb, xUb, N.ptr(X), N.ptr(xH), N.ptr(g), N.ptr(fh)),
+            "a2c_restart_read")
+    return X, xH, g, fh
 
 
 def peak_flops(precision: int | str = A2C_MIXED, device: int = 0) -> float:

@@ -64,6 +64,11 @@ class LatticeSpec(C.Structure):
     ]
 
 
+class DmdParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("nu", C.c_double), ("Qm", C.c_double), ("xLb", C.c_double),
+                ("xUb", C.c_double), ("x_bd", C.c_double), ("gamma_bd", C.c_double), ("lbfgs", LbfgsParams)]
+
+
 _lib = None
 
 P = C.c_void_p
@@ -113,6 +118,9 @@ def lib() -> C.CDLL:
         "a2c_gpp_macro_results": (I, [P, P, P, I, C.POINTER(D), C.POINTER(D)]),
         "a2c_lattice_fcc": (I, [C.POINTER(LatticeSpec), P, P, P]),
         "a2c_gpp_peak_flops": (I, [I, I, C.POINTER(D)]),
+        "a2c_gpp_dmd_run": (I, [P, P, P, P, P, P, I, P, I, C.POINTER(DmdParams), I, P, P, P, P]),
+        "a2c_restart_write": (I, [C.c_char_p, I, I, P, P, P, P, I, D]),
+        "a2c_restart_read": (I, [C.c_char_p, I, I, D, D, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -131,7 +139,7 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_neighbor_total", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
             "a2c_gpp_eval_device", "a2c_gpp_profile_eval", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
             "a2c_gpp_chem_potential", "a2c_gpp_minimize_stats", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",
-            "a2c_lattice_fcc", "a2c_gpp_peak_flops"]
+            "a2c_lattice_fcc", "a2c_gpp_peak_flops", "a2c_gpp_dmd_run", "a2c_restart_write", "a2c_restart_read"]
 
 
 class A2CError(RuntimeError):

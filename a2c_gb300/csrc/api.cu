@@ -562,4 +562,69 @@ a2c_status a2c_gpp_macro_results(a2c_gpp_ctx *c, const double *x, const int *HSu
   return finish(c);
 }
 
+a2c_status a2c_gpp_dmd_run(a2c_gpp_ctx *c, double *X, double *xH, double *gamma, int *full_H, const int *bd_sites,
+                           int n_bd, const int *surf_sites, int n_surf, const a2c_dmd_params *dp, int nsteps,
+                           double *xH_mean, double *xH_interior, double *fmin, int *iters) {
+  if (!c || !dp || nsteps < 0 || n_bd < 0 || n_surf < 0 || (c->N > 0 && !X) ||
+      (c->p.nH > 0 && (!xH || !gamma || !full_H)) || (n_bd > 0 && !bd_sites) || (n_surf > 0 && !surf_sites))
+    return A2C_ERR_INVALID;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  const int nH = c->p.nH;
+  for (int t = 0; t < n_bd; ++t)
+    if (bd_sites[t] < 0 || bd_sites[t] >= nH) return A2C_ERR_INVALID;
+  if (nH == 0) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  cudaStream_t st = c->stream;
+  std::vector<int> flags((size_t)nH, 0);
+  for (int t = 0; t < n_surf; ++t)
+    if (surf_sites[t] >= 0 && surf_sites[t] < nH) flags[(size_t)surf_sites[t]] = 1;
+  double *dg = nullptr, *dsend = nullptr, *dx = nullptr;
+  int *dfull = nullptr, *dbd = nullptr, *dsurf = nullptr;
+  A2C_TRY(ensure_hscratch(c, &dg, &dsend, &dx, &dfull));
+  a2c_status s = A2C_OK;
+  if (cudaMallocAsync((void **)&dbd, sizeof(int) * std::max(n_bd, 1), st) ||
+      cudaMallocAsync((void **)&dsurf, sizeof(int) * nH, st))
+    s = A2C_ERR_NOMEM;
+  if (!s && (cudaMemcpyAsync(c->d_X, X, sizeof(double) * 4 * c->N, cudaMemcpyHostToDevice, st) ||
+             cudaMemcpyAsync(c->d_occ + c->p.nPd, xH, sizeof(double) * nH, cudaMemcpyHostToDevice, st) ||
+             cudaMemcpyAsync(dg, gamma, sizeof(double) * nH, cudaMemcpyHostToDevice, st) ||
+             cudaMemcpyAsync(dfull, full_H, sizeof(int) * nH, cudaMemcpyHostToDevice, st) ||
+             (n_bd > 0 && cudaMemcpyAsync(dbd, bd_sites, sizeof(int) * n_bd, cudaMemcpyHostToDevice, st)) ||
+             cudaMemcpyAsync(dsurf, flags.data(), sizeof(int) * nH, cudaMemcpyHostToDevice, st)))
+    s = A2C_ERR_CUDA;
+  c->has_state = true;
+  for (int k = 0; k < nsteps && !s; ++k) {
+    double f = 0.0, gn = 0.0;
+    int it = 0, fev = 0, why = 0;
+    s = lbfgs_minimize(c, c->d_X, &dp->lbfgs, &f, &it, &fev, &gn, &why);  // minimizer.cpp:548
+    if (!s) s = launch_density64(c, c->d_X);                              // minimizer.cpp:607-633
+    if (!s) s = launch_chem64(c, c->d_X, dp->gamma_bd, dsend, dfull);     // minimizer.cpp:658-789
+    if (!s) s = launch_gamma_update(c, dsend, dp->gamma_bd, dg, dfull);   // minimizer.cpp:793-800
+    if (!s) s = launch_dirichlet(c, dbd, n_bd, dp->gamma_bd, dp->x_bd, dg, dfull);  // boundaryconditions.cpp:47-51
+    if (!s && cudaMemcpyAsync(dx, c->d_occ + c->p.nPd, sizeof(double) * nH, cudaMemcpyDeviceToDevice, st))
+      s = A2C_ERR_CUDA;
+    if (!s) s = launch_diffuse(c, dg, dfull, dp->dt, dp->nu, dp->Qm, dp->xLb, dp->xUb, dx);  // integrate.cpp:26-81
+    if (!s && cudaMemcpyAsync(c->d_occ + c->p.nPd, dx, sizeof(double) * nH, cudaMemcpyDeviceToDevice, st))
+      s = A2C_ERR_CUDA;
+    double a = 0.0, b = 0.0;
+    if (!s) s = launch_macro(c, dx, dsurf, n_surf, &a, &b);  // calculateresults.cpp:8-78
+    if (!s) s = check_status_word(c);
+    if (xH_mean) xH_mean[k] = a;
+    if (xH_interior) xH_interior[k] = b;
+    if (fmin) fmin[k] = f;
+    if (iters) iters[k] = it;
+  }
+  if (!s && (cudaMemcpyAsync(X, c->d_X, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToHost, st) ||
+             cudaMemcpyAsync(xH, c->d_occ + c->p.nPd, sizeof(double) * nH, cudaMemcpyDeviceToHost, st) ||
+             cudaMemcpyAsync(gamma, dg, sizeof(double) * nH, cudaMemcpyDeviceToHost, st) ||
+             cudaMemcpyAsync(full_H, dfull, sizeof(int) * nH, cudaMemcpyDeviceToHost, st)))
+    s = A2C_ERR_CUDA;
+  free_hscratch(c, dg, dsend, dx, dfull);
+  if (dbd) cudaFreeAsync(dbd, st);
+  if (dsurf) cudaFreeAsync(dsurf, st);
+  c->has_density = false;
+  if (s) return s;
+  return finish(c);
+}
+
 }  // extern "C"

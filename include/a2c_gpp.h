@@ -221,6 +221,40 @@ a2c_status a2c_gpp_macro_results(a2c_gpp_ctx *ctx, const double *x, const int *H
  * compute-bound kernels (no reference counterpart; a measurement aid). */
 a2c_status a2c_gpp_peak_flops(int device, int precision, double *flops_per_s);
 
+/* One DMD outer step, as the reference's (missing) driver sequences it
+ * (minimizer.cpp:548, 588; boundaryconditions.cpp:30; integrate.cpp:9;
+ * calculateresults.cpp:8): minimize the free entropy at fixed occupancy,
+ * chemical potential at the minimum, Dirichlet condition on the boundary
+ * sites, one explicit diffusion step, occupancy <- diffused occupancy, macro
+ * results. */
+typedef struct a2c_dmd_params {
+  double dt, nu, Qm;       /* time step [s], attempt frequency [1/s], activation energy [eV] */
+  double xLb, xUb;         /* clamp of the diffusion step */
+  double x_bd, gamma_bd;   /* occupancy and chemical potential held on the boundary sites */
+  a2c_lbfgs_params lbfgs;  /* the minimization of every step */
+} a2c_dmd_params;
+
+/* Runs nsteps outer steps with all state on the device; X (4N), xH, gamma,
+ * full_H (nH) are read at the start and written back at the end.
+ * Per step k: xH_mean[k], xH_interior[k] (macro results over all H sites /
+ * those not in surf_sites), fmin[k] and iters[k] of the minimization (any of
+ * the four output arrays may be NULL).  Neighbor lists are held fixed, as
+ * the reference holds them through a solve; build them before the call. */
+a2c_status a2c_gpp_dmd_run(a2c_gpp_ctx *ctx, double *X, double *xH, double *gamma, int *full_H, const int *bd_sites,
+                           int n_bd, const int *surf_sites, int n_surf, const a2c_dmd_params *dp, int nsteps,
+                           double *xH_mean, double *xH_interior, double *fmin, int *iters);
+
+/* Restart file in the format readResults reads (readresults.cpp:10-55):
+ * 9 header lines, then one row of 9 columns per site, Pd rows first:
+ *   id species qx qy qz sigma x gamma full_H
+ * (the reader ignores the first two columns and, for Pd rows, the last
+ * three).  The writer has no counterpart in the reference tree.  The reader
+ * clamps x to [xLb, xUb] as readresults.cpp:48-51 does. */
+a2c_status a2c_restart_write(const char *path, int nPd, int nH, const double *X, const double *xH,
+                             const double *gamma, const int *full_H, int step, double time);
+a2c_status a2c_restart_read(const char *path, int nPd, int nH, double xLb, double xUb, double *X, double *xH,
+                            double *gamma, int *full_H);
+
 /* Seeded synthetic fcc Pd lattice with octahedral H sites (stand-in for the
  * reference's SpaceInitializer lattice setup).  Site order: cells z, y, x,
  * then basis; all Pd then all H.  Writes X (4N), xH (nH) and surface flags

@@ -22,9 +22,10 @@
  *   calculateresults.cpp:8-78   macro results (H fraction)
  *   Vector3D.h:83,281-316       Vec3D norm / dot / scalar product order
  *
- * Parity pin: oracle/ref_build.sh compiles the reference's own hot-path
- * sources against single-rank shims (oracle/ref_shim) into oracle/_ref, and
- * tests/test_oracle_pin.py checks this restatement against it bit for bit.
+ * Parity pin: oracle/Makefile (target `ref`) compiles the reference's own
+ * hot-path sources against single-rank shims (oracle/ref_shim) into
+ * oracle/_ref, and tests/test_oracle_pin.py checks this restatement against
+ * it bit for bit.
  */
 #ifndef A2C_GPP_ORACLE_H
 #define A2C_GPP_ORACLE_H

@@ -119,6 +119,7 @@ def rlib() -> C.CDLL:
         L.ref_diffuse.argtypes = [I, P, P, P, P, P, D, D, D, D, D, D, P]
         L.ref_dirichlet.argtypes = [I, P, I, D, D, P, P, P]
         L.ref_macro_results.argtypes = [I, P, P, I, C.POINTER(D), C.POINTER(D)]
+        L.ref_read_results.argtypes = [C.c_char_p, C.c_char_p, I, I, I, D, D, P, P, P, P]
         _rlib = L
     return _rlib
 
@@ -339,6 +340,15 @@ def ref_dirichlet(nH, sites, gamma_bd, xUb, x0, gamma, full_H):
     return x0, g, fh
 
 
+def ref_read_results(folder, base, num, nPd, nH, xLb=1e-3, xUb=1.0 - 1e-16):
+    """The reference's readResults on <folder>/<base>.<num>.dat."""
+    X, xH, g = np.empty(4 * (nPd + nH)), np.empty(nH), np.empty(nH)
+    fh = np.empty(nH, dtype=np.int32)
+    assert rlib().ref_read_results(str(folder).encode(), str(base).encode(), num, nPd, nH, xLb, xUb, _p(X), _p(xH),
+                                   _p(g), _p(fh)) == 0
+    return X, xH, g, fh
+
+
 def ref_macro_results(x, HSurf):
     x = np.ascontiguousarray(x, dtype=np.float64)
     hs = np.ascontiguousarray(HSurf, dtype=np.int32)
@@ -346,3 +356,29 @@ def ref_macro_results(x, HSurf):
     assert rlib().ref_macro_results(x.size, _p(x), _p(hs) if hs.size else None, hs.size, C.byref(a),
                                     C.byref(b)) == 0
     return a.value, b.value
+
+
+def dmd_run(pb: Problem, X, xH, gamma, full_H, off, nbr, hh1_off, hh1, bd_sites, surf_sites, nsteps, *, dt, nu, Qm,
+            x_bd, gamma_bd, xLb=1e-3, xUb=1.0 - 1e-16, **lbfgs):
+    """The DMD outer loop in the order the device runs it: minimize ->
+    chemical potential -> Dirichlet -> diffuse -> occupancy update -> macro
+    results.  Returns the same fields as a2c_gb300.Gpp.dmd_run."""
+    X = np.array(X, dtype=np.float64)
+    x0 = np.array(xH, dtype=np.float64)
+    g = np.array(gamma, dtype=np.float64)
+    fh = np.array(full_H, dtype=np.int32)
+    out = {"xH_mean": [], "xH_interior": [], "fmin": [], "iters": []}
+    for _ in range(nsteps):
+        r = minimize(pb, X, x0, off, nbr, **lbfgs)
+        X = r["X"]
+        g, fh = chem_potential(pb, X, x0, off, nbr, gamma_bd, g, fh)
+        x0, g, fh = dirichlet(bd_sites, gamma_bd, x_bd, x0, g, fh)
+        x0 = diffuse(pb.nH, x0, hh1_off, hh1, g, fh, pb.p.T, dt, nu, Qm, xLb, xUb, x0.copy())
+        a, b = macro_results(x0, surf_sites)
+        out["xH_mean"].append(a)
+        out["xH_interior"].append(b)
+        out["fmin"].append(r["fmin"])
+        out["iters"].append(r["iters"])
+    res = {k: np.array(v) for k, v in out.items()}
+    res.update(X=X, xH=x0, gamma=g, full_H=fh)
+    return res

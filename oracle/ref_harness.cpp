@@ -1,13 +1,15 @@
 // Harness around the reference's own hot-path sources -- TEST INFRASTRUCTURE.
 //
-// oracle/ref_build.sh compiles this file together with the reference's
-// potential.cpp, electrondensity.cpp, quadrature.cpp, neighbors.cpp,
-// minimizer.cpp, integrate.cpp, boundaryconditions.cpp and
-// calculateresults.cpp (unmodified, read where they lie) against the
+// oracle/Makefile (target `ref`) compiles this file together with the
+// reference's potential.cpp, electrondensity.cpp, quadrature.cpp,
+// neighbors.cpp, minimizer.cpp, integrate.cpp, boundaryconditions.cpp,
+// calculateresults.cpp and readresults.cpp (unmodified, read where they lie)
+// against the
 // single-rank shims in oracle/ref_shim, producing oracle/_ref/liba2c_ref.so.
 // The tests use it to pin the oracle restatement bit for bit.  It is built
 // only where the reference tree is present and is never shipped.
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -36,6 +38,8 @@ int enforceBoundaryConditions(Input &input, double dt, vector<Vec3D> &q_Pd0, vec
 int calculateMacroResults(vector<vector<int> > &PdPd, vector<vector<int> > &PdPdnum, vector<Vec3D> &q_Pd,
                           vector<double> &x, vector<int> &PdSurf, vector<int> &HSurf, double &xH,
                           double &xHinterior);
+void readResults(Input &input, vector<Vec3D> &q_Pd0, vector<Vec3D> &q_H0, vector<double> &sigma_Pd0,
+                 vector<double> &sigma_H0, vector<double> &x0, vector<double> &gamma, vector<int> &full_H);
 
 namespace {
 
@@ -284,6 +288,33 @@ int ref_macro_results(int nH, const double *x, const int *HSurf, int nSurf, doub
   vector<double> xx(x, x + nH);
   vector<int> ps, hs(HSurf, HSurf + nSurf);
   return calculateMacroResults(a, b, q, xx, ps, hs, *xH, *xHinterior);
+}
+
+// Reference restart reader: readResults (reads <folder>/<base>.<num>.dat).
+int ref_read_results(const char *folder, const char *base, int num, int nPd, int nH, double xLb, double xUb,
+                     double *X, double *xH, double *gamma, int *full_H) {
+  Input in;
+  std::snprintf(in.file.foldername, sizeof(in.file.foldername), "%s", folder);
+  std::snprintf(in.file.filename_base, sizeof(in.file.filename_base), "%s", base);
+  in.file.restart_file_num = num;
+  in.file.xLb = xLb;
+  in.file.xUb = xUb;
+  vector<Vec3D> qPd(nPd), qH(nH);
+  vector<double> sPd(nPd), sH(nH), x0(nH), g(nH);
+  vector<int> fh(nH);
+  readResults(in, qPd, qH, sPd, sH, x0, g, fh);
+  for (int i = 0; i < nPd; ++i) {
+    for (int d = 0; d < 3; ++d) X[4 * i + d] = qPd[i][d];
+    X[4 * i + 3] = sPd[i];
+  }
+  for (int h = 0; h < nH; ++h) {
+    for (int d = 0; d < 3; ++d) X[4 * (nPd + h) + d] = qH[h][d];
+    X[4 * (nPd + h) + 3] = sH[h];
+    xH[h] = x0[h];
+    gamma[h] = g[h];
+    full_H[h] = fh[h];
+  }
+  return 0;
 }
 
 }  // extern "C"
