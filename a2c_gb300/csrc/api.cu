@@ -298,6 +298,92 @@ a2c_status host_lists(a2c_gpp_ctx *c, std::vector<int64_t> &off, std::vector<int
 }
 }  // namespace
 
+a2c_status a2c_gpp_set_neighbor_lists(a2c_gpp_ctx *c, const double *X, const int64_t *pdpd_off,
+                                      const int *pdpd_idx, const int64_t *pdh_off, const int *pdh_idx,
+                                      const int64_t *hpd_off, const int *hpd_idx, const int64_t *hh_off,
+                                      const int *hh_idx, const int64_t *hh1_off, const int *hh1_idx,
+                                      const int *PdPdnum) {
+  if (!c) return A2C_ERR_INVALID;
+  const int nPd = c->p.nPd, nH = c->p.nH;
+  const int64_t N = c->N;
+  const bool per = c->p.periodic[0] || c->p.periodic[1] || c->p.periodic[2];
+  if ((per && N > 0 && !X) || (nPd > 0 && (!pdpd_off || !pdh_off)) || (nH > 0 && (!hpd_off || !hh_off || !hh1_off)))
+    return A2C_ERR_INVALID;
+  std::vector<int64_t> off((size_t)N + 1, 0);
+  std::vector<uint32_t> nbr;
+  std::vector<int> npd((size_t)std::max<int64_t>(N, 1), 0);
+  auto code = [&](int64_t i, int64_t j) -> uint32_t {
+    if (!per) return kNoShift;
+    int m[3] = {0, 0, 0};
+    for (int d = 0; d < 3; ++d)
+      if (c->p.periodic[d]) m[d] = -(int)std::nearbyint((X[4 * j + d] - X[4 * i + d]) / c->p.box[d]);
+    for (int d = 0; d < 3; ++d)
+      if (m[d] < -1 || m[d] > 1) return 0xffffffffu;
+    return (uint32_t)((m[0] + 1) + 3 * (m[1] + 1) + 9 * (m[2] + 1));
+  };
+  auto append = [&](int64_t s, const int64_t *o, const int *idx, int64_t row, int64_t base, int64_t lim) -> bool {
+    for (int64_t t = o[row]; t < o[row + 1]; ++t) {
+      const int64_t j = idx[t];
+      if (j < 0 || j >= lim) return false;
+      const uint32_t cd = code(s, base + j);
+      if (cd == 0xffffffffu) return false;
+      nbr.push_back((uint32_t)(base + j) | (cd << kIdBits));
+    }
+    return true;
+  };
+  int maxn = 0;
+  for (int64_t s = 0; s < N; ++s) {
+    const bool iPd = s < nPd;
+    const int64_t row = iPd ? s : s - nPd;
+    if (!append(s, iPd ? pdpd_off : hpd_off, iPd ? pdpd_idx : hpd_idx, row, 0, nPd)) return A2C_ERR_INVALID;
+    npd[(size_t)s] = (int)(nbr.size() - (size_t)off[(size_t)s]);
+    if (!append(s, iPd ? pdh_off : hh_off, iPd ? pdh_idx : hh_idx, row, nPd, nH)) return A2C_ERR_INVALID;
+    off[(size_t)s + 1] = (int64_t)nbr.size();
+    const int cnt = (int)(off[(size_t)s + 1] - off[(size_t)s]);
+    if (cnt > 1000) return A2C_ERR_NEIGHBOR_OVERFLOW;
+    maxn = std::max(maxn, cnt);
+  }
+  const int64_t total = (int64_t)nbr.size(), total1 = nH > 0 ? hh1_off[nH] : 0;
+  for (int64_t t = 0; t < total1; ++t)
+    if (hh1_idx[t] < 0 || hh1_idx[t] >= nH) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  if (total > c->nbr_cap) {
+    if (c->d_nbr) cudaFree(c->d_nbr);
+    c->d_nbr = nullptr;
+    c->nbr_cap = 0;
+    if (cudaMalloc(&c->d_nbr, sizeof(uint32_t) * std::max<int64_t>(total, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
+    c->nbr_cap = total;
+  }
+  if (total1 > c->hh1_cap) {
+    if (c->d_hh1) cudaFree(c->d_hh1);
+    c->d_hh1 = nullptr;
+    c->hh1_cap = 0;
+    if (cudaMalloc(&c->d_hh1, sizeof(int) * std::max<int64_t>(total1, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
+    c->hh1_cap = total1;
+  }
+  cudaStream_t st = c->stream;
+  A2C_CUDA(cudaMemcpyAsync(c->d_off, off.data(), sizeof(int64_t) * (N + 1), cudaMemcpyHostToDevice, st));
+  if (N > 0) A2C_CUDA(cudaMemcpyAsync(c->d_npd, npd.data(), sizeof(int) * N, cudaMemcpyHostToDevice, st));
+  if (total > 0) A2C_CUDA(cudaMemcpyAsync(c->d_nbr, nbr.data(), sizeof(uint32_t) * total, cudaMemcpyHostToDevice, st));
+  if (nH > 0) A2C_CUDA(cudaMemcpyAsync(c->d_hh1_off, hh1_off, sizeof(int64_t) * (nH + 1), cudaMemcpyHostToDevice, st));
+  if (total1 > 0) A2C_CUDA(cudaMemcpyAsync(c->d_hh1, hh1_idx, sizeof(int) * total1, cudaMemcpyHostToDevice, st));
+  if (PdPdnum && nPd > 0)
+    A2C_CUDA(cudaMemcpyAsync(c->d_shell, PdPdnum, sizeof(int) * 3 * nPd, cudaMemcpyHostToDevice, st));
+  else if (nPd > 0)
+    A2C_CUDA(cudaMemsetAsync(c->d_shell, 0, sizeof(int) * 3 * nPd, st));
+  A2C_CUDA(cudaStreamSynchronize(st));  // host vectors go out of scope
+  c->nbr_total = total;
+  c->hh1_total = total1;
+  c->max_neighbors = maxn;
+  c->has_neighbors = true;
+  c->has_density = false;
+  if (X && N > 0) {
+    A2C_TRY(copy_in(c, c->d_X, X, 4 * N));
+    c->has_state = true;
+  }
+  return finish(c);
+}
+
 a2c_status a2c_gpp_neighbor_total(a2c_gpp_ctx *c, int list, int64_t *total) {
   if (!c || !total || list < 0 || list > 4) return A2C_ERR_INVALID;
   if (!c->has_neighbors) return A2C_ERR_STATE;
@@ -536,6 +622,44 @@ a2c_status a2c_gpp_diffuse(a2c_gpp_ctx *c, double dt, double nu, double Qm, doub
   free_hscratch(c, dg, dsend, dx, dfull);
   if (s) return s;
   return finish(c);
+}
+
+a2c_status a2c_diffuse_lists(int device, int nH, const int64_t *hh1_off, const int *hh1_idx, const double *x0,
+                             const double *gamma, const int *full_H, double T, double dt, double nu, double Qm,
+                             double xLb, double xUb, double *x) {
+  if (nH < 0 || (nH > 0 && (!hh1_off || !x0 || !gamma || !full_H || !x)) || !(T > 0.0)) return A2C_ERR_INVALID;
+  if (nH == 0) return A2C_OK;
+  const int64_t total = hh1_off[nH];
+  if (total > 0 && !hh1_idx) return A2C_ERR_INVALID;
+  for (int64_t t = 0; t < total; ++t)
+    if (hh1_idx[t] < 0 || hh1_idx[t] >= nH) return A2C_ERR_INVALID;
+  a2c_gpp_params p;
+  a2c_gpp_default_params(&p);
+  p.nPd = 0;
+  p.nH = nH;
+  p.T = T;
+  p.device = device;
+  a2c_gpp_ctx *c = nullptr;
+  A2C_TRY(a2c_gpp_create(&p, &c));
+  DeviceGuard g(c->device);
+  a2c_status s = A2C_OK;
+  double *dg = nullptr, *dsend = nullptr, *dx = nullptr;
+  int *dfull = nullptr;
+  if (cudaMalloc(&c->d_hh1, sizeof(int) * std::max<int64_t>(total, 1)) != cudaSuccess) s = A2C_ERR_NOMEM;
+  if (!s) s = ensure_hscratch(c, &dg, &dsend, &dx, &dfull);
+  if (!s && (cudaMemcpyAsync(c->d_hh1_off, hh1_off, sizeof(int64_t) * (nH + 1), cudaMemcpyHostToDevice, c->stream) ||
+             (total > 0 && cudaMemcpyAsync(c->d_hh1, hh1_idx, sizeof(int) * total, cudaMemcpyHostToDevice, c->stream)) ||
+             cudaMemcpyAsync(c->d_occ, x0, sizeof(double) * nH, cudaMemcpyHostToDevice, c->stream) ||
+             cudaMemcpyAsync(dg, gamma, sizeof(double) * nH, cudaMemcpyHostToDevice, c->stream) ||
+             cudaMemcpyAsync(dfull, full_H, sizeof(int) * nH, cudaMemcpyHostToDevice, c->stream) ||
+             cudaMemcpyAsync(dx, x, sizeof(double) * nH, cudaMemcpyHostToDevice, c->stream)))
+    s = A2C_ERR_CUDA;
+  if (!s) s = launch_diffuse(c, dg, dfull, dt, nu, Qm, xLb, xUb, dx);
+  if (!s && cudaMemcpyAsync(x, dx, sizeof(double) * nH, cudaMemcpyDeviceToHost, c->stream)) s = A2C_ERR_CUDA;
+  if (dg) free_hscratch(c, dg, dsend, dx, dfull);
+  if (!s) s = finish(c);
+  a2c_gpp_destroy(c);
+  return s;
 }
 
 a2c_status a2c_gpp_macro_results(a2c_gpp_ctx *c, const double *x, const int *HSurf, int nSurf, double *xH,

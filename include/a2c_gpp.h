@@ -136,6 +136,17 @@ a2c_status a2c_gpp_get_state(a2c_gpp_ctx *ctx, double *X);
  * as in the reference.  max_neighbors receives the largest per-site count
  * (the reference's maxNeib). */
 a2c_status a2c_gpp_build_neighbors(a2c_gpp_ctx *ctx, const double *X, int *max_neighbors);
+/* Neighbor lists supplied by the caller in the reference's form (the
+ * PdPd/PdH/HPd/HH/HH1 vectors of findNeighbors / findLocalNeighbors, as
+ * offsets[n+1] + local indices; PdPdnum may be NULL), e.g. the reference's
+ * own KD-tree lists.  Each site's sums then run in the given order, as the
+ * reference's loops do.  X gives the positions used to fix periodic images
+ * (the reference has none: with no periodic dimension X may be NULL). */
+a2c_status a2c_gpp_set_neighbor_lists(a2c_gpp_ctx *ctx, const double *X, const int64_t *pdpd_off,
+                                      const int *pdpd_idx, const int64_t *pdh_off, const int *pdh_idx,
+                                      const int64_t *hpd_off, const int *hpd_idx, const int64_t *hh_off,
+                                      const int *hh_idx, const int64_t *hh1_off, const int *hh1_idx,
+                                      const int *PdPdnum);
 /* Sizes for a2c_gpp_get_neighbors: total entries of a list. */
 a2c_status a2c_gpp_neighbor_total(a2c_gpp_ctx *ctx, int list_id, int64_t *total);
 /* Export a list in the reference's form: offsets[n+1], idx[total] local to
@@ -210,6 +221,13 @@ a2c_status a2c_gpp_apply_dirichlet(a2c_gpp_ctx *ctx, const int *sites, int n, do
  * caller's value).  Replaces integrateDiffusion (integrate.cpp:9-87). */
 a2c_status a2c_gpp_diffuse(a2c_gpp_ctx *ctx, double dt, double nu, double Qm, double xLb, double xUb,
                            const double *gamma, const int *full_H, double *x);
+
+/* The same step with caller-supplied first-shell lists and occupancy, no
+ * context: integrateDiffusion's own signature (integrate.cpp:9-87), on
+ * `device`.  x0, gamma, full_H, x are host arrays of nH. */
+a2c_status a2c_diffuse_lists(int device, int nH, const int64_t *hh1_off, const int *hh1_idx, const double *x0,
+                             const double *gamma, const int *full_H, double T, double dt, double nu, double Qm,
+                             double xLb, double xUb, double *x);
 
 /* Mean H fraction over all H sites and over sites not in HSurf.  Replaces
  * calculateMacroResults (calculateresults.cpp:8-78). */
