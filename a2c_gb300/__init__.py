@@ -14,8 +14,11 @@ import numpy as np
 
 from . import _native as N
 from ._native import A2CError, A2C_FP64, A2C_MIXED  # noqa: F401
+from ._native import (CONVERGED_GATOL, CONVERGED_STALLED, DIVERGED_LS_FAILURE, DIVERGED_MAXFCN,  # noqa: F401
+                      DIVERGED_MAXITS, DIVERGED_NAN)
 
-__all__ = ["Gpp", "lattice_fcc", "peak_flops", "restart_write", "restart_read", "A2CError", "A2C_FP64", "A2C_MIXED", "LbfgsResult"]
+__all__ = ["Gpp", "Batch", "BatchResult", "batch_workload", "lattice_fcc", "peak_flops", "restart_write",
+           "restart_read", "A2CError", "A2C_FP64", "A2C_MIXED", "LbfgsResult"]
 
 
 @dataclass
@@ -189,6 +192,14 @@ class Gpp:
         N.check(self._L.a2c_gpp_bounds(self._h, N.ptr(lb), N.ptr(ub)), "a2c_gpp_bounds")
         return lb, ub
 
+    def autotune(self, reps: int = 3) -> tuple[int, dict]:
+        """Threads per site chosen by the library's autotuner at the current
+        state, and the mean milliseconds per evaluation of each candidate."""
+        t = C.c_int()
+        ms = (C.c_float * 4)()
+        N.check(self._L.a2c_gpp_autotune(self._h, int(reps), C.byref(t), ms), "a2c_gpp_autotune")
+        return t.value, {k: float(v) for k, v in zip((1, 2, 4, 8), ms)}
+
     def minimize(self, X, **kw) -> LbfgsResult:
         lp = N.LbfgsParams()
         self._L.a2c_lbfgs_default_params(C.byref(lp))
@@ -260,6 +271,124 @@ class Gpp:
         return a.value, b.value
 
 
+@dataclass
+class BatchResult:
+    X: np.ndarray         # concatenated minima
+    fmin: np.ndarray      # per instance
+    iters: np.ndarray
+    nfev: np.ndarray
+    gnorm: np.ndarray
+    reason: np.ndarray
+    mixed_iters: np.ndarray
+    fp64_iters: np.ndarray
+    ticks: int            # evaluations of every live instance
+    seconds: float        # device time of the minimization
+
+
+class Batch:
+    """Many independent lattices evaluated and minimized together
+    (a2c_gpp_batch_*).  `instances` is a sequence of dicts with keys nPd, nH
+    and optionally T, box, periodic; the remaining parameters are shared.
+    Arrays are the instances' arrays concatenated in instance order."""
+
+    def __init__(self, instances, *, QWp: float = 1.0 / 12.0, eps: float = 1e-5, rc: float = 5.35,
+                 a_Pd: float = 3.89, precision: int | str = A2C_FP64, device: int = 0):
+        L = N.lib()
+        if isinstance(precision, str):
+            precision = {"fp64": A2C_FP64, "mixed": A2C_MIXED}[precision]
+        arr = (N.GppParams * len(instances))()
+        self.sizes = []
+        for k, inst in enumerate(instances):
+            p = arr[k]
+            L.a2c_gpp_default_params(C.byref(p))
+            p.nPd, p.nH = int(inst["nPd"]), int(inst["nH"])
+            p.T = float(inst.get("T", 300.0))
+            p.QWp, p.eps, p.rc, p.a_Pd = QWp, eps, rc, a_Pd
+            box, per = inst.get("box", (0.0, 0.0, 0.0)), inst.get("periodic", (0, 0, 0))
+            for d in range(3):
+                p.box[d] = float(box[d])
+                p.periodic[d] = int(bool(per[d]))
+            p.precision = int(precision)
+            p.device = int(device)
+            self.sizes.append((p.nPd, p.nH))
+        self.B = len(instances)
+        self.N = sum(a + b for a, b in self.sizes)
+        self.nH = sum(b for _, b in self.sizes)
+        self.offsets = np.cumsum([0] + [a + b for a, b in self.sizes])
+        h = C.c_void_p()
+        N.check(L.a2c_gpp_batch_create(arr, self.B, C.byref(h)), "a2c_gpp_batch_create")
+        self._h = h
+        self._L = L
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.check(self._L.a2c_gpp_batch_destroy(self._h), "a2c_gpp_batch_destroy")
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_occupancy(self, xH) -> None:
+        N.check(self._L.a2c_gpp_batch_set_occupancy(self._h, N.ptr(_f64(xH, self.nH))), "a2c_gpp_batch_set_occupancy")
+
+    def build_neighbors(self, X) -> int:
+        m = C.c_int()
+        N.check(self._L.a2c_gpp_batch_build_neighbors(self._h, N.ptr(_f64(X, 4 * self.N)), C.byref(m)),
+                "a2c_gpp_batch_build_neighbors")
+        return m.value
+
+    def set_threads_per_site(self, tps: int) -> None:
+        N.check(self._L.a2c_gpp_batch_set_threads_per_site(self._h, int(tps)), "a2c_gpp_batch_set_threads_per_site")
+
+    def set_graphs(self, on: bool) -> None:
+        N.check(self._L.a2c_gpp_batch_set_graphs(self._h, int(bool(on))), "a2c_gpp_batch_set_graphs")
+
+    def eval(self, X) -> tuple[np.ndarray, np.ndarray]:
+        f = np.empty(self.B)
+        G = np.empty(4 * self.N)
+        N.check(self._L.a2c_gpp_batch_eval(self._h, N.ptr(_f64(X, 4 * self.N)), N.ptr(f), N.ptr(G)),
+                "a2c_gpp_batch_eval")
+        return f, G
+
+    def minimize(self, X, **kw) -> BatchResult:
+        lp = N.LbfgsParams()
+        self._L.a2c_lbfgs_default_params(C.byref(lp))
+        for k, v in kw.items():
+            setattr(lp, k, v)
+        X = _f64(X, 4 * self.N).copy()
+        B = self.B
+        fmin, gn = np.empty(B), np.empty(B)
+        it, nf, why, mi, fi = (np.empty(B, dtype=np.int32) for _ in range(5))
+        N.check(self._L.a2c_gpp_batch_minimize(self._h, N.ptr(X), C.byref(lp), N.ptr(fmin), N.ptr(it), N.ptr(nf),
+                                               N.ptr(gn), N.ptr(why), N.ptr(mi), N.ptr(fi)), "a2c_gpp_batch_minimize")
+        t, sec = C.c_int(), C.c_double()
+        N.check(self._L.a2c_gpp_batch_stats(self._h, C.byref(t), C.byref(sec)), "a2c_gpp_batch_stats")
+        return BatchResult(X, fmin, it, nf, gn, why, mi, fi, t.value, sec.value)
+
+    def autotune(self, X, reps: int = 3) -> tuple[int, dict]:
+        """Threads per site chosen by the library's autotuner, and the mean
+        milliseconds per evaluation of each candidate."""
+        t = C.c_int()
+        ms = (C.c_float * 4)()
+        N.check(self._L.a2c_gpp_batch_autotune(self._h, N.ptr(_f64(X, 4 * self.N)), int(reps), C.byref(t), ms),
+                "a2c_gpp_batch_autotune")
+        return t.value, {k: float(v) for k, v in zip((1, 2, 4, 8), ms)}
+
+    def split(self, X) -> list[np.ndarray]:
+        """Per-instance views of a concatenated 4N array."""
+        X = np.asarray(X)
+        return [X[4 * self.offsets[k]:4 * self.offsets[k + 1]] for k in range(self.B)]
+
+
 def restart_write(path: str, nPd: int, nH: int, X, xH, gamma, full_H, step: int = 0, time: float = 0.0) -> None:
     """Restart file in the format the reference's readResults reads."""
     N.check(N.lib().a2c_restart_write(str(path).encode(), nPd, nH, N.ptr(_f64(X, 4 * (nPd + nH))),
@@ -312,3 +441,30 @@ def lattice_fcc(ncell, *, a: float = 3.89, periodic=(1, 1, 1), pos_std: float = 
     N.check(N.lib().a2c_lattice_fcc(C.byref(sp), N.ptr(X), N.ptr(xH), N.ptr(surf)), "a2c_lattice_fcc")
     box = tuple(float(ncell[d]) * a for d in range(3))
     return X, xH, surf, box, nPd, nH
+
+
+def batch_workload(n: int = 256, edge=(4, 16), T=(200.0, 600.0), x_mean=(0.01, 0.70), x_jitter: float = 0.02,
+                   pos_std: float = 0.02, sigma: float = 0.10, seed: int = 4):
+    """The batched-instances workload: n independent periodic fcc Pd + H
+    lattices, instance k with edge ~ U{edge[0]..edge[1]} cells, T ~ U(T),
+    mean occupancy ~ U(x_mean) with per-site jitter U(-x_jitter, x_jitter)
+    (clamped to [1e-3, 1 - 1e-16]), N(0, pos_std) positions, sigma fixed.
+    The per-instance draws come from numpy's PCG64 seeded with `seed`,
+    instance after instance; instance k's lattice is a2c_lattice_fcc with
+    seed 1000 * seed + k.
+
+    Returns (instances, X, xH): the dicts Batch() takes and the concatenated
+    state and occupancy."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    instances, Xs, xs = [], [], []
+    for k in range(n):
+        e = int(rng.integers(edge[0], edge[1] + 1))
+        t = float(rng.uniform(T[0], T[1]))
+        xm = float(rng.uniform(x_mean[0], x_mean[1]))
+        X, xH, _, box, nPd, nH = lattice_fcc(e, periodic=(1, 1, 1), pos_std=pos_std, sigma=(sigma, sigma),
+                                             x_center=xm, x_half=x_jitter, seed=1000 * seed + k)
+        instances.append({"nPd": nPd, "nH": nH, "T": t, "box": box, "periodic": (1, 1, 1), "edge": e,
+                          "x_mean": xm})
+        Xs.append(X)
+        xs.append(xH)
+    return instances, np.concatenate(Xs), np.concatenate(xs)

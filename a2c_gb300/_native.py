@@ -121,6 +121,18 @@ def lib() -> C.CDLL:
         "a2c_gpp_dmd_run": (I, [P, P, P, P, P, P, I, P, I, C.POINTER(DmdParams), I, P, P, P, P]),
         "a2c_restart_write": (I, [C.c_char_p, I, I, P, P, P, P, I, D]),
         "a2c_restart_read": (I, [C.c_char_p, I, I, D, D, P, P, P, P]),
+        "a2c_gpp_batch_create": (I, [C.POINTER(GppParams), I, C.POINTER(C.c_void_p)]),
+        "a2c_gpp_batch_destroy": (I, [P]),
+        "a2c_gpp_batch_info": (I, [P, C.POINTER(I), C.POINTER(C.c_int64)]),
+        "a2c_gpp_batch_set_occupancy": (I, [P, P]),
+        "a2c_gpp_batch_build_neighbors": (I, [P, P, C.POINTER(I)]),
+        "a2c_gpp_batch_set_threads_per_site": (I, [P, I]),
+        "a2c_gpp_batch_set_graphs": (I, [P, I]),
+        "a2c_gpp_batch_eval": (I, [P, P, P, P]),
+        "a2c_gpp_batch_minimize": (I, [P, P, C.POINTER(LbfgsParams), P, P, P, P, P, P, P]),
+        "a2c_gpp_batch_stats": (I, [P, C.POINTER(I), C.POINTER(D)]),
+        "a2c_gpp_batch_autotune": (I, [P, P, I, C.POINTER(I), P]),
+        "a2c_gpp_autotune": (I, [P, I, C.POINTER(I), P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -139,7 +151,11 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_neighbor_total", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
             "a2c_gpp_eval_device", "a2c_gpp_profile_eval", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
             "a2c_gpp_chem_potential", "a2c_gpp_minimize_stats", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",
-            "a2c_lattice_fcc", "a2c_gpp_peak_flops", "a2c_gpp_dmd_run", "a2c_restart_write", "a2c_restart_read"]
+            "a2c_lattice_fcc", "a2c_gpp_peak_flops", "a2c_gpp_dmd_run", "a2c_restart_write", "a2c_restart_read",
+            "a2c_gpp_batch_create", "a2c_gpp_batch_destroy", "a2c_gpp_batch_info", "a2c_gpp_batch_set_occupancy",
+            "a2c_gpp_batch_build_neighbors", "a2c_gpp_batch_set_threads_per_site", "a2c_gpp_batch_set_graphs",
+            "a2c_gpp_batch_eval", "a2c_gpp_batch_minimize", "a2c_gpp_batch_stats", "a2c_gpp_batch_autotune",
+            "a2c_gpp_autotune"]
 
 
 class A2CError(RuntimeError):

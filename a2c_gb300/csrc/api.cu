@@ -219,6 +219,50 @@ a2c_status a2c_gpp_set_threads_per_site(a2c_gpp_ctx *c, int tps) {
   return mixed_set_threads_per_site(c, tps);
 }
 
+// Autotuner of the mixed form's work mapping: each threads-per-site choice
+// (1, 2, 4, 8) evaluates the context's current state once untimed and then
+// `reps` times between two events on the context's stream; the fastest
+// choice is kept.
+a2c_status a2c_gpp_autotune(a2c_gpp_ctx *c, int reps, int *tps_out, float *ms) {
+  if (!c || reps < 1 || reps > 1000) return A2C_ERR_INVALID;
+  if (!c->has_neighbors || !c->has_state) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  const int saved = c->p.precision;
+  c->p.precision = A2C_MIXED;
+  double *d_f = c->d_red + 2 * 1024 + 8;
+  cudaEvent_t e0, e1;
+  A2C_CUDA(cudaEventCreate(&e0));
+  A2C_CUDA(cudaEventCreate(&e1));
+  const int choice[4] = {1, 2, 4, 8};
+  float best_ms = 0.0f;
+  int best = 0;
+  a2c_status s = A2C_OK;
+  for (int k = 0; k < 4 && !s; ++k) {
+    s = mixed_set_threads_per_site(c, choice[k]);
+    if (!s) s = eval_device_impl(c, c->d_X, d_f, c->d_G);
+    if (!s && cudaEventRecord(e0, c->stream) != cudaSuccess) s = A2C_ERR_CUDA;
+    for (int r = 0; r < reps && !s; ++r) s = eval_device_impl(c, c->d_X, d_f, c->d_G);
+    if (!s && cudaEventRecord(e1, c->stream) != cudaSuccess) s = A2C_ERR_CUDA;
+    float t = 0.0f;
+    if (!s && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+      s = A2C_ERR_CUDA;
+    t /= (float)reps;
+    if (ms) ms[k] = t;
+    if (!s && (best == 0 || t < best_ms)) {
+      best_ms = t;
+      best = choice[k];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->p.precision = saved;
+  c->has_density = false;
+  if (!s) s = mixed_set_threads_per_site(c, best);
+  if (!s && tps_out) *tps_out = best;
+  if (!s) s = check_status_word(c);
+  return s;
+}
+
 a2c_status a2c_gpp_synchronize(a2c_gpp_ctx *c) {
   if (!c) return A2C_ERR_INVALID;
   DeviceGuard g(c->device);

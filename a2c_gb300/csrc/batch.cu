@@ -1,0 +1,1265 @@
+// Batched independent instances: many Pd-H lattices of uneven size,
+// temperature and loading minimized together in one system.
+//
+// Layout.  The instances' sites are concatenated in the caller's order
+// (instance-major; within an instance Pd then H, the reference's layout of
+// minimizer.cpp:398-418), so the state vector of the batch is the
+// concatenation of the instances' 4N-double TAO vectors.  Each site carries
+// its instance index; the per-instance box, temperature and species split
+// come from a small table.  Neighbor lists are built per instance (the same
+// cell-list build as one system) and stored with batch-global ids, so one
+// launch of each evaluator kernel walks every instance at once.
+//
+// Minimization.  Each instance runs the projected L-BFGS of lbfgs.cu (the
+// stand-in for TAO BLMVM, minimizer.cpp:534-586) with its own iterate,
+// memory, step length and stopping state.  The control flow lives on the
+// device: one "tick" is a fixed sequence of launches that (A) computes a new
+// direction for every instance that needs one, (B) compacts the lists of
+// live sites and reduction chunks, (C) evaluates every live instance at its
+// trial point and (D) applies each instance's line-search decision.  Every
+// live instance receives exactly one evaluation per tick, so the tick can be
+// captured once in a CUDA graph and replayed; converged instances drop out
+// of the lists (they retire) and cost nothing afterwards.
+//
+// Reductions.  Per instance, its terms are cut into chunks of kChunk
+// consecutive terms; a block reduces each chunk and one block per instance
+// sums the chunk partials in order.  The order depends only on the
+// instance's own size, so an instance's results do not depend on the rest of
+// the batch, and the oracle reproduces them (its "batch" reduction order).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace a2c {
+namespace {
+
+constexpr int kChunk = 2048;  // terms per reduction chunk
+constexpr int kBlk = 256;
+constexpr int kMaxM = 48;
+
+enum : int { kNeedEval = 0, kNeedDir = 1, kLineSearch = 2, kDone = 3 };
+enum : int { kPhaseMixed = 0, kPhaseFp64 = 1 };
+
+// Per-instance L-BFGS state.
+struct Inst {
+  double f, fn, alpha, amax, gnorm, coef, gam_num, gam_den, f_noise, stall_rtol, mixed_gnorm;
+  int state, phase, npairs, head, it, fev, ls, why, copy, steep, nhist, it0, mixed_iters, fp64_iters;
+};
+
+struct Chunk {
+  int64_t start;  // first term (element or site index)
+  int len;
+  int inst;
+};
+
+// Constants of one minimization.
+struct Cfg {
+  int B, m, ring, max_it, max_fev, max_ls, polish, W;
+  int64_t nec, nsc, n;  // element chunks, site chunks, vector length
+  double gatol, c1, init_step, lb;
+  double fn_mixed, fn_fp64, st_mixed, st_fp64;
+};
+
+// Device pointers of the batch state (kernel parameter).
+struct Dev {
+  Inst *st;
+  const InstGeo *geo;
+  const Chunk *ech, *sch;  // element / site chunks
+  const int *ecb, *scb;    // per instance: first chunk (B + 1)
+  const int *le, *ls;      // live element / site chunks
+  int *cnt;                // list lengths, see kCnt*
+  double *x, *g, *pg, *d, *xn, *gn, *S, *Y;
+  double *part;            // 8 x nec element partials, then 2 x nsc site partials
+  double *rho, *alph;      // B x ring
+  double *fh;              // B x (W + 1): objective history of the phase
+  const double *Vs, *Ss;
+};
+
+enum : int { kCntMixed = 0, kCntFp64 = 1, kCntEch = 2, kCntSch = 3, kCntLive = 4, kCntChanged = 5, kCntLeft = 6 };
+
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double wmax(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+// block of kBlk threads: the warp tree, then warp 0 over the 8 warp sums
+template <bool MAX>
+__device__ __forceinline__ double bred(double v, double *sh) {
+  v = MAX ? wmax(v) : wsum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  v = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
+  if (w == 0) v = MAX ? wmax(v) : wsum(v);
+  __syncthreads();
+  return v;
+}
+
+__device__ __forceinline__ bool on_bound(int64_t t, const double *x, const double *g, double lb) {
+  return (t & 3) == 3 && x[t] <= lb && g[t] > 0.0;
+}
+
+// sum over the instance's chunk partials part[c], c in [c0, c1), in order
+__device__ __forceinline__ double chunk_total(const double *part, int c0, int c1, double *sh) {
+  double s = 0.0;
+  for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) s += part[i];
+  return bred<false>(s, sh);
+}
+__device__ __forceinline__ double chunk_max(const double *part, int c0, int c1, double *sh) {
+  double s = 0.0;
+  for (int i = c0 + threadIdx.x; i < c1; i += blockDim.x) s = fmax(s, part[i]);
+  return bred<true>(s, sh);
+}
+
+__device__ __forceinline__ int slot(int head, int k, int ring) { return ((head - 1 - k) % ring + ring) % ring; }
+
+// End of a phase: hand over to the FP64 polish, or retire.
+__device__ void end_phase(Inst &I, const Cfg &cf, int why) {
+  if (I.phase == kPhaseMixed) {
+    I.mixed_iters = I.it;
+    I.mixed_gnorm = I.gnorm;
+  } else {
+    I.fp64_iters = I.it - I.it0;
+  }
+  I.why = why;
+  if (I.phase == kPhaseMixed && cf.polish && (why == A2C_CONVERGED_GATOL || why == A2C_DIVERGED_LS_FAILURE ||
+                                               why == A2C_CONVERGED_STALLED)) {
+    I.phase = kPhaseFp64;
+    I.state = kNeedEval;
+    I.nhist = 0;
+    I.it0 = I.it;
+    I.f_noise = cf.fn_fp64;
+    I.stall_rtol = cf.st_fp64;
+  } else {
+    I.state = kDone;
+  }
+}
+
+// ------------------------------------------------------------ set-up
+__global__ void k_init_state(Dev D, Cfg cf, int phase0) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= cf.B) return;
+  Inst I;
+  memset(&I, 0, sizeof(I));
+  I.state = kNeedEval;
+  I.phase = phase0;
+  I.f_noise = phase0 == kPhaseMixed ? cf.fn_mixed : cf.fn_fp64;
+  I.stall_rtol = phase0 == kPhaseMixed ? cf.st_mixed : cf.st_fp64;
+  D.st[b] = I;
+}
+
+__global__ void k_project_all(double *x, int64_t n, double lb) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    if ((t & 3) == 3 && x[t] < lb) x[t] = lb;
+}
+
+// ------------------------------------------------------------ list plan
+// One block: per instance its listing code (-1 retired, 0 mixed, 1 FP64),
+// exclusive prefix sums of the site and chunk counts, and whether anything
+// changed since the last plan (only then does k_fill rewrite the lists).
+constexpr int kPlanThreads = 1024;
+__global__ void __launch_bounds__(kPlanThreads) k_plan(Dev D, int B, int *listed, int *loff) {
+  __shared__ int sh[7][kPlanThreads];
+  __shared__ int changed;
+  if (threadIdx.x == 0) changed = 0;
+  const int per = (B + kPlanThreads - 1) / kPlanThreads;
+  const int b0 = min(B, (int)threadIdx.x * per), b1 = min(B, b0 + per);
+  int q[7] = {0, 0, 0, 0, 0, 0, 0};
+  bool ch = false;
+  for (int b = b0; b < b1; ++b) {
+    const Inst &I = D.st[b];
+    const int code = I.state == kDone ? -1 : I.phase;
+    if (code != listed[b]) ch = true;
+    const InstGeo &g = D.geo[b];
+    if (code == 0) { q[0] += g.nPd; q[1] += g.nH; }
+    if (code == 1) { q[2] += g.nPd; q[3] += g.nH; }
+    if (code >= 0) {
+      q[4] += D.ecb[b + 1] - D.ecb[b];
+      q[5] += D.scb[b + 1] - D.scb[b];
+      q[6] += 1;
+    }
+  }
+  __syncthreads();
+  if (ch) atomicOr(&changed, 1);
+  for (int k = 0; k < 7; ++k) sh[k][threadIdx.x] = q[k];
+  __syncthreads();
+  // inclusive Hillis-Steele scan of the per-thread sums
+  for (int o = 1; o < kPlanThreads; o <<= 1) {
+    int v[7];
+    for (int k = 0; k < 7; ++k) v[k] = threadIdx.x >= (unsigned)o ? sh[k][threadIdx.x - o] : 0;
+    __syncthreads();
+    for (int k = 0; k < 7; ++k) sh[k][threadIdx.x] += v[k];
+    __syncthreads();
+  }
+  int run[7];
+  for (int k = 0; k < 7; ++k) run[k] = sh[k][threadIdx.x] - q[k];
+  const int totPdM = sh[0][kPlanThreads - 1], totPdF = sh[2][kPlanThreads - 1];
+  if (changed) {
+    for (int b = b0; b < b1; ++b) {
+      const Inst &I = D.st[b];
+      const int code = I.state == kDone ? -1 : I.phase;
+      const InstGeo &g = D.geo[b];
+      int *o = loff + 6 * b;
+      o[0] = code == 0 ? run[0] : (code == 1 ? run[2] : -1);               // Pd sites
+      o[1] = code == 0 ? totPdM + run[1] : (code == 1 ? totPdF + run[3] : -1);  // H sites
+      o[2] = code >= 0 ? run[4] : -1;
+      o[3] = code >= 0 ? run[5] : -1;
+      o[4] = code;
+      if (code == 0) { run[0] += g.nPd; run[1] += g.nH; }
+      if (code == 1) { run[2] += g.nPd; run[3] += g.nH; }
+      if (code >= 0) {
+        run[4] += D.ecb[b + 1] - D.ecb[b];
+        run[5] += D.scb[b + 1] - D.scb[b];
+      }
+      listed[b] = code;
+    }
+  }
+  if (threadIdx.x == kPlanThreads - 1) {
+    D.cnt[kCntMixed] = sh[0][threadIdx.x] + sh[1][threadIdx.x];
+    D.cnt[kCntFp64] = sh[2][threadIdx.x] + sh[3][threadIdx.x];
+    D.cnt[kCntEch] = sh[4][threadIdx.x];
+    D.cnt[kCntSch] = sh[5][threadIdx.x];
+    D.cnt[kCntLive] = sh[6][threadIdx.x];
+    D.cnt[kCntChanged] = changed;
+  }
+}
+
+// One block per instance: its sites into the mixed or FP64 list (Pd sites
+// of all listed instances first, so warps stay species-uniform) and its
+// chunks into the live chunk lists.
+__global__ void k_fill(Dev D, int B, const int *loff, int *lm, int *lf, int *le, int *ls) {
+  if (!D.cnt[kCntChanged]) return;
+  const int b = blockIdx.x;
+  if (b >= B) return;
+  const int *o = loff + 6 * b;
+  const int code = o[4];
+  if (code < 0) return;
+  const InstGeo &g = D.geo[b];
+  int *L = code == 0 ? lm : lf;
+  for (int i = threadIdx.x; i < g.nPd; i += blockDim.x) L[o[0] + i] = g.start + i;
+  for (int i = threadIdx.x; i < g.nH; i += blockDim.x) L[o[1] + i] = g.start + g.nPd + i;
+  const int e0 = D.ecb[b], ne = D.ecb[b + 1] - e0, s0 = D.scb[b], ns = D.scb[b + 1] - s0;
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) le[o[2] + i] = e0 + i;
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) ls[o[3] + i] = s0 + i;
+}
+
+__global__ void k_count_left(Dev D, int B) {
+  __shared__ double sh[kBlk / 32];
+  double v = 0.0;
+  for (int b = threadIdx.x; b < B; b += blockDim.x) v += D.st[b].state != kDone ? 1.0 : 0.0;
+  v = bred<false>(v, sh);
+  if (threadIdx.x == 0) D.cnt[kCntLeft] = (int)v;
+}
+
+// ------------------------------------------------------------ direction
+// Element-chunk kernels walk the live element chunks; a whole block takes
+// one chunk, so the per-instance tests below are block-uniform.
+#define A2C_ECHUNKS(D)                                                     \
+  for (int kk = blockIdx.x; kk < (D).cnt[kCntEch]; kk += gridDim.x) {       \
+    const int c = (D).le[kk];                                             \
+    const Chunk ch = (D).ech[c];                                          \
+    Inst &I = (D).st[ch.inst];
+#define A2C_ECHUNKS_END }
+
+// pg = projected gradient; partials of |pg|^2 and max |pg|
+__global__ void __launch_bounds__(kBlk) k_projgrad(Dev D, Cfg cf) {
+  __shared__ double sh[kBlk / 32];
+  A2C_ECHUNKS(D)
+  if (I.state != kNeedDir) continue;
+  double s = 0.0, mx = 0.0;
+  for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+    const int64_t t = ch.start + i;
+    const double v = on_bound(t, D.x, D.g, cf.lb) ? 0.0 : D.g[t];
+    D.pg[t] = v;
+    s += v * v;
+    mx = fmax(mx, fabs(v));
+  }
+  s = bred<false>(s, sh);
+  mx = bred<true>(mx, sh);
+  if (threadIdx.x == 0) {
+    D.part[c] = s;
+    D.part[cf.nec + c] = mx;
+  }
+  A2C_ECHUNKS_END
+}
+
+// gnorm and the stopping tests (TAO's gatol test and the caps)
+__global__ void __launch_bounds__(kBlk) k_dir_begin(Dev D, Cfg cf) {
+  __shared__ double sh[kBlk / 32];
+  const int b = blockIdx.x;
+  Inst &I = D.st[b];
+  if (threadIdx.x == 0) I.copy = 0;
+  if (I.state != kNeedDir) return;
+  const double s = chunk_total(D.part, D.ecb[b], D.ecb[b + 1], sh);
+  const double mx = chunk_max(D.part + cf.nec, D.ecb[b], D.ecb[b + 1], sh);
+  if (threadIdx.x != 0) return;
+  I.gnorm = sqrt(s);
+  I.amax = mx;
+  I.steep = 0;
+  if (!isfinite(I.f) || !isfinite(I.gnorm)) end_phase(I, cf, A2C_DIVERGED_NAN);
+  else if (I.gnorm <= cf.gatol) end_phase(I, cf, A2C_CONVERGED_GATOL);
+  else if (I.it >= cf.max_it) end_phase(I, cf, A2C_DIVERGED_MAXITS);
+  else if (I.fev >= cf.max_fev) end_phase(I, cf, A2C_DIVERGED_MAXFCN);
+  else I.steep = I.npairs == 0 ? 1 : 0;
+}
+
+// Two-loop recursion, first loop, step j (newest pair first): apply the
+// update of step j-1, then the partial dot S_j . q.
+__global__ void __launch_bounds__(kBlk) k_loop1(Dev D, Cfg cf, int j) {
+  __shared__ double sh[kBlk / 32];
+  A2C_ECHUNKS(D)
+  if (I.state != kNeedDir || I.steep) continue;
+  const int b = ch.inst, np = I.npairs;
+  const bool upd = j > 0 && j - 1 < np, dot = j < np;
+  if (j > 0 && !upd && !dot) continue;
+  const int slp = slot(I.head, j - 1, cf.ring), sl = slot(I.head, j, cf.ring);
+  const double a = upd ? D.alph[b * cf.ring + slp] : 0.0;
+  const double *Yp = D.Y + (size_t)slp * cf.n, *Sj = D.S + (size_t)sl * cf.n;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+    const int64_t t = ch.start + i;
+    double q = j == 0 ? D.pg[t] : D.d[t];
+    if (upd) q -= a * Yp[t];
+    D.d[t] = q;
+    if (dot) s += Sj[t] * q;
+  }
+  s = bred<false>(s, sh);
+  if (threadIdx.x == 0) D.part[2 * cf.nec + c] = s;
+  A2C_ECHUNKS_END
+}
+
+__global__ void __launch_bounds__(kBlk) k_loop1_fin(Dev D, Cfg cf, int j) {
+  __shared__ double sh[kBlk / 32];
+  const int b = blockIdx.x;
+  Inst &I = D.st[b];
+  if (I.state != kNeedDir || I.steep || j >= I.npairs) return;
+  const double s = chunk_total(D.part + 2 * cf.nec, D.ecb[b], D.ecb[b + 1], sh);
+  if (threadIdx.x == 0) {
+    const int sl = slot(I.head, j, cf.ring);
+    D.alph[b * cf.ring + sl] = s * D.rho[b * cf.ring + sl];
+  }
+}
+
+// the pending update of the last first-loop step, then q *= s.y / y.y
+__global__ void __launch_bounds__(kBlk) k_scale(Dev D, Cfg cf) {
+  A2C_ECHUNKS(D)
+  if (I.state != kNeedDir || I.steep) continue;
+  const int b = ch.inst;
+  const bool upd = I.npairs == cf.m;
+  const int slp = slot(I.head, cf.m - 1, cf.ring);
+  const double a = upd ? D.alph[b * cf.ring + slp] : 0.0;
+  const double gam = I.gam_num / I.gam_den;
+  const double *Yp = D.Y + (size_t)slp * cf.n;
+  for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+    const int64_t t = ch.start + i;
+    double q = D.d[t];
+    if (upd) q -= a * Yp[t];
+    D.d[t] = q * gam;
+  }
+  A2C_ECHUNKS_END
+}
+
+// Second loop, step j (oldest pair first): apply the update of step j-1,
+// then the partial dot Y_j . q.
+__global__ void __launch_bounds__(kBlk) k_loop2(Dev D, Cfg cf, int j) {
+  __shared__ double sh[kBlk / 32];
+  A2C_ECHUNKS(D)
+  if (I.state != kNeedDir || I.steep) continue;
+  const int np = I.npairs;
+  const bool upd = j > 0 && j - 1 < np, dot = j < np;
+  if (!upd && !dot) continue;
+  const int slp = slot(I.head, np - j, cf.ring), sl = slot(I.head, np - 1 - j, cf.ring);
+  const double cp = I.coef;
+  const double *Sp = D.S + (size_t)slp * cf.n, *Yj = D.Y + (size_t)sl * cf.n;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+    const int64_t t = ch.start + i;
+    double q = D.d[t];
+    if (upd) q += cp * Sp[t];
+    D.d[t] = q;
+    if (dot) s += Yj[t] * q;
+  }
+  s = bred<false>(s, sh);
+  if (threadIdx.x == 0) D.part[2 * cf.nec + c] = s;
+  A2C_ECHUNKS_END
+}
+
+__global__ void __launch_bounds__(kBlk) k_loop2_fin(Dev D, Cfg cf, int j) {
+  __shared__ double sh[kBlk / 32];
+  const int b = blockIdx.x;
+  Inst &I = D.st[b];
+  if (I.state != kNeedDir || I.steep || j >= I.npairs) return;
+  const double s = chunk_total(D.part + 2 * cf.nec, D.ecb[b], D.ecb[b + 1], sh);
+  if (threadIdx.x == 0) {
+    const int sl = slot(I.head, I.npairs - 1 - j, cf.ring);
+    I.coef = D.alph[b * cf.ring + sl] - D.rho[b * cf.ring + sl] * s;
+  }
+}
+
+// d = -q off the active set (or the scaled steepest descent); partial g.d
+__global__ void __launch_bounds__(kBlk) k_finish(Dev D, Cfg cf) {
+  __shared__ double sh[kBlk / 32];
+  A2C_ECHUNKS(D)
+  if (I.state != kNeedDir) continue;
+  const bool steep = I.steep != 0;
+  const bool upd = !steep && I.npairs == cf.m;
+  const int slp = slot(I.head, 0, cf.ring);
+  const double cp = I.coef, sc = -cf.init_step / I.amax;
+  const double *Sp = D.S + (size_t)slp * cf.n;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+    const int64_t t = ch.start + i;
+    double v;
+    if (steep) {
+      v = D.pg[t] * sc;
+    } else {
+      double q = D.d[t];
+      if (upd) q += cp * Sp[t];
+      v = on_bound(t, D.x, D.g, cf.lb) ? 0.0 : -q;
+    }
+    D.d[t] = v;
+    s += D.g[t] * v;
+  }
+  s = bred<false>(s, sh);
+  if (threadIdx.x == 0) D.part[3 * cf.nec + c] = s;
+  A2C_ECHUNKS_END
+}
+
+// not a descent direction: drop the memory, fall back to steepest descent
+__global__ void __launch_bounds__(kBlk) k_dir_end(Dev D, Cfg cf) {
+  __shared__ double sh[kBlk / 32];
+  const int b = blockIdx.x;
+  Inst &I = D.st[b];
+  if (I.state != kNeedDir) return;
+  const double gd = chunk_total(D.part + 3 * cf.nec, D.ecb[b], D.ecb[b + 1], sh);
+  if (threadIdx.x != 0) return;
+  if (!(gd < 0.0)) {
+    I.npairs = 0;
+    I.head = 0;
+    I.steep = 2;
+  } else {
+    I.steep = 0;
+  }
+  I.alpha = 1.0;
+  I.ls = 0;
+  I.state = kLineSearch;
+}
+
+__global__ void __launch_bounds__(kBlk) k_steep(Dev D, Cfg cf) {
+  A2C_ECHUNKS(D)
+  if (I.steep != 2) continue;
+  const double sc = -cf.init_step / I.amax;
+  for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+    const int64_t t = ch.start + i;
+    D.d[t] = D.pg[t] * sc;
+  }
+  A2C_ECHUNKS_END
+}
+
+// ------------------------------------------------------------ trial / decide
+// xn = P(x + alpha d) (line search) or xn = x (first evaluation of a
+// phase); partial g.(xn - x)
+__global__ void __launch_bounds__(kBlk) k_trial(Dev D, Cfg cf) {
+  __shared__ double sh[kBlk / 32];
+  A2C_ECHUNKS(D)
+  if (I.state != kLineSearch && I.state != kNeedEval) continue;
+  const bool ls = I.state == kLineSearch;
+  const double al = I.alpha;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+    const int64_t t = ch.start + i;
+    double v = D.x[t];
+    if (ls) {
+      v = D.x[t] + al * D.d[t];
+      if ((t & 3) == 3 && v < cf.lb) v = cf.lb;
+      s += D.g[t] * (v - D.x[t]);
+    }
+    D.xn[t] = v;
+  }
+  s = bred<false>(s, sh);
+  if (threadIdx.x == 0) D.part[4 * cf.nec + c] = s;
+  A2C_ECHUNKS_END
+}
+
+// candidate pair into the free ring slot; partials gn.s, s.y, y.y
+__global__ void __launch_bounds__(kBlk) k_post(Dev D, Cfg cf) {
+  __shared__ double sh[kBlk / 32];
+  A2C_ECHUNKS(D)
+  if (I.state != kLineSearch) continue;
+  double *Sh = D.S + (size_t)I.head * cf.n, *Yh = D.Y + (size_t)I.head * cf.n;
+  double dn = 0.0, sy = 0.0, yy = 0.0;
+  for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+    const int64_t t = ch.start + i;
+    const double s = D.xn[t] - D.x[t], y = D.gn[t] - D.g[t];
+    Sh[t] = s;
+    Yh[t] = y;
+    dn += D.gn[t] * s;
+    sy += s * y;
+    yy += y * y;
+  }
+  dn = bred<false>(dn, sh);
+  sy = bred<false>(sy, sh);
+  yy = bred<false>(yy, sh);
+  if (threadIdx.x == 0) {
+    D.part[5 * cf.nec + c] = dn;
+    D.part[6 * cf.nec + c] = sy;
+    D.part[7 * cf.nec + c] = yy;
+  }
+  A2C_ECHUNKS_END
+}
+
+// site-chunk partials of the energy and sigma-entropy sums
+__global__ void __launch_bounds__(kBlk) k_objpart(Dev D, Cfg cf, int all) {
+  __shared__ double sh[kBlk / 32];
+  for (int kk = blockIdx.x; kk < D.cnt[kCntSch]; kk += gridDim.x) {
+    const int c = D.ls[kk];
+    const Chunk ch = D.sch[c];
+    const Inst &I = D.st[ch.inst];
+    if (!all && I.state != kLineSearch && I.state != kNeedEval) continue;
+    double v = 0.0, s = 0.0;
+    for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+      v += D.Vs[ch.start + i];
+      s += D.Ss[ch.start + i];
+    }
+    v = bred<false>(v, sh);
+    s = bred<false>(s, sh);
+    if (threadIdx.x == 0) {
+      D.part[8 * cf.nec + c] = v;
+      D.part[8 * cf.nec + cf.nsc + c] = s;
+    }
+  }
+}
+
+// f = (1/T) sum V - 3 kB sum sigma  (minimizer.cpp:353)
+__device__ __forceinline__ double objective(const Dev &D, const Cfg &cf, int b, double *sh) {
+  const double sv = chunk_total(D.part + 8 * cf.nec, D.scb[b], D.scb[b + 1], sh);
+  const double ss = chunk_total(D.part + 8 * cf.nec + cf.nsc, D.scb[b], D.scb[b + 1], sh);
+  return 1.0 / D.geo[b].T * sv - 3.0 * kB * ss;
+}
+
+__global__ void __launch_bounds__(kBlk) k_objective(Dev D, Cfg cf, double *f) {
+  __shared__ double sh[kBlk / 32];
+  const int b = blockIdx.x;
+  const double v = objective(D, cf, b, sh);
+  if (threadIdx.x == 0) f[b] = v;
+}
+
+// The line-search decision (lbfgs.cu, one instance per block).
+__global__ void __launch_bounds__(kBlk) k_decide(Dev D, Cfg cf) {
+  __shared__ double sh[kBlk / 32];
+  const int b = blockIdx.x;
+  Inst &I = D.st[b];
+  if (I.state != kLineSearch && I.state != kNeedEval) return;
+  const double fn = objective(D, cf, b, sh);
+  const int e0 = D.ecb[b], e1 = D.ecb[b + 1];
+  const double dec = chunk_total(D.part + 4 * cf.nec, e0, e1, sh);
+  const double dn = chunk_total(D.part + 5 * cf.nec, e0, e1, sh);
+  const double sy = chunk_total(D.part + 6 * cf.nec, e0, e1, sh);
+  const double yy = chunk_total(D.part + 7 * cf.nec, e0, e1, sh);
+  if (threadIdx.x != 0) return;
+  I.fev += 1;
+  I.fn = fn;
+  if (I.state == kNeedEval) {
+    I.f = fn;
+    I.copy = 2;
+    I.nhist = 0;
+    I.state = kNeedDir;
+    return;
+  }
+  bool ok = isfinite(fn) && fn <= I.f + cf.c1 * dec;
+  if (!ok && isfinite(fn) && fabs(fn - I.f) <= I.f_noise * fabs(I.f)) ok = dn <= (2.0 * cf.c1 - 1.0) * dec;
+  if (ok) {
+    if (sy > 2.220446049250313e-16 * yy) {
+      D.rho[b * cf.ring + I.head] = 1.0 / sy;
+      I.gam_num = sy;
+      I.gam_den = yy;
+      I.head = (I.head + 1) % cf.ring;
+      if (I.npairs < cf.m) ++I.npairs;
+    }
+    I.copy = 1;
+    I.f = fn;
+    I.it += 1;
+    const int W = cf.W;
+    if (W > 0) {
+      double *h = D.fh + (size_t)b * (W + 1);
+      h[I.nhist % (W + 1)] = fn;
+      I.nhist += 1;
+      if (I.nhist > W && h[(I.nhist - 1 - W) % (W + 1)] - fn <= I.stall_rtol * fabs(fn)) {
+        end_phase(I, cf, A2C_CONVERGED_STALLED);
+        return;
+      }
+    }
+    I.state = kNeedDir;
+    return;
+  }
+  I.copy = 0;
+  I.alpha *= 0.5;
+  I.ls += 1;
+  if (I.fev >= cf.max_fev || I.ls >= cf.max_ls) {
+    if (I.npairs > 0 && I.fev < cf.max_fev) {
+      I.npairs = 0;
+      I.head = 0;
+      I.state = kNeedDir;
+    } else {
+      end_phase(I, cf, I.fev >= cf.max_fev ? A2C_DIVERGED_MAXFCN : A2C_DIVERGED_LS_FAILURE);
+    }
+  }
+}
+
+// accepted step: x <- xn, g <- gn; first evaluation of a phase: g <- gn
+__global__ void __launch_bounds__(kBlk) k_copy(Dev D, Cfg cf) {
+  A2C_ECHUNKS(D)
+  if (!I.copy) continue;
+  const bool both = I.copy == 1;
+  for (int i = threadIdx.x; i < ch.len; i += kBlk) {
+    const int64_t t = ch.start + i;
+    if (both) D.x[t] = D.xn[t];
+    D.g[t] = D.gn[t];
+  }
+  A2C_ECHUNKS_END
+}
+
+// ------------------------------------------------------------ CSR assembly
+__global__ void k_copy_csr(const int64_t *off, const uint32_t *nbr, const int *npd, int64_t n, int64_t total,
+                           int64_t start, int64_t base, int64_t *boff, uint32_t *bnbr, int *bnpd) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+    boff[start + s] = base + off[s];
+    bnpd[start + s] = npd[s];
+  }
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t e = nbr[t];
+    bnbr[base + t] = (uint32_t)((e & kIdMask) + (uint32_t)start) | (e & ~kIdMask);
+  }
+}
+
+__global__ void k_set_i64(int64_t *p, int64_t v) { *p = v; }
+
+}  // namespace
+}  // namespace a2c
+
+using namespace a2c;
+
+struct a2c_gpp_batch {
+  int B = 0;
+  int device = 0;
+  int precision = A2C_FP64;
+  int tps = 0;
+  bool graphs = true;
+  a2c_gpp_ctx *c = nullptr;  // the union system (evaluator buffers, lists, stream)
+  std::vector<a2c_gpp_params> P;
+  std::vector<int64_t> start;  // B + 1
+  std::vector<int> ecb, scb;   // B + 1
+  int64_t nec = 0, nsc = 0;
+  // device tables
+  InstGeo *geo = nullptr;
+  uint16_t *inst = nullptr;
+  Chunk *ech = nullptr, *sch = nullptr;
+  int *d_ecb = nullptr, *d_scb = nullptr;
+  int *lm = nullptr, *lf = nullptr, *le = nullptr, *ls = nullptr;
+  int *cnt = nullptr, *listed = nullptr, *loff = nullptr;
+  Inst *st = nullptr;
+  double *part = nullptr;
+  // L-BFGS buffers (allocated at the first minimization)
+  int m = 0, W = -1;
+  double *x = nullptr, *g = nullptr, *pg = nullptr, *d = nullptr, *xn = nullptr, *gn = nullptr;
+  double *S = nullptr, *Y = nullptr, *rho = nullptr, *alph = nullptr, *fh = nullptr;
+  int *h_cnt = nullptr;  // pinned
+  // the captured tick
+  cudaGraphExec_t exec = nullptr;
+  Cfg exec_cfg{};
+  int exec_tps = -1;
+  // statistics of the last minimization
+  int ticks = 0;
+  double seconds = 0.0;
+};
+
+namespace {
+
+template <class T>
+a2c_status dmalloc(T **p, int64_t n) {
+  *p = nullptr;
+  if (cudaMalloc((void **)p, sizeof(T) * (size_t)std::max<int64_t>(n, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
+  return A2C_OK;
+}
+
+void free_lbfgs(a2c_gpp_batch *b) {
+  for (double *p : {b->x, b->g, b->pg, b->d, b->xn, b->gn, b->S, b->Y, b->rho, b->alph, b->fh})
+    if (p) cudaFree(p);
+  b->x = b->g = b->pg = b->d = b->xn = b->gn = b->S = b->Y = b->rho = b->alph = b->fh = nullptr;
+  b->m = 0;
+  b->W = -1;
+}
+
+Dev dev_view(a2c_gpp_batch *b) {
+  Dev D{};
+  D.st = b->st;
+  D.geo = b->geo;
+  D.ech = b->ech;
+  D.sch = b->sch;
+  D.ecb = b->d_ecb;
+  D.scb = b->d_scb;
+  D.le = b->le;
+  D.ls = b->ls;
+  D.cnt = b->cnt;
+  D.x = b->x;
+  D.g = b->g;
+  D.pg = b->pg;
+  D.d = b->d;
+  D.xn = b->xn;
+  D.gn = b->gn;
+  D.S = b->S;
+  D.Y = b->Y;
+  D.part = b->part;
+  D.rho = b->rho;
+  D.alph = b->alph;
+  D.fh = b->fh;
+  D.Vs = b->c->d_Vs;
+  D.Ss = b->c->d_Ss;
+  return D;
+}
+
+BatchView view(a2c_gpp_batch *b, int which) {
+  BatchView v;
+  v.inst = b->inst;
+  v.geo = b->geo;
+  v.list = which == 0 ? b->lm : b->lf;
+  v.count = b->cnt + (which == 0 ? kCntMixed : kCntFp64);
+  return v;
+}
+
+int chunk_grid(int64_t nchunks) {
+  static int sms = 0;  // queried once, before any capture (the eager first tick)
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
+  }
+  return (int)std::max<int64_t>(1, std::min<int64_t>(nchunks, 8 * (int64_t)sms));
+}
+
+a2c_status plan(a2c_gpp_batch *b, const Dev &D) {
+  cudaStream_t s = b->c->stream;
+  k_plan<<<1, kPlanThreads, 0, s>>>(D, b->B, b->listed, b->loff);
+  k_fill<<<b->B, kBlk, 0, s>>>(D, b->B, b->loff, b->lm, b->lf, b->le, b->ls);
+  A2C_CUDA(cudaGetLastError());
+  return A2C_OK;
+}
+
+int default_tps(a2c_gpp_batch *b) { return b->tps ? b->tps : (b->c->N < 152 * 2048 ? 4 : 1); }
+
+// Evaluation of every listed site at xn into gn (both forms; a form with
+// an empty list costs an empty launch).
+a2c_status eval_lists(a2c_gpp_batch *b, const double *X, double *G, int tps) {
+  A2C_TRY(mixed_eval_list(b->c, X, G, view(b, 0), tps));
+  A2C_TRY(launch_eval64_list(b->c, X, G, view(b, 1)));
+  return A2C_OK;
+}
+
+// One tick (see the file comment); the same launches whether captured or not.
+a2c_status tick(a2c_gpp_batch *b, const Dev &D, const Cfg &cf, int tps) {
+  cudaStream_t s = b->c->stream;
+  const int ge = chunk_grid(cf.nec), gs = chunk_grid(cf.nsc), B = cf.B;
+  k_projgrad<<<ge, kBlk, 0, s>>>(D, cf);
+  k_dir_begin<<<B, kBlk, 0, s>>>(D, cf);
+  for (int j = 0; j < cf.m; ++j) {
+    k_loop1<<<ge, kBlk, 0, s>>>(D, cf, j);
+    k_loop1_fin<<<B, kBlk, 0, s>>>(D, cf, j);
+  }
+  k_scale<<<ge, kBlk, 0, s>>>(D, cf);
+  for (int j = 0; j < cf.m; ++j) {
+    k_loop2<<<ge, kBlk, 0, s>>>(D, cf, j);
+    k_loop2_fin<<<B, kBlk, 0, s>>>(D, cf, j);
+  }
+  k_finish<<<ge, kBlk, 0, s>>>(D, cf);
+  k_dir_end<<<B, kBlk, 0, s>>>(D, cf);
+  k_steep<<<ge, kBlk, 0, s>>>(D, cf);
+  A2C_TRY(plan(b, D));
+  k_trial<<<ge, kBlk, 0, s>>>(D, cf);
+  A2C_TRY(eval_lists(b, b->xn, b->gn, tps));
+  k_post<<<ge, kBlk, 0, s>>>(D, cf);
+  k_objpart<<<gs, kBlk, 0, s>>>(D, cf, 0);
+  k_decide<<<B, kBlk, 0, s>>>(D, cf);
+  k_copy<<<ge, kBlk, 0, s>>>(D, cf);
+  k_count_left<<<1, kBlk, 0, s>>>(D, B);
+  A2C_CUDA(cudaGetLastError());
+  return A2C_OK;
+}
+
+a2c_status ensure_lbfgs(a2c_gpp_batch *b, int m, int W) {
+  if (b->x && b->m == m && b->W == W) return A2C_OK;
+  free_lbfgs(b);
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  const int64_t n = 4 * b->c->N;
+  for (double **p : {&b->x, &b->g, &b->pg, &b->d, &b->xn, &b->gn}) A2C_TRY(dmalloc(p, n));
+  A2C_TRY(dmalloc(&b->S, n * (m + 1)));
+  A2C_TRY(dmalloc(&b->Y, n * (m + 1)));
+  A2C_TRY(dmalloc(&b->rho, (int64_t)b->B * (m + 1)));
+  A2C_TRY(dmalloc(&b->alph, (int64_t)b->B * (m + 1)));
+  A2C_TRY(dmalloc(&b->fh, (int64_t)b->B * (W + 1)));
+  A2C_CUDA(cudaMemset(b->rho, 0, sizeof(double) * b->B * (m + 1)));
+  A2C_CUDA(cudaMemset(b->alph, 0, sizeof(double) * b->B * (m + 1)));
+  b->m = m;
+  b->W = W;
+  return A2C_OK;
+}
+
+struct DeviceGuard {
+  explicit DeviceGuard(int d) { cudaSetDevice(d); }
+};
+
+bool same_common(const a2c_gpp_params &a, const a2c_gpp_params &b) {
+  if (a.QWp != b.QWp || a.eps != b.eps || a.rc != b.rc || a.a_Pd != b.a_Pd || a.precision != b.precision ||
+      a.device != b.device)
+    return false;
+  for (int k = 0; k < 4; ++k)
+    if (a.coe_Pd[k] != b.coe_Pd[k] || a.coe_H[k] != b.coe_H[k]) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+a2c_status a2c_gpp_batch_create(const a2c_gpp_params *params, int n, a2c_gpp_batch **out) {
+  if (!out) return A2C_ERR_INVALID;
+  *out = nullptr;
+  if (!params || n < 1 || n > 65535) return A2C_ERR_INVALID;
+  int64_t N = 0, nPd = 0, nH = 0;
+  for (int b = 0; b < n; ++b) {
+    const a2c_gpp_params &p = params[b];
+    if (!same_common(p, params[0]) || p.nPd < 0 || p.nH < 0 || (int64_t)p.nPd + p.nH < 1 || !(p.T > 0.0))
+      return A2C_ERR_INVALID;
+    for (int d = 0; d < 3; ++d)
+      if (p.periodic[d] && !(p.box[d] > 2.0 * p.rc)) return A2C_ERR_INVALID;
+    N += (int64_t)p.nPd + p.nH;
+    nPd += p.nPd;
+    nH += p.nH;
+  }
+  if (N >= (int64_t(1) << kIdBits) || N > INT32_MAX / 4) return A2C_ERR_INVALID;
+  a2c_gpp_params u = params[0];
+  u.nPd = (int)nPd;
+  u.nH = (int)nH;
+  a2c_gpp_batch *b = new (std::nothrow) a2c_gpp_batch();
+  if (!b) return A2C_ERR_NOMEM;
+  b->B = n;
+  b->device = u.device;
+  b->precision = u.precision;
+  b->P.assign(params, params + n);
+  a2c_status s = a2c_gpp_create(&u, &b->c);
+  if (s) {
+    delete b;
+    return s;
+  }
+  DeviceGuard dg(b->device);
+  // instance table and chunk tables
+  b->start.assign(n + 1, 0);
+  b->ecb.assign(n + 1, 0);
+  b->scb.assign(n + 1, 0);
+  std::vector<InstGeo> geo(n);
+  std::vector<Chunk> ech, sch;
+  std::vector<uint16_t> inst((size_t)N);
+  std::vector<double> occ((size_t)N, 0.0);
+  for (int k = 0; k < n; ++k) {
+    const a2c_gpp_params &p = params[k];
+    const int64_t s0 = b->start[k], nk = (int64_t)p.nPd + p.nH;
+    b->start[k + 1] = s0 + nk;
+    InstGeo &G = geo[k];
+    for (int d = 0; d < 3; ++d) {
+      G.S[d] = p.periodic[d] ? p.box[d] : 64.0;
+      G.sc[d] = (float)(G.S[d] / 4294967296.0);
+    }
+    G.T = p.T;
+    G.start = (int)s0;
+    G.nPd = p.nPd;
+    G.nH = p.nH;
+    for (int64_t i = 0; i < nk; ++i) inst[(size_t)(s0 + i)] = (uint16_t)k;
+    for (int64_t i = 0; i < p.nPd; ++i) occ[(size_t)(s0 + i)] = 1.0;
+    b->ecb[k] = (int)ech.size();
+    for (int64_t c0 = 0; c0 < 4 * nk; c0 += kChunk)
+      ech.push_back({4 * s0 + c0, (int)std::min<int64_t>(kChunk, 4 * nk - c0), k});
+    b->scb[k] = (int)sch.size();
+    for (int64_t c0 = 0; c0 < nk; c0 += kChunk) sch.push_back({s0 + c0, (int)std::min<int64_t>(kChunk, nk - c0), k});
+  }
+  b->ecb[n] = (int)ech.size();
+  b->scb[n] = (int)sch.size();
+  b->nec = (int64_t)ech.size();
+  b->nsc = (int64_t)sch.size();
+  s = A2C_OK;
+  if (!s) s = dmalloc(&b->geo, n);
+  if (!s) s = dmalloc(&b->inst, N);
+  if (!s) s = dmalloc(&b->ech, b->nec);
+  if (!s) s = dmalloc(&b->sch, b->nsc);
+  if (!s) s = dmalloc(&b->d_ecb, n + 1);
+  if (!s) s = dmalloc(&b->d_scb, n + 1);
+  if (!s) s = dmalloc(&b->lm, N);
+  if (!s) s = dmalloc(&b->lf, N);
+  if (!s) s = dmalloc(&b->le, b->nec);
+  if (!s) s = dmalloc(&b->ls, b->nsc);
+  if (!s) s = dmalloc(&b->cnt, 8);
+  if (!s) s = dmalloc(&b->listed, n);
+  if (!s) s = dmalloc(&b->loff, 6 * (int64_t)n);
+  if (!s) s = dmalloc(&b->st, n);
+  if (!s) s = dmalloc(&b->part, 8 * b->nec + 2 * b->nsc);
+  if (!s && cudaMallocHost((void **)&b->h_cnt, 8 * sizeof(int)) != cudaSuccess) s = A2C_ERR_NOMEM;
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    if (!s && bytes && cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) s = A2C_ERR_CUDA;
+  };
+  up(b->geo, geo.data(), sizeof(InstGeo) * n);
+  up(b->inst, inst.data(), sizeof(uint16_t) * N);
+  up(b->ech, ech.data(), sizeof(Chunk) * ech.size());
+  up(b->sch, sch.data(), sizeof(Chunk) * sch.size());
+  up(b->d_ecb, b->ecb.data(), sizeof(int) * (n + 1));
+  up(b->d_scb, b->scb.data(), sizeof(int) * (n + 1));
+  up(b->c->d_occ, occ.data(), sizeof(double) * N);
+  if (!s && cudaMemset(b->cnt, 0, 8 * sizeof(int)) != cudaSuccess) s = A2C_ERR_CUDA;
+  if (s) {
+    a2c_gpp_batch_destroy(b);
+    return s;
+  }
+  *out = b;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_batch_destroy(a2c_gpp_batch *b) {
+  if (!b) return A2C_OK;
+  DeviceGuard dg(b->device);
+  if (b->c && b->c->stream) cudaStreamSynchronize(b->c->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  free_lbfgs(b);
+  for (void *p : {(void *)b->geo, (void *)b->inst, (void *)b->ech, (void *)b->sch, (void *)b->d_ecb, (void *)b->d_scb,
+                  (void *)b->lm, (void *)b->lf, (void *)b->le, (void *)b->ls, (void *)b->cnt, (void *)b->listed,
+                  (void *)b->loff, (void *)b->st, (void *)b->part})
+    if (p) cudaFree(p);
+  if (b->h_cnt) cudaFreeHost(b->h_cnt);
+  a2c_gpp_destroy(b->c);
+  delete b;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_batch_info(a2c_gpp_batch *b, int *n_instances, int64_t *n_sites) {
+  if (!b) return A2C_ERR_INVALID;
+  if (n_instances) *n_instances = b->B;
+  if (n_sites) *n_sites = b->c->N;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_batch_set_occupancy(a2c_gpp_batch *b, const double *xH) {
+  if (!b || (!xH && b->c->p.nH > 0)) return A2C_ERR_INVALID;
+  DeviceGuard dg(b->device);
+  std::vector<double> occ((size_t)b->c->N, 1.0);
+  int64_t h = 0;
+  for (int k = 0; k < b->B; ++k)
+    for (int i = 0; i < b->P[k].nH; ++i) {
+      const double v = xH[h++];
+      if (!std::isfinite(v) || v < 0.0 || v > 1.0) return A2C_ERR_INVALID;
+      occ[(size_t)(b->start[k] + b->P[k].nPd + i)] = v;
+    }
+  A2C_CUDA(cudaMemcpy(b->c->d_occ, occ.data(), sizeof(double) * occ.size(), cudaMemcpyHostToDevice));
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_batch_build_neighbors(a2c_gpp_batch *b, const double *X, int *max_neighbors) {
+  if (!b || !X) return A2C_ERR_INVALID;
+  DeviceGuard dg(b->device);
+  a2c_gpp_ctx *c = b->c;
+  const int64_t N = c->N;
+  for (int64_t t = 0; t < 4 * N; ++t)
+    if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
+  if (b->exec) {  // the captured tick holds the list arrays' addresses
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  int64_t base = 0;
+  int maxn = 0;
+  for (int k = 0; k < b->B; ++k) {
+    a2c_gpp_params p = b->P[k];
+    p.precision = A2C_FP64;
+    a2c_gpp_ctx *t = nullptr;
+    A2C_TRY(a2c_gpp_create(&p, &t));
+    int mk = 0;
+    a2c_status s = a2c_gpp_build_neighbors(t, X + 4 * b->start[k], &mk);
+    const int64_t nk = t->N, tot = t->nbr_total;
+    if (!s && base + tot > c->nbr_cap) {  // grow, keeping what is there
+      const int64_t cap = std::max<int64_t>(base + tot, 2 * c->nbr_cap);
+      uint32_t *nn = nullptr;
+      if (cudaMalloc(&nn, sizeof(uint32_t) * (size_t)cap) != cudaSuccess) s = A2C_ERR_NOMEM;
+      if (!s && base > 0 && cudaMemcpy(nn, c->d_nbr, sizeof(uint32_t) * base, cudaMemcpyDeviceToDevice) != cudaSuccess)
+        s = A2C_ERR_CUDA;
+      if (!s) {
+        if (c->d_nbr) cudaFree(c->d_nbr);
+        c->d_nbr = nn;
+        c->nbr_cap = cap;
+      } else if (nn) {
+        cudaFree(nn);
+      }
+    }
+    if (!s) {
+      const int64_t w = std::max(nk, tot);
+      k_copy_csr<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((w + 255) / 256, 4096)), 256, 0, c->stream>>>(
+          t->d_off, t->d_nbr, t->d_npd, nk, tot, b->start[k], base, c->d_off, c->d_nbr, c->d_npd);
+      if (cudaStreamSynchronize(c->stream) != cudaSuccess) s = A2C_ERR_CUDA;
+    }
+    a2c_gpp_destroy(t);
+    A2C_TRY(s);
+    base += tot;
+    maxn = std::max(maxn, mk);
+  }
+  k_set_i64<<<1, 1, 0, c->stream>>>(c->d_off + N, base);
+  A2C_CUDA(cudaStreamSynchronize(c->stream));
+  c->nbr_total = base;
+  c->max_neighbors = maxn;
+  c->has_neighbors = true;
+  if (max_neighbors) *max_neighbors = maxn;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_batch_set_threads_per_site(a2c_gpp_batch *b, int tps) {
+  if (!b || (tps != 0 && tps != 1 && tps != 2 && tps != 4 && tps != 8)) return A2C_ERR_INVALID;
+  b->tps = tps;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_batch_set_graphs(a2c_gpp_batch *b, int on) {
+  if (!b) return A2C_ERR_INVALID;
+  b->graphs = on != 0;
+  return A2C_OK;
+}
+
+// Per-instance objective (f[B]) and gradient (G[4N]) at X (4N), every
+// instance in the batch's precision.
+a2c_status a2c_gpp_batch_eval(a2c_gpp_batch *b, const double *X, double *f, double *G) {
+  if (!b || !X || !f || !G) return A2C_ERR_INVALID;
+  a2c_gpp_ctx *c = b->c;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  DeviceGuard dg(b->device);
+  const int64_t N = c->N;
+  cudaStream_t s = c->stream;
+  double *df = nullptr;
+  A2C_TRY(dmalloc(&df, b->B));
+  Dev D = dev_view(b);
+  Cfg cf{};
+  cf.B = b->B;
+  cf.nec = b->nec;
+  cf.nsc = b->nsc;
+  cf.n = 4 * N;
+  cf.fn_mixed = cf.fn_fp64 = 0.0;
+  a2c_status st = A2C_OK;
+  const int phase = b->precision == A2C_MIXED ? kPhaseMixed : kPhaseFp64;
+  k_init_state<<<(b->B + 127) / 128, 128, 0, s>>>(D, cf, phase);
+  if (cudaMemsetAsync(b->listed, 0xff, sizeof(int) * b->B, s) != cudaSuccess) st = A2C_ERR_CUDA;  // -1: force a plan
+  if (!st && cudaMemsetAsync(c->d_status, 0, sizeof(int), s) != cudaSuccess) st = A2C_ERR_CUDA;
+  if (!st) st = plan(b, D);
+  if (!st && cudaMemcpyAsync(c->d_X, X, sizeof(double) * 4 * N, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    st = A2C_ERR_CUDA;
+  if (!st) st = eval_lists(b, c->d_X, c->d_G, default_tps(b));
+  if (!st) {
+    k_objpart<<<chunk_grid(b->nsc), kBlk, 0, s>>>(D, cf, 1);
+    k_objective<<<b->B, kBlk, 0, s>>>(D, cf, df);
+    if (cudaGetLastError() != cudaSuccess) st = A2C_ERR_CUDA;
+  }
+  if (!st && cudaMemcpyAsync(G, c->d_G, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    st = A2C_ERR_CUDA;
+  if (!st && cudaMemcpyAsync(f, df, sizeof(double) * b->B, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    st = A2C_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess && !st) st = A2C_ERR_CUDA;
+  cudaFree(df);
+  if (!st) {
+    c->has_state = true;
+    st = check_status_word(c);
+  }
+  return st;
+}
+
+// Minimizes every instance from X (4N, in/out).  Per instance: fmin, iters,
+// nfev, gnorm, reason (a2c_reason numbering), and, where not NULL,
+// mixed_iters / fp64_iters (the mixed phase and the FP64 polish).
+a2c_status a2c_gpp_batch_minimize(a2c_gpp_batch *b, double *X, const a2c_lbfgs_params *lp, double *fmin, int *iters,
+                                  int *nfev, double *gnorm, int *reason, int *mixed_iters, int *fp64_iters) {
+  if (!b || !X || !lp || !fmin || !iters || !nfev || !gnorm || !reason) return A2C_ERR_INVALID;
+  if (lp->m < 1 || lp->m > kMaxM || lp->max_ls < 1 || !(lp->sigma_lb > 0.0) || !(lp->init_step > 0.0) ||
+      lp->stall_window < 0 || lp->stall_window > 4096 || lp->max_fev < 1)
+    return A2C_ERR_INVALID;
+  a2c_gpp_ctx *c = b->c;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  DeviceGuard dg(b->device);
+  const int64_t N = c->N;
+  for (int64_t t = 0; t < 4 * N; ++t)
+    if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
+  A2C_TRY(ensure_lbfgs(b, lp->m, lp->stall_window));
+  cudaStream_t s = c->stream;
+  Cfg cf{};
+  cf.B = b->B;
+  cf.m = lp->m;
+  cf.ring = lp->m + 1;
+  cf.max_it = lp->max_it;
+  cf.max_fev = lp->max_fev;
+  cf.max_ls = lp->max_ls;
+  cf.polish = b->precision == A2C_MIXED ? lp->polish : 0;
+  cf.W = lp->stall_window;
+  cf.nec = b->nec;
+  cf.nsc = b->nsc;
+  cf.n = 4 * N;
+  cf.gatol = lp->gatol;
+  cf.c1 = lp->c1;
+  cf.init_step = lp->init_step;
+  cf.lb = lp->sigma_lb;
+  cf.fn_mixed = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-7;
+  cf.fn_fp64 = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-14;
+  cf.st_mixed = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-10;
+  cf.st_fp64 = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-14;
+  const int tps = default_tps(b);
+  if (b->precision == A2C_MIXED) A2C_TRY(mixed_prepare(c));
+  Dev D = dev_view(b);
+  cudaEvent_t e0, e1;
+  A2C_CUDA(cudaEventCreate(&e0));
+  A2C_CUDA(cudaEventCreate(&e1));
+  a2c_status st = A2C_OK;
+  auto fail = [&](a2c_status v) {
+    if (!st) st = v;
+  };
+  if (cudaMemcpyAsync(b->x, X, sizeof(double) * 4 * N, cudaMemcpyHostToDevice, s) != cudaSuccess) fail(A2C_ERR_CUDA);
+  cudaEventRecord(e0, s);
+  k_project_all<<<chunk_grid((4 * N + 255) / 256), 256, 0, s>>>(b->x, 4 * N, cf.lb);
+  k_init_state<<<(b->B + 127) / 128, 128, 0, s>>>(D, cf, b->precision == A2C_MIXED ? kPhaseMixed : kPhaseFp64);
+  if (cudaMemsetAsync(b->listed, 0xff, sizeof(int) * b->B, s) != cudaSuccess) fail(A2C_ERR_CUDA);
+  if (!st) fail(plan(b, D));
+  // the first tick (every instance's first evaluation) runs eagerly: it also
+  // performs the launchers' one-time occupancy queries outside any capture
+  if (!st) fail(tick(b, D, cf, tps));
+  // the captured tick, reused while the configuration is unchanged
+  const bool same = b->exec && b->exec_tps == tps && !std::memcmp(&b->exec_cfg, &cf, sizeof(Cfg));
+  if (!st && b->graphs && !same) {
+    if (b->exec) {
+      cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+    }
+    cudaGraph_t gr = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) fail(A2C_ERR_CUDA);
+    const a2c_status ts = st ? st : tick(b, D, cf, tps);
+    if (cudaStreamEndCapture(s, &gr) != cudaSuccess) fail(A2C_ERR_CUDA);
+    fail(ts);
+    if (!st && cudaGraphInstantiate(&b->exec, gr, 0) != cudaSuccess) fail(A2C_ERR_CUDA);
+    if (gr) cudaGraphDestroy(gr);
+    b->exec_cfg = cf;
+    b->exec_tps = tps;
+  }
+  // replay: K ticks, then read how many instances are left
+  const int K = 8;
+  const int64_t max_ticks = 2 * ((int64_t)lp->max_fev + 2) + 2 * K;
+  int64_t ticks = 1;
+  while (!st) {
+    for (int k = 0; k < K; ++k) {
+      if (b->graphs) {
+        if (cudaGraphLaunch(b->exec, s) != cudaSuccess) fail(A2C_ERR_CUDA);
+      } else {
+        fail(tick(b, D, cf, tps));
+      }
+    }
+    ticks += K;
+    if (cudaMemcpyAsync(b->h_cnt, b->cnt, 8 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      fail(A2C_ERR_CUDA);
+    if (st || b->h_cnt[kCntLeft] == 0) break;
+    if (ticks >= max_ticks) {
+      fail(A2C_ERR_STATE);
+      break;
+    }
+  }
+  cudaEventRecord(e1, s);
+  if (!st && cudaMemcpyAsync(X, b->x, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    fail(A2C_ERR_CUDA);
+  std::vector<Inst> hs((size_t)b->B);
+  if (!st && cudaMemcpyAsync(hs.data(), b->st, sizeof(Inst) * b->B, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    fail(A2C_ERR_CUDA);
+  if (cudaStreamSynchronize(s) != cudaSuccess) fail(A2C_ERR_CUDA);
+  float ms = 0.0f;
+  if (!st && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) b->seconds = 1e-3 * ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->ticks = (int)ticks;
+  // a trial point with a non-finite objective is rejected by the line
+  // search; it is not an error of the minimization
+  cudaMemsetAsync(c->d_status, 0, sizeof(int), s);
+  if (st) return st;
+  for (int k = 0; k < b->B; ++k) {
+    fmin[k] = hs[k].f;
+    iters[k] = hs[k].it;
+    nfev[k] = hs[k].fev;
+    gnorm[k] = hs[k].gnorm;
+    reason[k] = hs[k].why;
+    if (mixed_iters) mixed_iters[k] = hs[k].mixed_iters;
+    if (fp64_iters) fp64_iters[k] = hs[k].phase == kPhaseFp64 ? hs[k].fp64_iters : 0;
+  }
+  c->has_state = true;
+  return A2C_OK;
+}
+
+// Autotuner of the mixed form's threads per site over the whole batch at X
+// (every instance listed): each choice evaluates once untimed, then `reps`
+// times between two events; the fastest choice is kept for the batch.
+a2c_status a2c_gpp_batch_autotune(a2c_gpp_batch *b, const double *X, int reps, int *tps_out, float *ms) {
+  if (!b || !X || reps < 1 || reps > 1000) return A2C_ERR_INVALID;
+  a2c_gpp_ctx *c = b->c;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  DeviceGuard dg(b->device);
+  cudaStream_t s = c->stream;
+  A2C_TRY(mixed_prepare(c));
+  Dev D = dev_view(b);
+  Cfg cf{};
+  cf.B = b->B;
+  k_init_state<<<(b->B + 127) / 128, 128, 0, s>>>(D, cf, kPhaseMixed);
+  A2C_CUDA(cudaMemsetAsync(b->listed, 0xff, sizeof(int) * b->B, s));
+  A2C_TRY(plan(b, D));
+  A2C_CUDA(cudaMemcpyAsync(c->d_X, X, sizeof(double) * 4 * c->N, cudaMemcpyHostToDevice, s));
+  cudaEvent_t e0, e1;
+  A2C_CUDA(cudaEventCreate(&e0));
+  A2C_CUDA(cudaEventCreate(&e1));
+  const int choice[4] = {1, 2, 4, 8};
+  float best_ms = 0.0f;
+  int best = 0;
+  a2c_status st = A2C_OK;
+  for (int k = 0; k < 4 && !st; ++k) {
+    st = mixed_eval_list(c, c->d_X, c->d_G, view(b, 0), choice[k]);
+    if (!st && cudaEventRecord(e0, s) != cudaSuccess) st = A2C_ERR_CUDA;
+    for (int r = 0; r < reps && !st; ++r) st = mixed_eval_list(c, c->d_X, c->d_G, view(b, 0), choice[k]);
+    if (!st && cudaEventRecord(e1, s) != cudaSuccess) st = A2C_ERR_CUDA;
+    float t = 0.0f;
+    if (!st && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+      st = A2C_ERR_CUDA;
+    t /= (float)reps;
+    if (ms) ms[k] = t;
+    if (!st && (best == 0 || t < best_ms)) {
+      best_ms = t;
+      best = choice[k];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  b->tps = best;
+  if (tps_out) *tps_out = best;
+  return check_status_word(c);
+}
+
+// Ticks replayed and device seconds of the last a2c_gpp_batch_minimize.
+a2c_status a2c_gpp_batch_stats(a2c_gpp_batch *b, int *ticks, double *seconds) {
+  if (!b) return A2C_ERR_INVALID;
+  if (ticks) *ticks = b->ticks;
+  if (seconds) *seconds = b->seconds;
+  return A2C_OK;
+}
+
+}  // extern "C"

@@ -15,6 +15,26 @@ constexpr uint32_t kIdMask = (1u << kIdBits) - 1u;
 constexpr uint32_t kNoShift = 13u;
 constexpr double kB = 8.6173324e-5;  // minimizer.cpp:92
 
+// Batched instances (many independent lattices in one system): the sites
+// of instance b are [start, start + nPd + nH), Pd first, in the caller's
+// concatenated layout; neighbor lists never cross instances.
+struct InstGeo {
+  double S[3];   // periodic box length, or 64 A in a free direction
+  double T;      // temperature [K]
+  float sc[3];   // S / 2^32 (one fixed-point unit of the mixed form)
+  int start;     // first site
+  int nPd, nH;
+};
+
+// What a list-driven evaluator launch reads: the instance of every site,
+// the per-instance geometry, and the sites to evaluate (count on device).
+struct BatchView {
+  const uint16_t *inst = nullptr;
+  const InstGeo *geo = nullptr;
+  const int *list = nullptr;
+  const int *count = nullptr;
+};
+
 // Device pointers and scalars one FP64 kernel launch needs.
 struct SiteArgs {
   int nPd, nH;
@@ -31,6 +51,7 @@ struct SiteArgs {
   double *Vs;           // N: per-site energy partial
   double *Ss;           // N: per-site sigma-entropy partial
   int *status;          // device status word (0 = ok)
+  BatchView bv;         // list-driven batched launch when bv.list != nullptr
 };
 
 // Device status bits (a2c never traps; kernels record and return).
@@ -92,6 +113,8 @@ a2c_status launch_density64(a2c_gpp_ctx *c, const double *dX);
 a2c_status launch_gradient64(a2c_gpp_ctx *c, const double *dX, double *dG);
 a2c_status launch_eam64(a2c_gpp_ctx *c, int which, const double *d_in, int64_t n, double *d_out);
 a2c_status launch_chem64(a2c_gpp_ctx *c, const double *dX, double gamma_bd, double *d_send, const int *d_full);
+// batched: both passes over the listed sites (persistent grids; G, Vs, Ss)
+a2c_status launch_eval64_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv);
 
 // k_misc.cu
 a2c_status reduce_objective(a2c_gpp_ctx *c, double *d_f);        // f from Vs, Ss
@@ -115,6 +138,9 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
 void mixed_free(a2c_gpp_ctx *c);
 a2c_status mixed_set_threads_per_site(a2c_gpp_ctx *c, int tps);
 int mixed_threads_per_site(a2c_gpp_ctx *c);
+// batched: prep + both passes over the listed sites (G, Vs, Ss; no objective)
+a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, int tps);
+a2c_status mixed_prepare(a2c_gpp_ctx *c);  // tables and buffers, before any graph capture
 
 // lbfgs.cu
 a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp, double *fmin, int *iters,

@@ -11,6 +11,8 @@
 // r = ((q_i + u_i*xi0) - q_j) - u_j*xi1 with u = sqrt(2)*sigma; adding or
 // subtracting an exact zero leaves a value unchanged, so the component-wise
 // forms used below are bit-identical to it.
+#include <algorithm>
+
 #include "eam64.cuh"
 #include "internal.cuh"
 
@@ -26,7 +28,7 @@ struct PairGeo {
   double D2[3];     // D[c]^2
 };
 
-__device__ __forceinline__ void image_pos(const SiteArgs &a, uint32_t e, double q[3]) {
+__device__ __forceinline__ void image_pos(const SiteArgs &a, const double *box, uint32_t e, double q[3]) {
   const int64_t j = e & kIdMask;
   q[0] = a.X[4 * j];
   q[1] = a.X[4 * j + 1];
@@ -34,9 +36,9 @@ __device__ __forceinline__ void image_pos(const SiteArgs &a, uint32_t e, double 
   const uint32_t c = e >> kIdBits;
   if (c != kNoShift) {
     const int m0 = (int)(c % 3u) - 1, m1 = (int)((c / 3u) % 3u) - 1, m2 = (int)(c / 9u) - 1;
-    if (m0) q[0] = q[0] + m0 * a.box[0];
-    if (m1) q[1] = q[1] + m1 * a.box[1];
-    if (m2) q[2] = q[2] + m2 * a.box[2];
+    if (m0) q[0] = q[0] + m0 * box[0];
+    if (m1) q[1] = q[1] + m1 * box[1];
+    if (m2) q[2] = q[2] + m2 * box[2];
   }
 }
 
@@ -89,10 +91,8 @@ __device__ __forceinline__ void accum(double Fq[3], double &Fs, double c, const 
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_density64(SiteArgs a) {
-  const int64_t N = (int64_t)a.nPd + a.nH;
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= N) return;
+// Pass 1 for site s (electrondensity.cpp:20-49).
+__device__ __forceinline__ void density_site(const SiteArgs &a, int64_t s, bool iPd, const double *box) {
   const double qi[3] = {a.X[4 * s], a.X[4 * s + 1], a.X[4 * s + 2]};
   const double ui = (1.4142135623730951 * a.X[4 * s + 3]) * 1.7320508075688772;
   const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kBlock) k_density64(SiteArgs a) {
     const uint32_t en = a.nbr[t];
     const int64_t j = en & kIdMask;
     double qj[3];
-    image_pos(a, en, qj);
+    image_pos(a, box, en, qj);
     const double uj = (1.4142135623730951 * a.X[4 * j + 3]) * 1.7320508075688772;
     PairGeo g;
     make_geo(qi, ui, qj, uj, g);
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kBlock) k_density64(SiteArgs a) {
     const uint32_t en = a.nbr[t];
     const int64_t j = en & kIdMask;
     double qj[3];
-    image_pos(a, en, qj);
+    image_pos(a, box, en, qj);
     const double uj = (1.4142135623730951 * a.X[4 * j + 3]) * 1.7320508075688772;
     const double xj = a.occ[j];
     PairGeo g;
@@ -132,8 +132,15 @@ __global__ void __launch_bounds__(kBlock) k_density64(SiteArgs a) {
     }
   }
   a.rho[s] = rho;
-  a.Fp[s] = (s < a.nPd) ? eam64::F_Pd_d(rho, a.eps) : eam64::F_H_d(rho, a.eps);
+  a.Fp[s] = iPd ? eam64::F_Pd_d(rho, a.eps) : eam64::F_H_d(rho, a.eps);
   if (!isfinite(rho)) atomicOr(a.status, kStatusNonfinite);
+}
+
+__global__ void __launch_bounds__(kBlock) k_density64(SiteArgs a) {
+  const int64_t N = (int64_t)a.nPd + a.nH;
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  density_site(a, s, s < a.nPd, a.box);
 }
 
 // Pass 2.  Per pair-point the three gradient terms of minimizer.cpp:180-190
@@ -143,11 +150,7 @@ __global__ void __launch_bounds__(kBlock) k_density64(SiteArgs a) {
 //   c3 = ((x_j*W)*phi'_AB(s))/s
 // and the energy term ((0.5*x_i)*x_j)*W*phi_AB(s); the factors equal to 1
 // for Pd sites multiply exactly, so one form serves all four pair types.
-__global__ void __launch_bounds__(kBlock) k_gradient64(SiteArgs a) {
-  const int64_t N = (int64_t)a.nPd + a.nH;
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= N) return;
-  const bool iPd = s < a.nPd;
+__device__ __forceinline__ void gradient_site(const SiteArgs &a, int64_t s, bool iPd, const double *box, double T) {
   const double qi[3] = {a.X[4 * s], a.X[4 * s + 1], a.X[4 * s + 2]};
   const double sigmai = a.X[4 * s + 3];
   const double ui = (1.4142135623730951 * sigmai) * 1.7320508075688772;
@@ -166,7 +169,7 @@ __global__ void __launch_bounds__(kBlock) k_gradient64(SiteArgs a) {
     const uint32_t en = a.nbr[t];
     const int64_t j = en & kIdMask;
     double qj[3];
-    image_pos(a, en, qj);
+    image_pos(a, box, en, qj);
     const double uj = (1.4142135623730951 * a.X[4 * j + 3]) * 1.7320508075688772;
     const double Fpj = a.Fp[j];
     PairGeo g;
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(kBlock) k_gradient64(SiteArgs a) {
     const uint32_t en = a.nbr[t];
     const int64_t j = en & kIdMask;
     double qj[3];
-    image_pos(a, en, qj);
+    image_pos(a, box, en, qj);
     const double uj = (1.4142135623730951 * a.X[4 * j + 3]) * 1.7320508075688772;
     const double Fpj = a.Fp[j];
     const double xj = a.occ[j];
@@ -222,8 +225,8 @@ __global__ void __launch_bounds__(kBlock) k_gradient64(SiteArgs a) {
     }
   }
   // minimizer.cpp:220-223 and 282-285
-  const double cq = (1.0 / a.T) * xi;
-  const double cs = ((1.0 / a.T) * 1.4142135623730951) * xi;
+  const double cq = (1.0 / T) * xi;
+  const double cs = ((1.0 / T) * 1.4142135623730951) * xi;
   const double ce = ((3.0 * kB) / sigmai) * xi;
   a.G[4 * s] = Fq[0] * cq;
   a.G[4 * s + 1] = Fq[1] * cq;
@@ -232,6 +235,34 @@ __global__ void __launch_bounds__(kBlock) k_gradient64(SiteArgs a) {
   a.Vs[s] = V;
   a.Ss[s] = dd::cr_log(sigmai) * xi;
   if (!isfinite(V) || !isfinite(Fs) || !isfinite(Fq[0] + Fq[1] + Fq[2])) atomicOr(a.status, kStatusNonfinite);
+}
+
+__global__ void __launch_bounds__(kBlock) k_gradient64(SiteArgs a) {
+  const int64_t N = (int64_t)a.nPd + a.nH;
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  gradient_site(a, s, s < a.nPd, a.box, a.T);
+}
+
+// Batched: the listed sites, each with its instance's box, T and species.
+// Persistent grids (a fixed launch serves any list length, so the launch
+// can live in a CUDA graph while the list shrinks).
+__global__ void __launch_bounds__(kBlock) k_density64_list(SiteArgs a) {
+  const int n = *a.bv.count;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t s = a.bv.list[k];
+    const InstGeo &g = a.bv.geo[a.bv.inst[s]];
+    density_site(a, s, s - g.start < g.nPd, g.S);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_gradient64_list(SiteArgs a) {
+  const int n = *a.bv.count;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t s = a.bv.list[k];
+    const InstGeo &g = a.bv.geo[a.bv.inst[s]];
+    gradient_site(a, s, s - g.start < g.nPd, g.S, g.T);
+  }
 }
 
 // Occupancy gradient, minimizer.cpp:658-789, one thread per H site.  d_send
@@ -248,6 +279,7 @@ __global__ void __launch_bounds__(kBlock) k_chem64(SiteArgs a, const double coeP
   const double qi[3] = {a.X[4 * s], a.X[4 * s + 1], a.X[4 * s + 2]};
   const double ui = (1.4142135623730951 * a.X[4 * s + 3]) * 1.7320508075688772;
   const double W = a.W, T = a.T, eps = a.eps;
+  const double *box = a.box;
   const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
   const double nHPd = (double)(m - b);
   double sum = 0.0;
@@ -263,7 +295,7 @@ __global__ void __launch_bounds__(kBlock) k_chem64(SiteArgs a, const double coeP
     const uint32_t en = a.nbr[t];
     const int64_t j = en & kIdMask;
     double qj[3];
-    image_pos(a, en, qj);
+    image_pos(a, box, en, qj);
     const double uj = (1.4142135623730951 * a.X[4 * j + 3]) * 1.7320508075688772;
     const double WF = W * a.Fp[j];
     PairGeo g;
@@ -284,7 +316,7 @@ __global__ void __launch_bounds__(kBlock) k_chem64(SiteArgs a, const double coeP
     const uint32_t en = a.nbr[t];
     const int64_t j = en & kIdMask;
     double qj[3];
-    image_pos(a, en, qj);
+    image_pos(a, box, en, qj);
     const double uj = (1.4142135623730951 * a.X[4 * j + 3]) * 1.7320508075688772;
     const double xj = a.occ[j];
     const double xWF = (xj * W) * a.Fp[j];
@@ -368,6 +400,28 @@ a2c_status launch_gradient64(a2c_gpp_ctx *c, const double *dX, double *dG) {
   SiteArgs a = site_args(c, dX);
   a.G = dG;
   k_gradient64<<<grid_for(c->N, kBlock), kBlock, 0, c->stream>>>(a);
+  A2C_CUDA(cudaGetLastError());
+  return A2C_OK;
+}
+
+a2c_status launch_eval64_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv) {
+  static int cap[2] = {0, 0};
+  if (!cap[0]) {
+    int dev = 0, sms = 0, b0 = 0, b1 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_density64_list, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_gradient64_list, kBlock, 0);
+    cap[0] = std::max(1, sms * b0);
+    cap[1] = std::max(1, sms * b1);
+  }
+  if (c->N == 0) return A2C_OK;
+  SiteArgs a = site_args(c, dX);
+  a.G = dG;
+  a.bv = bv;
+  const int64_t need = (c->N + kBlock - 1) / kBlock;
+  k_density64_list<<<(unsigned)std::min<int64_t>(need, cap[0]), kBlock, 0, c->stream>>>(a);
+  k_gradient64_list<<<(unsigned)std::min<int64_t>(need, cap[1]), kBlock, 0, c->stream>>>(a);
   A2C_CUDA(cudaGetLastError());
   return A2C_OK;
 }

@@ -76,6 +76,7 @@ struct MixArgs {
   float2 *FF;
   double *G, *Vs, *Ss;
   double T;
+  BatchView bv;  // batched list launch (LIST kernels)
 };
 
 __device__ __forceinline__ float ex2(float x) {
@@ -95,10 +96,36 @@ __device__ __forceinline__ void kahan(float &s, float &c, float v) {
   s = t;
 }
 
-__device__ __forceinline__ float3 pair_vec(const MixArgs &a, int4 pi, int4 pj) {  // q_i - q_j
-  return make_float3((float)(int)((unsigned)pi.x - (unsigned)pj.x) * a.sc[0],
-                     (float)(int)((unsigned)pi.y - (unsigned)pj.y) * a.sc[1],
-                     (float)(int)((unsigned)pi.z - (unsigned)pj.z) * a.sc[2]);
+__device__ __forceinline__ float3 pair_vec(float3 sc, int4 pi, int4 pj) {  // q_i - q_j
+  return make_float3((float)(int)((unsigned)pi.x - (unsigned)pj.x) * sc.x,
+                     (float)(int)((unsigned)pi.y - (unsigned)pj.y) * sc.y,
+                     (float)(int)((unsigned)pi.z - (unsigned)pj.z) * sc.z);
+}
+
+// The site handled by work item k and what it needs from its instance.
+template <bool LIST>
+struct SiteRef {
+  int64_t s;
+  bool iPd;
+  float3 sc;
+  double T;
+};
+template <bool LIST>
+__device__ __forceinline__ SiteRef<LIST> site_ref(const MixArgs &a, int64_t k) {
+  SiteRef<LIST> r;
+  if (LIST) {
+    r.s = a.bv.list[k];
+    const InstGeo &g = a.bv.geo[a.bv.inst[r.s]];
+    r.iPd = r.s - g.start < g.nPd;
+    r.sc = make_float3(g.sc[0], g.sc[1], g.sc[2]);
+    r.T = g.T;
+  } else {
+    r.s = k;
+    r.iPd = k < a.nPd;
+    r.sc = make_float3(a.sc[0], a.sc[1], a.sc[2]);
+    r.T = a.T;
+  }
+  return r;
 }
 
 __device__ __forceinline__ float hv(float4 c, float t) { return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x); }
@@ -188,24 +215,29 @@ __device__ __forceinline__ void walk_neighbors(const MixArgs &a, int64_t begin, 
 }
 
 // ---------------------------------------------------------------- pass 1
-template <int TPS>
+template <int TPS, bool LIST>
 __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
+  constexpr int kSitesPerBlock = kBlock / TPS;
+  const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
+  if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
   __shared__ float4 sF[kTabN];
   for (int i = threadIdx.x; i < kTabN; i += blockDim.x) sF[i] = __ldg(&a.tabPair[i]);
   __syncthreads();
-  constexpr int kSitesPerBlock = kBlock / TPS;
-  for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < a.N;
+  for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < n;
        base += (int64_t)gridDim.x * kSitesPerBlock) {
-  const int64_t s = base + threadIdx.x / TPS;
+  const int64_t k = base + threadIdx.x / TPS;
   const int lane = (int)(threadIdx.x % TPS);
-  const bool live = s < a.N;
+  const bool live = k < n;
+  SiteRef<LIST> R{};
+  if (live) R = site_ref<LIST>(a, k);
+  const int64_t s = R.s;
   float acc = 0.0f, cmp = 0.0f;
   if (live) {
     const int4 pi = a.P[s];
     const float ui = kSqrt6 * __int_as_float(pi.w), ui2 = ui * ui;
     const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
     walk_neighbors<false, false>(a, b + lane, m, TPS, [&](int4 pj, float, float) {  // Pd neighbors: f_Pd
-      const float3 D = pair_vec(a, pi, pj);
+      const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
       const float Ai = D2 + ui2, Aj = fmaf(uj, uj, D2);
@@ -225,7 +257,7 @@ __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
       kahan(acc, cmp, part);
     });
     walk_neighbors<true, false>(a, m + lane, e, TPS, [&](int4 pj, float xj, float) {  // H neighbors: x_j f_H
-      const float3 D = pair_vec(a, pi, pj);
+      const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
       const float Ai = D2 + ui2, Aj = fmaf(uj, uj, D2);
@@ -245,7 +277,7 @@ __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
   for (int o = TPS / 2; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
   if (live && lane == 0) {
     const float rho = tot * a.W;
-    const bool iPd = s < a.nPd;
+    const bool iPd = R.iPd;
     float x = fminf(fmaxf(rho * (float)kEmbInvH, 0.0f), (float)kEmbN - 0.5f);
     const int i = (int)x;
     const float tt = x - (float)i;
@@ -325,20 +357,25 @@ __device__ __forceinline__ void add_pair(SiteAcc &A, const PairAcc &p, float3 D,
   kahan(A.s[4], A.c[4], vx * p.v);
 }
 
-template <int TPS>
+template <int TPS, bool LIST>
 __global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
+  constexpr int kSitesPerBlock = kBlock / TPS;
+  const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
+  if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
   __shared__ float4 sF[kTabN], sP[kTabN];
   for (int i = threadIdx.x; i < kTabN; i += blockDim.x) {
     sF[i] = __ldg(&a.tabPair[i]);
     sP[i] = __ldg(&a.tabPair[kTabN + i]);
   }
   __syncthreads();
-  constexpr int kSitesPerBlock = kBlock / TPS;
-  for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < a.N;
+  for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < n;
        base += (int64_t)gridDim.x * kSitesPerBlock) {
-  const int64_t s = base + threadIdx.x / TPS;
+  const int64_t k = base + threadIdx.x / TPS;
   const int lane = (int)(threadIdx.x % TPS);
-  const bool live = s < a.N;
+  const bool live = k < n;
+  SiteRef<LIST> R{};
+  if (live) R = site_ref<LIST>(a, k);
+  const int64_t s = R.s;
   SiteAcc A;
 #pragma unroll
   for (int k = 0; k < 5; ++k) A.s[k] = A.c[k] = 0.0f;
@@ -350,11 +387,11 @@ __global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
     const float ui = kSqrt6 * sigi;
     xi = a.occ[s];
     ffi = a.FF[s];
-    const bool iPd = s < a.nPd;
+    const bool iPd = R.iPd;
     const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
     const float hw = 0.5f * a.W * xi;
     walk_neighbors<false, true>(a, b + lane, m, TPS, [&](int4 pj, float, float Fb) {  // Pd neighbors
-      const float3 D = pair_vec(a, pi, pj);
+      const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       PairAcc p;
       if (iPd) pair_terms<0>(sF, sP, ffi.x, Fb, D, ui, uj, p);
@@ -362,7 +399,7 @@ __global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
       add_pair(A, p, D, a.W, hw);
     });
     walk_neighbors<true, true>(a, m + lane, e, TPS, [&](int4 pj, float xj, float Fb) {  // H neighbors
-      const float3 D = pair_vec(a, pi, pj);
+      const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       PairAcc p;
       if (iPd) pair_terms<1>(sF, sP, ffi.x, Fb, D, ui, uj, p);
@@ -379,7 +416,7 @@ __global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
     tot[k] = (double)v;
   }
   if (live && lane == 0) {
-    const double x = xi, sg = sigi, invT = 1.0 / a.T;
+    const double x = xi, sg = sigi, invT = 1.0 / R.T;
     a.G[4 * s] = tot[0] * (invT * x);
     a.G[4 * s + 1] = tot[1] * (invT * x);
     a.G[4 * s + 2] = tot[2] * (invT * x);
@@ -401,24 +438,39 @@ __global__ void k_prep(const double *X, const double *occ, int64_t N, double k0,
   occf[s] = (float)occ[s];
 }
 
+// Batched: positions of the listed sites with their instance's scale.
+__global__ void k_prep_list(const double *X, const double *occ, BatchView bv, int4 *P, float *occf) {
+  const int n = *bv.count;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t s = bv.list[k];
+    const InstGeo &g = bv.geo[bv.inst[s]];
+    const long long u0 = __double2ll_rn(X[4 * s] * (4294967296.0 / g.S[0]));
+    const long long u1 = __double2ll_rn(X[4 * s + 1] * (4294967296.0 / g.S[1]));
+    const long long u2 = __double2ll_rn(X[4 * s + 2] * (4294967296.0 / g.S[2]));
+    P[s] = make_int4((int)(unsigned)u0, (int)(unsigned)u1, (int)(unsigned)u2, __float_as_int((float)X[4 * s + 3]));
+    occf[s] = (float)occ[s];
+  }
+}
+
 // Persistent grids: as many blocks as fit on the device at once (occupancy
-// query, cached per kernel), capped by the work.
-template <int TPS>
+// query, cached per kernel), capped by the work (for a list launch, by the
+// largest list the system can have).
+template <int TPS, bool LIST>
 void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev) {
   static int cap[2] = {0, 0};
   if (!cap[0]) {
     int dev = 0, sms = 0, b0 = 0, b1 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_rho_mixed<TPS>, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_grad_mixed<TPS>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_rho_mixed<TPS, LIST>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_grad_mixed<TPS, LIST>, kBlock, 0);
     cap[0] = std::max(1, sms * b0);
     cap[1] = std::max(1, sms * b1);
   }
   const int64_t need = (a.N * TPS + kBlock - 1) / kBlock;
-  k_rho_mixed<TPS><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[0])), kBlock, 0, st>>>(a);
+  k_rho_mixed<TPS, LIST><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[0])), kBlock, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
-  k_grad_mixed<TPS><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[1])), kBlock, 0, st>>>(a);
+  k_grad_mixed<TPS, LIST><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[1])), kBlock, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[3], st);
 }
 
@@ -504,10 +556,10 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
     if (ev) cudaEventRecord(ev[1], c->stream);
     int tps = M->tps ? M->tps : (N < 152 * 2048 ? 4 : 1);
     switch (tps) {
-      case 1: launch_pair_kernels<1>(a, c->stream, ev); break;
-      case 2: launch_pair_kernels<2>(a, c->stream, ev); break;
-      case 4: launch_pair_kernels<4>(a, c->stream, ev); break;
-      default: launch_pair_kernels<8>(a, c->stream, ev); break;
+      case 1: launch_pair_kernels<1, false>(a, c->stream, ev); break;
+      case 2: launch_pair_kernels<2, false>(a, c->stream, ev); break;
+      case 4: launch_pair_kernels<4, false>(a, c->stream, ev); break;
+      default: launch_pair_kernels<8, false>(a, c->stream, ev); break;
     }
     A2C_CUDA(cudaGetLastError());
   } else if (ev) {
@@ -515,6 +567,47 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   }
   A2C_TRY(reduce_objective(c, d_f));
   if (ev) cudaEventRecord(ev[4], c->stream);
+  return A2C_OK;
+}
+
+a2c_status mixed_prepare(a2c_gpp_ctx *c) { return ensure_mixed(c); }
+
+a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, int tps) {
+  A2C_TRY(ensure_mixed(c));
+  Mixed *M = c->mixed;
+  const int64_t N = c->N;
+  if (N == 0) return A2C_OK;
+  MixArgs a{};
+  a.N = N;  // upper bound of the list length (sizes the persistent grids)
+  a.W = (float)c->p.QWp;
+  a.P = M->P;
+  a.occ = M->occ;
+  a.off = c->d_off;
+  a.nbr = c->d_nbr;
+  a.npd = c->d_npd;
+  a.tabPair = M->tabPair;
+  a.tabEmb = M->tabEmb;
+  a.FF = M->FF;
+  a.G = dG;
+  a.Vs = c->d_Vs;
+  a.Ss = c->d_Ss;
+  a.bv = bv;
+  static int prep_cap = 0;
+  if (!prep_cap) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    prep_cap = 8 * sms;
+  }
+  k_prep_list<<<(unsigned)std::min<int64_t>(grid_for(N, 256), prep_cap), 256, 0, c->stream>>>(dX, c->d_occ, bv, M->P,
+                                                                                               M->occ);
+  switch (tps) {
+    case 1: launch_pair_kernels<1, true>(a, c->stream, nullptr); break;
+    case 2: launch_pair_kernels<2, true>(a, c->stream, nullptr); break;
+    case 4: launch_pair_kernels<4, true>(a, c->stream, nullptr); break;
+    default: launch_pair_kernels<8, true>(a, c->stream, nullptr); break;
+  }
+  A2C_CUDA(cudaGetLastError());
   return A2C_OK;
 }
 
@@ -682,10 +775,10 @@ extern "C" a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *c, const double *d
                                                      (float *)(base + kNaOcc));
     const int tps = (c->mixed && c->mixed->tps) ? c->mixed->tps : (N < 152 * 2048 ? 4 : 1);
     switch (tps) {
-      case 1: launch_pair_kernels<1>(a, c->stream, nullptr); break;
-      case 2: launch_pair_kernels<2>(a, c->stream, nullptr); break;
-      case 4: launch_pair_kernels<4>(a, c->stream, nullptr); break;
-      default: launch_pair_kernels<8>(a, c->stream, nullptr); break;
+      case 1: launch_pair_kernels<1, false>(a, c->stream, nullptr); break;
+      case 2: launch_pair_kernels<2, false>(a, c->stream, nullptr); break;
+      case 4: launch_pair_kernels<4, false>(a, c->stream, nullptr); break;
+      default: launch_pair_kernels<8, false>(a, c->stream, nullptr); break;
     }
   }
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(kNaRedGrid, (N + kNaRedBlock - 1) / kNaRedBlock));

@@ -220,6 +220,182 @@ def time_to_minimum(cells: int, gatol: float, device: int):
     return out
 
 
+def dmd_slab(cells_xy: int, cells_z: int, seed: int = 5):
+    """The coupled-DMD workload: fcc Pd + octahedral H, periodic in x and y,
+    free surfaces in z, x = 0.01 everywhere, N(0, 0.02 A) positions, sigma =
+    0.10 A; the H sites of the z = 0 layer are the Dirichlet sites."""
+    import numpy as np
+
+    import a2c_gb300 as A
+
+    X, xH, surf, box, nPd, nH = A.lattice_fcc((cells_xy, cells_xy, cells_z), periodic=(1, 1, 0), pos_std=0.02,
+                                             sigma=(0.1, 0.1), x_center=0.01, x_half=0.0, seed=seed)
+    return X, xH, np.nonzero(surf)[0].astype(np.int32), box, nPd, nH
+
+
+def dirichlet_gamma(T: float, x_bd: float, device: int) -> float:
+    """gamma_bd: the mean chemical potential (gamma, with its +1.5 offset) of
+    a periodic 4x4x4-cell crystal held at x = x_bd after minimization -- the
+    value a bulk region at the Dirichlet occupancy has."""
+    import numpy as np
+
+    import a2c_gb300 as A
+
+    X, xH, _, box, nPd, nH = A.lattice_fcc(4, periodic=(1, 1, 1), pos_std=0.0, sigma=(0.1, 0.1), x_center=x_bd,
+                                           x_half=0.0, seed=1)
+    with A.Gpp(nPd, nH, T=T, box=box, periodic=(1, 1, 1), device=device) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        r = g.minimize(X, gatol=1e-6)
+        gam, _ = g.chem_potential(1e300, np.zeros(nH), np.zeros(nH, dtype=np.int32))
+    return float(np.mean(gam))
+
+
+def depth_profile(X, xH, nPd: int, a: float = 3.89):
+    """Mean H occupancy per z-layer of octahedral sites (spacing a/2); X is
+    the lattice state the layers are read from (the initial one: relaxed
+    subsurface sites can move by more than a/4)."""
+    import numpy as np
+
+    z = X.reshape(-1, 4)[nPd:, 2]
+    layer = np.rint(z / (0.5 * a)).astype(np.int64)
+    layer -= layer.min()
+    cnt = np.bincount(layer)
+    return np.bincount(layer, weights=xH) / np.maximum(cnt, 1)
+
+
+def run_dmd_case(args):
+    """Coupled diffusive MD: `--dmd-steps` outer steps (minimization to
+    gatol 1e-5 in the mixed form -- FP32 quadrature, FP64 L-BFGS, rates and
+    occupancy update -- then one diffusion step) on a cells x cells x cells
+    slab, T = 400 K, Dirichlet x = 0.80 on the z = 0 H layer, nu = 1e13 /s,
+    Qm = 0.23 eV, dt = 1e-12 s (12 nu exp(-Qm/kT) dt = 0.15).  Reported: wall
+    time per outer step, total H per step and the final depth profile; then
+    the same protocol on a reduced 8x8x12-cell slab in FP64 and mixed, whose
+    FP64 loop is bit-identical to the oracle's."""
+    import numpy as np
+
+    import a2c_gb300 as A
+
+    dev = dist_env()[2]
+    T, x_bd = 400.0, 0.80
+    dmd = dict(dt=1e-12, nu=1e13, Qm=0.23, x_bd=x_bd, xLb=1e-3, xUb=1 - 1e-16)
+    gbd = dirichlet_gamma(T, x_bd, dev)
+    out = {"case": "coupled DMD", "T": T, "x_bd": x_bd, "gamma_bd": gbd, **{k: v for k, v in dmd.items()}}
+
+    def run(cells_xy, cells_z, prec, steps):
+        X, xH, bd, box, nPd, nH = dmd_slab(cells_xy, cells_z)
+        with A.Gpp(nPd, nH, T=T, box=box, periodic=(1, 1, 0), precision=prec, device=dev) as g:
+            g.set_occupancy(xH)
+            g.build_neighbors(X)
+            g.eval(X)  # lazy set-up outside the timed region
+            g.synchronize()
+            t0 = time.perf_counter()
+            r = g.dmd_run(X, xH, np.zeros(nH), np.zeros(nH, dtype=np.int32), bd, bd, steps, gamma_bd=gbd,
+                          gatol=1e-5, max_it=2000, polish=0, **dmd)
+            dt = time.perf_counter() - t0
+        return r, dt, nPd + nH, depth_profile(X, r["xH"], nPd)
+
+    c = args.dmd_cells
+    r, dt, n, prof = run(c, c, "mixed", args.dmd_steps)
+    out["full"] = {"cells": [c, c, c], "sites": n, "steps": args.dmd_steps, "precision": "mixed",
+                   "wall_s": dt, "wall_s_per_outer_step": dt / max(args.dmd_steps, 1),
+                   "iters_per_step": r["iters"].tolist(), "xH_total": r["xH_mean"].tolist(),
+                   "depth_profile_first_layers": prof[:12].tolist()}
+    ks = args.dmd_ref_steps
+    r64, t64, nr, p64 = run(8, 12, "fp64", ks)
+    rmx, tmx, _, pmx = run(8, 12, "mixed", ks)
+    out["reduced"] = {"cells": [8, 8, 12], "sites": nr, "steps": ks,
+                      "fp64": {"wall_s_per_outer_step": t64 / ks, "xH_total": r64["xH_mean"].tolist(),
+                               "iters_per_step": r64["iters"].tolist()},
+                      "mixed": {"wall_s_per_outer_step": tmx / ks, "xH_total": rmx["xH_mean"].tolist(),
+                                "iters_per_step": rmx["iters"].tolist()},
+                      "xH_total_rel_err": float(np.max(np.abs(rmx["xH_mean"] - r64["xH_mean"]) / r64["xH_mean"])),
+                      "profile_max_abs_err": float(np.max(np.abs(pmx - p64))),
+                      "occupancy_max_abs_err": float(np.max(np.abs(rmx["xH"] - r64["xH"])))}
+    print(json.dumps({"coupled_dmd": out}))
+    return 0
+
+
+def run_batch_case(args):
+    """Batched uneven instances: `--batch-n` independent periodic lattices
+    (edge ~ U{4..16} cells, T ~ U(200, 600) K, mean x ~ U(0.01, 0.70) +-
+    0.02, N(0, 0.02 A) positions, sigma = 0.10 A; 256 lattices = 3,040,448
+    sites) minimized to gatol 1e-6 as one batch in the mixed form with the
+    FP64 polish, every L-BFGS tick a replayed CUDA graph, instances retiring
+    as they converge.  Reported: time to finish the whole batch, aggregate
+    atom-evals/s (sum over instances of sites x evaluations / device time),
+    and, on every `--batch-stride`-th instance, the same instances minimized
+    one by one with the plain FP64 path (a2c_gpp_minimize) and with the
+    mixed path, and as one FP64 batch; the loop times are scaled to the whole
+    batch by sites (labelled extrapolated)."""
+    import numpy as np
+
+    import a2c_gb300 as A
+
+    dev = dist_env()[2]
+    inst, X, xH = A.batch_workload(n=args.batch_n)
+    sizes = np.array([i["nPd"] + i["nH"] for i in inst])
+    kw = dict(gatol=1e-6, max_it=5000, max_fev=10000)
+    out = {"case": "batched instances", "instances": len(inst), "sites": int(sizes.sum()),
+           "edge_cells": [int(i["edge"]) for i in inst], "gatol": 1e-6}
+    with A.Batch(inst, precision="mixed", device=dev) as b:
+        b.set_occupancy(xH)
+        t0 = time.perf_counter()
+        b.build_neighbors(X)
+        out["neighbor_build_s"] = time.perf_counter() - t0
+        b.eval(X)  # set-up outside the timed region
+        t0 = time.perf_counter()
+        r = b.minimize(X, **kw)
+        wall = time.perf_counter() - t0
+    evals = float((sizes * r.nfev).sum())
+    out["mixed_batch"] = {"wall_s": wall, "device_s": r.seconds, "ticks": r.ticks,
+                          "atom_evals": evals, "atom_evals_per_s": evals / r.seconds,
+                          "reasons": {int(k): int(v) for k, v in zip(*np.unique(r.reason, return_counts=True))},
+                          "mixed_iters_mean": float(r.mixed_iters.mean()), "fp64_polish_iters_mean":
+                          float(r.fp64_iters.mean()), "nfev_max": int(r.nfev.max())}
+    sub = list(range(0, len(inst), args.batch_stride))
+    sub_sites = int(sizes[sub].sum())
+    scale = float(sizes.sum()) / sub_sites
+    so = np.concatenate([[0], np.cumsum(sizes)])
+    ho = np.concatenate([[0], np.cumsum([i["nH"] for i in inst])])
+    Xs = [X[4 * so[k]:4 * so[k + 1]] for k in range(len(inst))]
+    hs = [xH[ho[k]:ho[k + 1]] for k in range(len(inst))]
+    loops = {}
+    for prec in ("fp64", "mixed"):
+        tot, ev = 0.0, 0.0
+        for k in sub:
+            it = inst[k]
+            with A.Gpp(it["nPd"], it["nH"], T=it["T"], box=it["box"], periodic=it["periodic"], precision=prec,
+                       device=dev) as g:
+                g.set_occupancy(hs[k])
+                g.build_neighbors(Xs[k])
+                g.eval(Xs[k])
+                t0 = time.perf_counter()
+                rr = g.minimize(Xs[k], **kw)
+                tot += time.perf_counter() - t0
+                ev += (it["nPd"] + it["nH"]) * rr.nfev
+        loops[prec] = {"subset_s": tot, "subset_atom_evals_per_s": ev / tot,
+                       "extrapolated_whole_batch_s": tot * scale}
+    sub_inst = [inst[k] for k in sub]
+    with A.Batch(sub_inst, precision="fp64", device=dev) as b:
+        Xsub = np.concatenate([Xs[k] for k in sub])
+        b.set_occupancy(np.concatenate([hs[k] for k in sub]))
+        b.build_neighbors(Xsub)
+        b.eval(Xsub)
+        t0 = time.perf_counter()
+        r64 = b.minimize(Xsub, **kw)
+        t64 = time.perf_counter() - t0
+    out["subset"] = {"instances": len(sub), "sites": sub_sites, "scale_to_batch": scale,
+                     "fp64_loop": loops["fp64"], "mixed_loop": loops["mixed"],
+                     "fp64_batch_s": t64, "fp64_batch_extrapolated_s": t64 * scale,
+                     "fp64_batch_reasons": {int(k): int(v) for k, v in
+                                            zip(*np.unique(r64.reason, return_counts=True))}}
+    out["speedup_vs_fp64_loop_extrapolated"] = loops["fp64"]["extrapolated_whole_batch_s"] / wall
+    print(json.dumps({"batched": out}))
+    return 0
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -486,13 +662,22 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--ttm-cells", type=int, default=12,
                     help="time-to-minimum leg on a cells^3 nucleus lattice (0 = skip; 64 = the full 2,097,152 sites)")
-    ap.add_argument("--case", choices=["bench", "profile", "ttm"], default="bench",
+    ap.add_argument("--case", choices=["bench", "profile", "ttm", "dmd", "batch"], default="bench",
                     help="profile: the small untimed case used for ncu captures")
     ap.add_argument("--case-cells", type=int, default=40)
     ap.add_argument("--case-tps", type=int, default=0, help="threads per site in the profile case (0 = library)")
+    ap.add_argument("--dmd-cells", type=int, default=48, help="coupled-DMD slab edge in cells")
+    ap.add_argument("--dmd-steps", type=int, default=100, help="coupled-DMD outer steps")
+    ap.add_argument("--dmd-ref-steps", type=int, default=10, help="outer steps of the reduced FP64/mixed comparison")
+    ap.add_argument("--batch-n", type=int, default=256, help="instances of the batched case")
+    ap.add_argument("--batch-stride", type=int, default=16, help="every k-th instance forms the looped subset")
     args = ap.parse_args()
     if args.case == "profile":
         return run_profile_case(args)
+    if args.case == "dmd":
+        return run_dmd_case(args)
+    if args.case == "batch":
+        return run_batch_case(args)
     if args.case == "ttm":
         print(json.dumps({"time_to_minimum": time_to_minimum(args.ttm_cells, 1e-6, dist_env()[2])}))
         return 0

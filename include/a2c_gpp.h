@@ -176,6 +176,14 @@ a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, d
  * last call's contents; nothing in it needs clearing, but calls that
  * overlap on the GPU (two streams, two contexts on one device) race.
  * Stream-ordered on the context's stream, like a2c_gpp_eval_device. */
+/* Autotuner (no reference counterpart): times the mixed-precision
+ * evaluation at the context's current state (set by a2c_gpp_eval /
+ * a2c_gpp_set_state) for 1, 2, 4 and 8 threads per site, `reps` timed
+ * evaluations each after one untimed, and keeps the fastest for the
+ * context.  tps receives the choice, ms[4] (may be NULL) the mean time per
+ * evaluation of each candidate in milliseconds. */
+a2c_status a2c_gpp_autotune(a2c_gpp_ctx *ctx, int reps, int *tps, float *ms);
+
 a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG);
 /* Profiling aid: one stream-ordered evaluation on device pointers with CUDA
  * events between its launches; stage_ms[4] receives the durations of the
@@ -272,6 +280,49 @@ a2c_status a2c_restart_write(const char *path, int nPd, int nH, const double *X,
                              const double *gamma, const int *full_H, int step, double time);
 a2c_status a2c_restart_read(const char *path, int nPd, int nH, double xLb, double xUb, double *X, double *xH,
                             double *gamma, int *full_H);
+
+/* ------------------------------------------------------------------------
+ * Batched independent instances (the reference runs one lattice per
+ * process; these entry points have no reference counterpart and replace a
+ * loop of Minimizer::initialize + minimizeFreeEntropy, minimizer.cpp:484-586,
+ * over many lattices).  Instance b is described by params[b] (its nPd, nH,
+ * T, box, periodic flags); QWp, eps, rc, a_Pd, the correction coefficients,
+ * the precision and the device must agree across instances.  Arrays are the
+ * instances' reference-layout arrays concatenated in instance order: X and
+ * G are sum(4 (nPd_b + nH_b)) doubles, xH is sum(nH_b).  All instances are
+ * evaluated by one launch of each kernel; their reductions are per instance
+ * and do not depend on the other instances.
+ * ------------------------------------------------------------------------ */
+typedef struct a2c_gpp_batch a2c_gpp_batch;
+
+a2c_status a2c_gpp_batch_create(const a2c_gpp_params *params, int n_instances, a2c_gpp_batch **out);
+a2c_status a2c_gpp_batch_destroy(a2c_gpp_batch *batch);
+a2c_status a2c_gpp_batch_info(a2c_gpp_batch *batch, int *n_instances, int64_t *n_sites);
+a2c_status a2c_gpp_batch_set_occupancy(a2c_gpp_batch *batch, const double *xH);
+/* per-instance neighbor build (findNeighbors + findLocalNeighbors, as
+ * a2c_gpp_build_neighbors) from host X; max_neighbors may be NULL */
+a2c_status a2c_gpp_batch_build_neighbors(a2c_gpp_batch *batch, const double *X, int *max_neighbors);
+/* mixed-precision threads per site (0 = library choice), as
+ * a2c_gpp_set_threads_per_site */
+a2c_status a2c_gpp_batch_set_threads_per_site(a2c_gpp_batch *batch, int tps);
+/* 1 (default): one L-BFGS tick of all instances is captured once in a CUDA
+ * graph and replayed; 0: the same launches issued one by one */
+a2c_status a2c_gpp_batch_set_graphs(a2c_gpp_batch *batch, int on);
+/* host X (4N) -> f[n_instances], G (4N) */
+a2c_status a2c_gpp_batch_eval(a2c_gpp_batch *batch, const double *X, double *f, double *G);
+/* Minimizes every instance (the algorithm of a2c_gpp_minimize, per
+ * instance) from X, which receives the minima.  Per instance: fmin, iters,
+ * nfev, gnorm, reason; mixed_iters / fp64_iters (may be NULL) split the
+ * iterations between the mixed phase and the FP64 polish.  Instances retire
+ * when they stop; the call returns when all have. */
+a2c_status a2c_gpp_batch_minimize(a2c_gpp_batch *batch, double *X, const a2c_lbfgs_params *lbfgs, double *fmin,
+                                  int *iters, int *nfev, double *gnorm, int *reason, int *mixed_iters,
+                                  int *fp64_iters);
+/* ticks (one evaluation of every live instance each) and device seconds of
+ * the last a2c_gpp_batch_minimize */
+a2c_status a2c_gpp_batch_stats(a2c_gpp_batch *batch, int *ticks, double *seconds);
+/* the autotuner (see a2c_gpp_autotune) over the whole batch at host X */
+a2c_status a2c_gpp_batch_autotune(a2c_gpp_batch *batch, const double *X, int reps, int *tps, float *ms);
 
 /* Seeded synthetic fcc Pd lattice with octahedral H sites (stand-in for the
  * reference's SpaceInitializer lattice setup).  Site order: cells z, y, x,

@@ -72,6 +72,38 @@ double gpu_tree_sum(int64_t n, int maxgrid, Term term) {
   return block_tree(lane);
 }
 
+// The batched-instance reduction (one instance's terms): the n terms are
+// cut into chunks of g_chunk consecutive terms; one block of 256 threads
+// reduces each chunk (thread t sums its terms t, t+256, ... from 0.0, then
+// the block tree above), and one block sums the chunk partials strided by
+// 256 and combines them by the same tree.  g_chunk = 0 selects the
+// single-system reduction (gpu_tree_sum).
+int g_chunk = 0;
+template <class Term>
+double chunk_sum(int64_t n, Term term) {
+  std::vector<double> part;
+  double lane[256];
+  for (int64_t c0 = 0; c0 < n; c0 += g_chunk) {
+    const int64_t len = std::min<int64_t>(g_chunk, n - c0);
+    for (int t = 0; t < 256; ++t) {
+      double s = 0.0;
+      for (int64_t i = t; i < len; i += 256) s += term(c0 + i);
+      lane[t] = s;
+    }
+    part.push_back(block_tree(lane));
+  }
+  for (int t = 0; t < 256; ++t) {
+    double s = 0.0;
+    for (size_t i = (size_t)t; i < part.size(); i += 256) s += part[i];
+    lane[t] = s;
+  }
+  return block_tree(lane);
+}
+template <class Term>
+double dev_sum(int64_t n, int maxgrid, Term term) {
+  return g_chunk > 0 ? chunk_sum(n, term) : gpu_tree_sum(n, maxgrid, term);
+}
+
 // --------------------------------------------------------------------------
 // Vec3D arithmetic, in the order of Vector3D.h:83 (norm), 281-286 (dot),
 // 291-302 (scalar * vector), and the component-wise +/- operators.
@@ -466,8 +498,8 @@ int eval_impl(const orc_params *p, const double *X, const double *xH, const int6
       Ss[(size_t)s] = sg;
     }
     if (g_arith) {
-      sum_V = gpu_tree_sum(N, 1024, [&](int64_t i) { return Vs[(size_t)i]; });
-      sum_sigma = gpu_tree_sum(N, 1024, [&](int64_t i) { return Ss[(size_t)i]; });
+      sum_V = dev_sum(N, 1024, [&](int64_t i) { return Vs[(size_t)i]; });
+      sum_sigma = dev_sum(N, 1024, [&](int64_t i) { return Ss[(size_t)i]; });
     } else {
       for (int64_t s = 0; s < N; ++s) {
         sum_V += Vs[(size_t)s];
@@ -617,6 +649,8 @@ extern "C" {
 
 void orc_set_arith(int mode) { g_arith = mode ? 1 : 0; }
 int orc_get_arith(void) { return g_arith; }
+void orc_set_reduction(int chunk) { g_chunk = chunk > 0 ? chunk : 0; }
+int orc_get_reduction(void) { return g_chunk; }
 
 void orc_eam(int which, const double *in, int64_t n, double eps, double *out) {
   Eam e{eps};
@@ -866,7 +900,7 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
       if (v[(size_t)t] < lb) v[(size_t)t] = lb;
   };
   auto dotv = [&](const std::vector<double> &a, const std::vector<double> &b) {
-    if (g_arith) return gpu_tree_sum(n, 512, [&](int64_t t) { return a[(size_t)t] * b[(size_t)t]; });
+    if (g_arith) return dev_sum(n, 512, [&](int64_t t) { return a[(size_t)t] * b[(size_t)t]; });
     double s = 0.0;
     for (int64_t t = 0; t < n; ++t) s += a[(size_t)t] * b[(size_t)t];
     return s;
@@ -937,7 +971,7 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
       if (F(xn, &fn, gn)) return 1;
       double dec = 0.0;
       if (g_arith)
-        dec = gpu_tree_sum(n, 512, [&](int64_t t) { return g[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]); });
+        dec = dev_sum(n, 512, [&](int64_t t) { return g[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]); });
       else
         for (int64_t t = 0; t < n; ++t) dec += g[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]);
       if (std::isfinite(fn) && fn <= f + lp->c1 * dec) { ok = true; break; }
@@ -946,7 +980,7 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
       if (std::isfinite(fn) && std::fabs(fn - f) <= f_noise * std::fabs(f)) {
         double dn = 0.0;
         if (g_arith)
-          dn = gpu_tree_sum(n, 512, [&](int64_t t) { return gn[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]); });
+          dn = dev_sum(n, 512, [&](int64_t t) { return gn[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]); });
         else
           for (int64_t t = 0; t < n; ++t) dn += gn[(size_t)t] * (xn[(size_t)t] - x[(size_t)t]);
         if (dn <= (2.0 * lp->c1 - 1.0) * dec) { ok = true; break; }

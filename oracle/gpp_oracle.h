@@ -67,6 +67,11 @@ typedef struct orc_lbfgs {
  * exp/pow/log of a2c_gb300/csrc/ddmath.cuh and the GPU reduction tree). */
 void orc_set_arith(int mode);
 int orc_get_arith(void);
+/* Reduction order of the device arithmetic: 0 = the single-system trees
+ * (grid-strided partials); chunk > 0 = the batched-instance order (per
+ * instance, partials of `chunk` consecutive terms, then one block). */
+void orc_set_reduction(int chunk);
+int orc_get_reduction(void);
 
 /* EAM function by id (see gpp_oracle.cpp: 0..13), applied elementwise. */
 void orc_eam(int which, const double *in, int64_t n, double eps, double *out);

@@ -62,6 +62,8 @@ def olib() -> C.CDLL:
         L = C.CDLL(str(ORACLE_SO))
         L.orc_set_arith.argtypes = [I]
         L.orc_set_arith.restype = None
+        L.orc_set_reduction.argtypes = [I]
+        L.orc_set_reduction.restype = None
         L.orc_eam.argtypes = [I, P, I64, D, P]
         L.orc_neighbor_counts.argtypes = [C.POINTER(OrcParams), P, P, P]
         L.orc_neighbor_fill.argtypes = [C.POINTER(OrcParams), P, P, P, P, P, P]
@@ -93,6 +95,26 @@ class arithmetic:
 
     def __exit__(self, *exc):
         olib().orc_set_arith(0)
+
+
+# terms per reduction chunk of the batched-instance evaluator and L-BFGS
+BATCH_CHUNK = 2048
+
+
+class reduction:
+    """Context manager selecting the reduction order of the device
+    arithmetic: "single" (one system: grid-strided partials) or "batch" (one
+    instance of a batch: partials of BATCH_CHUNK consecutive terms)."""
+
+    def __init__(self, mode: str):
+        self.chunk = {"single": 0, "batch": BATCH_CHUNK}[mode]
+
+    def __enter__(self):
+        olib().orc_set_reduction(self.chunk)
+        return self
+
+    def __exit__(self, *exc):
+        olib().orc_set_reduction(0)
 
 
 def ref_available() -> bool:

