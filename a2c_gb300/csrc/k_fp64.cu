@@ -387,10 +387,18 @@ SiteArgs site_args(a2c_gpp_ctx *c, const double *dX) {
 
 }  // namespace
 
+// Block size of the thread-per-site FP64 kernels.  A site's thread runs a
+// long serial FP64 chain, and the warps of one SM share its narrow FP64
+// pipe: a small system finishes sooner when its warps are spread over as
+// many SMs as possible (one-warp blocks); a large one fills the device
+// either way.  Results do not depend on the block size.
+unsigned block64(int64_t n) { return n < (int64_t)152 * kBlock * 4 ? 32u : (unsigned)kBlock; }
+
 a2c_status launch_density64(a2c_gpp_ctx *c, const double *dX) {
   if (c->N == 0) return A2C_OK;
   SiteArgs a = site_args(c, dX);
-  k_density64<<<grid_for(c->N, kBlock), kBlock, 0, c->stream>>>(a);
+  const unsigned bs = block64(c->N);
+  k_density64<<<grid_for(c->N, (int)bs), bs, 0, c->stream>>>(a);
   A2C_CUDA(cudaGetLastError());
   return A2C_OK;
 }
@@ -399,19 +407,23 @@ a2c_status launch_gradient64(a2c_gpp_ctx *c, const double *dX, double *dG) {
   if (c->N == 0) return A2C_OK;
   SiteArgs a = site_args(c, dX);
   a.G = dG;
-  k_gradient64<<<grid_for(c->N, kBlock), kBlock, 0, c->stream>>>(a);
+  const unsigned bs = block64(c->N);
+  k_gradient64<<<grid_for(c->N, (int)bs), bs, 0, c->stream>>>(a);
   A2C_CUDA(cudaGetLastError());
   return A2C_OK;
 }
 
+// One-warp blocks (see block64): the list length is only known on the
+// device, and a short list must still spread over all SMs.
 a2c_status launch_eval64_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv) {
+  constexpr int kLB = 32;
   static int cap[2] = {0, 0};
   if (!cap[0]) {
     int dev = 0, sms = 0, b0 = 0, b1 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_density64_list, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_gradient64_list, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_density64_list, kLB, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_gradient64_list, kLB, 0);
     cap[0] = std::max(1, sms * b0);
     cap[1] = std::max(1, sms * b1);
   }
@@ -419,9 +431,9 @@ a2c_status launch_eval64_list(a2c_gpp_ctx *c, const double *dX, double *dG, cons
   SiteArgs a = site_args(c, dX);
   a.G = dG;
   a.bv = bv;
-  const int64_t need = (c->N + kBlock - 1) / kBlock;
-  k_density64_list<<<(unsigned)std::min<int64_t>(need, cap[0]), kBlock, 0, c->stream>>>(a);
-  k_gradient64_list<<<(unsigned)std::min<int64_t>(need, cap[1]), kBlock, 0, c->stream>>>(a);
+  const int64_t need = (c->N + kLB - 1) / kLB;
+  k_density64_list<<<(unsigned)std::min<int64_t>(need, cap[0]), kLB, 0, c->stream>>>(a);
+  k_gradient64_list<<<(unsigned)std::min<int64_t>(need, cap[1]), kLB, 0, c->stream>>>(a);
   A2C_CUDA(cudaGetLastError());
   return A2C_OK;
 }

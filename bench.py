@@ -181,42 +181,62 @@ def nucleus_lattice(cells: int, seed: int = 3):
                          seed=seed)
 
 
-def time_to_minimum(cells: int, gatol: float, device: int):
+def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0):
     """Wall time of a2c_gpp_minimize to gatol in FP64 and in mixed precision
-    (mixed phase then FP64 polish), and the mixed result's distance from the
-    FP64 minimum."""
+    -- the mixed form alone and the mixed form followed by the FP64 polish --
+    and the mixed results' distance from the FP64 minimum.  With fp64_cap >
+    0 the FP64 run stops after fp64_cap iterations (the full run is too long
+    for one GPU session); its time to minimum is then extrapolated as its
+    measured seconds per iteration times the iterations the mixed run with
+    polish needed, and labelled so."""
     import numpy as np
 
     import a2c_gb300 as A
 
     X, xH, _, box, nPd, nH = nucleus_lattice(cells)
     out = {"cells": cells, "sites": nPd + nH, "gatol": gatol}
+    kw = dict(gatol=gatol, max_it=20000, max_fev=40000)
     with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), device=device) as g:
         g.set_occupancy(xH)
         g.build_neighbors(X)
         g.eval(X)  # warm-up (lazy set-up of both forms)
         g.set_precision("mixed")
         g.eval(X)
+        out["autotune_tps"] = g.autotune()[0]
         g.set_precision("fp64")
         t0 = time.perf_counter()
-        r64 = g.minimize(X, gatol=gatol, max_it=20000, max_fev=40000)
+        r64 = g.minimize(X, **(dict(kw, max_it=fp64_cap) if fp64_cap else kw))
         t64 = time.perf_counter() - t0
         g.set_precision("mixed")
-        t0 = time.perf_counter()
-        rmx = g.minimize(X, gatol=gatol, max_it=20000, max_fev=40000)
-        tmx = time.perf_counter() - t0
+        runs = {}
+        for name, polish in (("mixed", 1), ("mixed_no_polish", 0)):
+            t0 = time.perf_counter()
+            r = g.minimize(X, polish=polish, **kw)
+            runs[name] = (r, time.perf_counter() - t0)
         g.set_precision("fp64")
-        f_at_mixed, _ = g.eval(rmx.X)
-    dq = float(np.abs(rmx.X.reshape(-1, 4)[:, :3] - r64.X.reshape(-1, 4)[:, :3]).max())
-    ds = float(np.abs(rmx.X.reshape(-1, 4)[:, 3] - r64.X.reshape(-1, 4)[:, 3]).max())
-    out.update({"fp64": {"seconds": t64, "iters": r64.iters, "nfev": r64.nfev, "reason": r64.reason,
-                         "gnorm": r64.gnorm, "f": r64.fmin},
-                "mixed": {"seconds": tmx, "iters": rmx.iters, "mixed_iters": rmx.mixed_iters,
-                          "fp64_polish_iters": rmx.fp64_iters, "mixed_phase_gnorm": rmx.mixed_gnorm,
-                          "nfev": rmx.nfev, "reason": rmx.reason, "gnorm": rmx.gnorm},
-                "speedup": t64 / tmx,
-                "mixed_vs_fp64": {"free_entropy_rel": abs(f_at_mixed - r64.fmin) / abs(r64.fmin),
-                                  "max_position_A": dq, "max_sigma_A": ds}})
+        f64_at, g64_at = {}, {}
+        for name, (r, _) in runs.items():
+            fv, gv = g.eval(r.X)
+            f64_at[name] = fv
+            g64_at[name] = float(np.linalg.norm(gv))
+    out["fp64"] = {"seconds": t64, "iters": r64.iters, "nfev": r64.nfev, "reason": r64.reason, "gnorm": r64.gnorm,
+                   "f": r64.fmin, "seconds_per_iter": t64 / max(r64.iters, 1)}
+    if fp64_cap:
+        need = runs["mixed"][0].iters
+        out["fp64"].update(capped_at_iters=fp64_cap, extrapolated_seconds=t64 / max(r64.iters, 1) * need,
+                           extrapolation="FP64 seconds per iteration x iterations of the mixed run with polish")
+    t64_ref = out["fp64"].get("extrapolated_seconds", t64)
+    for name, (r, t) in runs.items():
+        dq = float(np.abs(r.X.reshape(-1, 4)[:, :3] - r64.X.reshape(-1, 4)[:, :3]).max())
+        ds = float(np.abs(r.X.reshape(-1, 4)[:, 3] - r64.X.reshape(-1, 4)[:, 3]).max())
+        out[name] = {"seconds": t, "iters": r.iters, "mixed_iters": r.mixed_iters, "fp64_polish_iters": r.fp64_iters,
+                     "mixed_phase_gnorm": r.mixed_gnorm, "nfev": r.nfev, "reason": r.reason, "gnorm": r.gnorm,
+                     "fp64_gnorm_at_result": g64_at[name], "speedup_vs_fp64": t64_ref / t}
+        if not fp64_cap:
+            out[name]["vs_fp64_minimum"] = {"free_entropy_rel": abs(f64_at[name] - r64.fmin) / abs(r64.fmin),
+                                            "max_position_A": dq, "max_sigma_A": ds}
+        else:
+            out[name]["free_entropy_fp64_at_result"] = f64_at[name]
     return out
 
 
@@ -321,14 +341,18 @@ def run_batch_case(args):
     """Batched uneven instances: `--batch-n` independent periodic lattices
     (edge ~ U{4..16} cells, T ~ U(200, 600) K, mean x ~ U(0.01, 0.70) +-
     0.02, N(0, 0.02 A) positions, sigma = 0.10 A; 256 lattices = 3,040,448
-    sites) minimized to gatol 1e-6 as one batch in the mixed form with the
-    FP64 polish, every L-BFGS tick a replayed CUDA graph, instances retiring
-    as they converge.  Reported: time to finish the whole batch, aggregate
-    atom-evals/s (sum over instances of sites x evaluations / device time),
-    and, on every `--batch-stride`-th instance, the same instances minimized
-    one by one with the plain FP64 path (a2c_gpp_minimize) and with the
-    mixed path, and as one FP64 batch; the loop times are scaled to the whole
-    batch by sites (labelled extrapolated)."""
+    sites) minimized to gatol 1e-6 as one batch, every L-BFGS tick a
+    replayed CUDA graph, instances retiring as they converge, threads per
+    site chosen by the library's autotuner.  Two mixed-precision runs: the
+    mixed form alone (gatol on its gradient; FP32 quadrature, FP64 L-BFGS)
+    and the mixed form followed by the FP64 polish (gatol on the FP64
+    gradient).  Reported: time to finish the whole batch, aggregate
+    atom-evals/s (sum over instances of sites x evaluations / device time).
+    On every `--batch-stride`-th instance: the plain FP64 path looped
+    instance by instance (a2c_gpp_minimize, the baseline), the mixed path
+    looped, and one FP64 batch; loop times are scaled to the whole batch by
+    sites (labelled extrapolated); the mixed results' distance to the FP64
+    minima of the same instances."""
     import numpy as np
 
     import a2c_gb300 as A
@@ -336,33 +360,42 @@ def run_batch_case(args):
     dev = dist_env()[2]
     inst, X, xH = A.batch_workload(n=args.batch_n)
     sizes = np.array([i["nPd"] + i["nH"] for i in inst])
+    so = np.concatenate([[0], np.cumsum(sizes)])
+    ho = np.concatenate([[0], np.cumsum([i["nH"] for i in inst])])
     kw = dict(gatol=1e-6, max_it=5000, max_fev=10000)
     out = {"case": "batched instances", "instances": len(inst), "sites": int(sizes.sum()),
            "edge_cells": [int(i["edge"]) for i in inst], "gatol": 1e-6}
+
+    def reasons(r):
+        return {int(k): int(v) for k, v in zip(*np.unique(r.reason, return_counts=True))}
+
+    res = {}
     with A.Batch(inst, precision="mixed", device=dev) as b:
         b.set_occupancy(xH)
         t0 = time.perf_counter()
         b.build_neighbors(X)
         out["neighbor_build_s"] = time.perf_counter() - t0
-        b.eval(X)  # set-up outside the timed region
-        t0 = time.perf_counter()
-        r = b.minimize(X, **kw)
-        wall = time.perf_counter() - t0
-    evals = float((sizes * r.nfev).sum())
-    out["mixed_batch"] = {"wall_s": wall, "device_s": r.seconds, "ticks": r.ticks,
-                          "atom_evals": evals, "atom_evals_per_s": evals / r.seconds,
-                          "reasons": {int(k): int(v) for k, v in zip(*np.unique(r.reason, return_counts=True))},
-                          "mixed_iters_mean": float(r.mixed_iters.mean()), "fp64_polish_iters_mean":
-                          float(r.fp64_iters.mean()), "nfev_max": int(r.nfev.max())}
+        tps, ms = b.autotune(X)
+        out["autotune"] = {"threads_per_site": tps, "ms_per_eval": ms}
+        for name, polish in (("mixed_batch", 0), ("mixed_polish_batch", 1)):
+            t0 = time.perf_counter()
+            r = b.minimize(X, polish=polish, **kw)
+            wall = time.perf_counter() - t0
+            evals = float((sizes * r.nfev).sum())
+            res[name] = r
+            out[name] = {"wall_s": wall, "device_s": r.seconds, "ticks": r.ticks, "atom_evals": evals,
+                         "atom_evals_per_s": evals / r.seconds, "reasons": reasons(r),
+                         "mixed_iters_mean": float(r.mixed_iters.mean()),
+                         "fp64_polish_iters_mean": float(r.fp64_iters.mean()),
+                         "fp64_polish_iters_max": int(r.fp64_iters.max()), "nfev_max": int(r.nfev.max())}
+            print(json.dumps({name: out[name]}), flush=True)
     sub = list(range(0, len(inst), args.batch_stride))
     sub_sites = int(sizes[sub].sum())
     scale = float(sizes.sum()) / sub_sites
-    so = np.concatenate([[0], np.cumsum(sizes)])
-    ho = np.concatenate([[0], np.cumsum([i["nH"] for i in inst])])
     Xs = [X[4 * so[k]:4 * so[k + 1]] for k in range(len(inst))]
     hs = [xH[ho[k]:ho[k + 1]] for k in range(len(inst))]
     loops = {}
-    for prec in ("fp64", "mixed"):
+    for prec, polish in (("fp64", 1), ("mixed", 0)):
         tot, ev = 0.0, 0.0
         for k in sub:
             it = inst[k]
@@ -372,11 +405,12 @@ def run_batch_case(args):
                 g.build_neighbors(Xs[k])
                 g.eval(Xs[k])
                 t0 = time.perf_counter()
-                rr = g.minimize(Xs[k], **kw)
+                rr = g.minimize(Xs[k], polish=polish, **kw)
                 tot += time.perf_counter() - t0
                 ev += (it["nPd"] + it["nH"]) * rr.nfev
         loops[prec] = {"subset_s": tot, "subset_atom_evals_per_s": ev / tot,
                        "extrapolated_whole_batch_s": tot * scale}
+        print(json.dumps({prec + "_loop": loops[prec]}), flush=True)
     sub_inst = [inst[k] for k in sub]
     with A.Batch(sub_inst, precision="fp64", device=dev) as b:
         Xsub = np.concatenate([Xs[k] for k in sub])
@@ -386,12 +420,24 @@ def run_batch_case(args):
         t0 = time.perf_counter()
         r64 = b.minimize(Xsub, **kw)
         t64 = time.perf_counter() - t0
+        X64 = b.split(r64.X)
+    acc = {}
+    for name in ("mixed_batch", "mixed_polish_batch"):
+        r = res[name]
+        dq, df = 0.0, 0.0
+        for j, k in enumerate(sub):
+            a = r.X[4 * so[k]:4 * so[k + 1]].reshape(-1, 4)
+            c = X64[j].reshape(-1, 4)
+            dq = max(dq, float(np.abs(a[:, :3] - c[:, :3]).max()))
+            df = max(df, abs(r.fmin[k] - r64.fmin[j]) / abs(r64.fmin[j]))
+        acc[name] = {"max_position_A": dq, "max_free_entropy_rel": df}
     out["subset"] = {"instances": len(sub), "sites": sub_sites, "scale_to_batch": scale,
                      "fp64_loop": loops["fp64"], "mixed_loop": loops["mixed"],
                      "fp64_batch_s": t64, "fp64_batch_extrapolated_s": t64 * scale,
-                     "fp64_batch_reasons": {int(k): int(v) for k, v in
-                                            zip(*np.unique(r64.reason, return_counts=True))}}
-    out["speedup_vs_fp64_loop_extrapolated"] = loops["fp64"]["extrapolated_whole_batch_s"] / wall
+                     "fp64_batch_reasons": reasons(r64), "mixed_vs_fp64_minima": acc}
+    base = loops["fp64"]["extrapolated_whole_batch_s"]
+    out["speedup_vs_fp64_loop_extrapolated"] = {k: base / out[k]["wall_s"]
+                                                for k in ("mixed_batch", "mixed_polish_batch")}
     print(json.dumps({"batched": out}))
     return 0
 
@@ -666,6 +712,8 @@ def main():
                     help="profile: the small untimed case used for ncu captures")
     ap.add_argument("--case-cells", type=int, default=40)
     ap.add_argument("--case-tps", type=int, default=0, help="threads per site in the profile case (0 = library)")
+    ap.add_argument("--ttm-fp64-cap", type=int, default=0,
+                    help="stop the FP64 time-to-minimum run after this many iterations (0 = run to the end)")
     ap.add_argument("--dmd-cells", type=int, default=48, help="coupled-DMD slab edge in cells")
     ap.add_argument("--dmd-steps", type=int, default=100, help="coupled-DMD outer steps")
     ap.add_argument("--dmd-ref-steps", type=int, default=10, help="outer steps of the reduced FP64/mixed comparison")
@@ -679,7 +727,8 @@ def main():
     if args.case == "batch":
         return run_batch_case(args)
     if args.case == "ttm":
-        print(json.dumps({"time_to_minimum": time_to_minimum(args.ttm_cells, 1e-6, dist_env()[2])}))
+        print(json.dumps({"time_to_minimum": time_to_minimum(args.ttm_cells, 1e-6, dist_env()[2],
+                                                             args.ttm_fp64_cap)}))
         return 0
     if args.warmup < 3:
         args.warmup = 3
