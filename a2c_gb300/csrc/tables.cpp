@@ -7,9 +7,9 @@
 // interpolants on a uniform grid: values and exact first derivatives are
 // computed in FP64 by forward-mode differentiation (dual numbers) of the
 // reference's formulas, and the cubic's coefficients are rounded to FP32.
-// Grid: r in [1, 8) A, h = 1/320 A, so the branch points 5.0 (f_Pd tail)
-// and 5.05 (phi_Pd tail) are knots and each interval lies in one branch.
-// Interpolation error is below 1e-9 relative inside the polynomial range.
+// The caller picks the grid; the mixed kernels use r in [1, 7) A with
+// h = 1/160 A, so the branch points 5.0 (f_Pd tail) and 5.05 (phi_Pd tail)
+// are knots and each interval lies in one branch.
 // The embedding functions F_Pd(rho), F_H(rho) (per site) are tabulated the
 // same way on rho in [0, 64), h = 1/64.
 #include <cmath>
