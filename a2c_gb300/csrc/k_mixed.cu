@@ -39,6 +39,7 @@
 namespace a2c {
 
 void build_pair_table(double r0, double h, int n, std::vector<float> &out);
+void build_pair_table_raw(double r0, double h, int n, float *out);
 void build_embed_table(int species, double h, int n, std::vector<float> &out);
 
 struct Mixed {
@@ -46,7 +47,7 @@ struct Mixed {
   int4 *P = nullptr;        // per site: fixed-point x, y, z; sigma (FP32 bits)
   float *occ = nullptr;     // per site occupancy (1 for Pd)
   float2 *FF = nullptr;     // per site (F'(rho), F(rho))
-  float4 *tabPair = nullptr;  // kTabN f_Pd cubics, then kTabN phi_Pd cubics
+  float4 *tabPair = nullptr;  // f_Pd cubics, phi_Pd cubics, f_Pd' quadratics (kTabN each)
   int grid_cap[9] = {};       // persistent grid size per threads-per-site
   float4 *tabEmb = nullptr;   // per rho interval: F_Pd cubics, then F_H cubics
   int tps = 0;                // threads per site (0 = choose)
@@ -130,6 +131,8 @@ __device__ __forceinline__ SiteRef<LIST> site_ref(const MixArgs &a, int64_t k) {
 
 __device__ __forceinline__ float hv(float4 c, float t) { return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x); }
 __device__ __forceinline__ float hd(float4 c, float t) { return fmaf(fmaf(3.0f * c.w, t, 2.0f * c.z), t, c.y); }
+// h times the derivative from its own coefficients (c1, 2 c2, 3 c3)
+__device__ __forceinline__ float dq(float4 d, float t) { return fmaf(fmaf(d.z, t, d.y), t, d.x); }
 
 __device__ __forceinline__ int tab_index(float s, float &t) {
   float x = (s - (float)kTabR0) * (float)kTabInvH;
@@ -319,8 +322,10 @@ __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, f
         float tt;
         const int i = tab_index(r, tt);
         const float4 cf = sF[i], cp = sP[i];
-        g = fmaf(Fa + Fb, hd(cf, tt), hd(cp, tt)) * (float)kTabInvH;
-        phi = hv(cp, tt);
+        // phi and h phi' share one Horner chain
+        const float hp = fmaf(cp.w, tt, cp.z), hq = fmaf(hp, tt, cp.y);
+        phi = fmaf(hq, tt, cp.x);
+        g = fmaf(Fa + Fb, dq(cf, tt), fmaf(fmaf(cp.w, tt, hp), tt, hq)) * (float)kTabInvH;
       } else if (TYPE == 3) {
         const float fh = fH(r);
         float dphi;
@@ -329,7 +334,7 @@ __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, f
       } else {
         float tt;
         const int i = tab_index(r, tt);
-        const float fpd = hd(sF[i], tt) * (float)kTabInvH;
+        const float fpd = dq(sF[i], tt) * (float)kTabInvH;
         const float fhd = fH(r) * kFH_D;
         float dphi;
         morse(kPdH, r, phi, dphi);
@@ -364,7 +369,7 @@ __global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
   __shared__ float4 sF[kTabN], sP[kTabN];
   for (int i = threadIdx.x; i < kTabN; i += blockDim.x) {
-    sF[i] = __ldg(&a.tabPair[i]);
+    sF[i] = __ldg(&a.tabPair[2 * kTabN + i]);  // f_Pd' only
     sP[i] = __ldg(&a.tabPair[kTabN + i]);
   }
   __syncthreads();
@@ -474,6 +479,28 @@ void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev) {
   if (ev) cudaEventRecord(ev[3], st);
 }
 
+// The pair tables as the kernels read them (3 kTabN float4): the f_Pd
+// cubics (pass 1), the phi_Pd cubics, and the f_Pd' quadratics
+// (c1, 2 c2, 3 c3) of pass 2, which needs only the derivative.
+void pair_tables(float *out) {
+  static std::mutex m;  // guards the static scratch below
+  std::lock_guard<std::mutex> lock(m);
+  static float inter[8 * kTabN];
+  build_pair_table_raw(kTabR0, 1.0 / kTabInvH, kTabN, inter);
+  for (int i = 0; i < kTabN; ++i) {
+    const float *f = inter + 8 * i, *p = inter + 8 * i + 4;
+    for (int k = 0; k < 4; ++k) {
+      out[4 * i + k] = f[k];
+      out[4 * (kTabN + i) + k] = p[k];
+    }
+    float *d = out + 4 * (2 * kTabN + i);
+    d[0] = f[1];
+    d[1] = 2.0f * f[2];
+    d[2] = 3.0f * f[3];
+    d[3] = 0.0f;
+  }
+}
+
 a2c_status ensure_mixed(a2c_gpp_ctx *c) {
   if (c->mixed && c->mixed->N == c->N) return A2C_OK;
   mixed_free(c);
@@ -483,16 +510,11 @@ a2c_status ensure_mixed(a2c_gpp_ctx *c) {
   const int64_t n = std::max<int64_t>(c->N, 1);
   if (cudaMalloc(&M->P, sizeof(int4) * n) != cudaSuccess || cudaMalloc(&M->occ, sizeof(float) * n) != cudaSuccess ||
       cudaMalloc(&M->FF, sizeof(float2) * n) != cudaSuccess ||
-      cudaMalloc(&M->tabPair, sizeof(float4) * 2 * kTabN) != cudaSuccess ||
+      cudaMalloc(&M->tabPair, sizeof(float4) * 3 * kTabN) != cudaSuccess ||
       cudaMalloc(&M->tabEmb, sizeof(float4) * 2 * kEmbN) != cudaSuccess)
     return A2C_ERR_NOMEM;
-  std::vector<float> inter, pair((size_t)8 * kTabN), embPd, embH;
-  build_pair_table(kTabR0, 1.0 / kTabInvH, kTabN, inter);
-  for (int i = 0; i < kTabN; ++i)  // interleaved (f, phi) per interval -> all f cubics, then all phi cubics
-    for (int k = 0; k < 4; ++k) {
-      pair[(size_t)4 * i + k] = inter[(size_t)8 * i + k];
-      pair[(size_t)4 * (kTabN + i) + k] = inter[(size_t)8 * i + 4 + k];
-    }
+  std::vector<float> pair((size_t)12 * kTabN), embPd, embH;
+  pair_tables(pair.data());
   build_embed_table(0, 1.0 / kEmbInvH, kEmbN, embPd);
   build_embed_table(1, 1.0 / kEmbInvH, kEmbN, embH);
   A2C_CUDA(cudaMemcpyAsync(M->tabPair, pair.data(), sizeof(float) * pair.size(), cudaMemcpyHostToDevice, c->stream));
@@ -642,7 +664,7 @@ constexpr size_t kNaVs = kNaFF + 8 * (size_t)kNaMaxSites;
 constexpr size_t kNaSs = kNaVs + 8 * (size_t)kNaMaxSites;
 constexpr size_t kNaPart = kNaSs + 8 * (size_t)kNaMaxSites;
 constexpr size_t kNaTabPair = kNaPart + 8 * 2 * (size_t)kNaRedGrid;
-constexpr size_t kNaTabEmb = kNaTabPair + 16 * 2 * (size_t)kTabN;
+constexpr size_t kNaTabEmb = kNaTabPair + 16 * 3 * (size_t)kTabN;
 constexpr size_t kNaBytes = kNaTabEmb + 16 * 2 * (size_t)kEmbN;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
@@ -651,7 +673,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 constexpr int kNaMaxDevices = 64;
 unsigned char *g_na_base[kNaMaxDevices] = {};
 std::mutex g_na_mutex;
-float g_na_pair_host[8 * kTabN];
+float g_na_pair_host[12 * kTabN];
 float g_na_emb_host[2 * 4 * kEmbN];
 bool g_na_host_ready = false;
 
@@ -668,13 +690,7 @@ a2c_status na_setup(int dev, unsigned char **base) {
   cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
   if (e != cudaSuccess) return cuda_status(e);
   if (!g_na_host_ready) {
-    static float inter[8 * kTabN];
-    build_pair_table_raw(kTabR0, 1.0 / kTabInvH, kTabN, inter);
-    for (int i = 0; i < kTabN; ++i)  // all f cubics, then all phi cubics
-      for (int k = 0; k < 4; ++k) {
-        g_na_pair_host[4 * i + k] = inter[8 * i + k];
-        g_na_pair_host[4 * (kTabN + i) + k] = inter[8 * i + 4 + k];
-      }
+    pair_tables(g_na_pair_host);
     build_embed_table_raw(0, 1.0 / kEmbInvH, kEmbN, g_na_emb_host);
     build_embed_table_raw(1, 1.0 / kEmbInvH, kEmbN, g_na_emb_host + 4 * kEmbN);
     g_na_host_ready = true;

@@ -394,7 +394,7 @@ def run_batch_case(args):
     scale = float(sizes.sum()) / sub_sites
     Xs = [X[4 * so[k]:4 * so[k + 1]] for k in range(len(inst))]
     hs = [xH[ho[k]:ho[k + 1]] for k in range(len(inst))]
-    loops = {}
+    loops, loopX = {}, {}
     for prec, polish in (("fp64", 1), ("mixed", 0)):
         tot, ev = 0.0, 0.0
         for k in sub:
@@ -408,6 +408,8 @@ def run_batch_case(args):
                 rr = g.minimize(Xs[k], polish=polish, **kw)
                 tot += time.perf_counter() - t0
                 ev += (it["nPd"] + it["nH"]) * rr.nfev
+                if prec == "fp64":
+                    loopX[k] = (rr.X, rr.fmin)
         loops[prec] = {"subset_s": tot, "subset_atom_evals_per_s": ev / tot,
                        "extrapolated_whole_batch_s": tot * scale}
         print(json.dumps({prec + "_loop": loops[prec]}), flush=True)
@@ -431,6 +433,15 @@ def run_batch_case(args):
             dq = max(dq, float(np.abs(a[:, :3] - c[:, :3]).max()))
             df = max(df, abs(r.fmin[k] - r64.fmin[j]) / abs(r64.fmin[j]))
         acc[name] = {"max_position_A": dq, "max_free_entropy_rel": df}
+    # the same FP64 minimization in two reduction orders (looped vs batched):
+    # how well gatol 1e-6 determines the minimum at all
+    dq, df = 0.0, 0.0
+    for j, k in enumerate(sub):
+        a = loopX[k][0].reshape(-1, 4)
+        c = X64[j].reshape(-1, 4)
+        dq = max(dq, float(np.abs(a[:, :3] - c[:, :3]).max()))
+        df = max(df, abs(loopX[k][1] - r64.fmin[j]) / abs(r64.fmin[j]))
+    acc["fp64_loop_vs_fp64_batch"] = {"max_position_A": dq, "max_free_entropy_rel": df}
     out["subset"] = {"instances": len(sub), "sites": sub_sites, "scale_to_batch": scale,
                      "fp64_loop": loops["fp64"], "mixed_loop": loops["mixed"],
                      "fp64_batch_s": t64, "fp64_batch_extrapolated_s": t64 * scale,
