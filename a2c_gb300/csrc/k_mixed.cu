@@ -61,6 +61,11 @@ constexpr int kTabN = 960;  // r in [1, 7): knots on the 5.0 / 5.05 A branch poi
 constexpr double kEmbInvH = 64.0;
 constexpr int kEmbN = 4096;  // rho in [0, 64)
 constexpr int kBlock = 256;
+// Pass 2 resident blocks per SM the register allocation must allow (4
+// blocks of 256 threads = 64 registers per thread).
+#ifndef A2C_GRAD_MIN_BLOCKS
+#define A2C_GRAD_MIN_BLOCKS 4
+#endif
 
 struct MixArgs {
   int64_t N;
@@ -154,6 +159,12 @@ __device__ __forceinline__ float fH(float s) { return kFH_A * ex2(kFH_K * (s - 3
 struct Morse {
   float A1, K1, R1, A2, K2, R2, rc, At, Kt;
 };
+// Inside the switch radius only (the caller has checked s <= rc).
+__device__ __forceinline__ void morse_in(const Morse &m, float s, float &v, float &d) {
+  const float e1 = m.A1 * ex2(m.K1 * (s - m.R1)), e2 = m.A2 * ex2(m.K2 * (s - m.R2));
+  v = e1 + e2;
+  d = (e1 * m.K1 + e2 * m.K2) * 0.6931471805599453f;
+}
 __device__ __forceinline__ void morse(const Morse &m, float s, float &v, float &d) {
   const bool tail = s > m.rc;
   const float A1 = tail ? 0.0f : m.A1, A2 = tail ? m.At : m.A2;
@@ -300,7 +311,19 @@ struct PairAcc {
   float csum, e[3], sig, v;
 };
 
-template <int TYPE>  // 0 Pd-Pd, 1 Pd i / H j, 2 H i / Pd j, 3 H-H
+// True when all 12 quadrature points of the pair lie within the 5.35 A
+// switch radius of phi_PdH / phi_H: the largest squared radius is
+// |D|^2 + u^2 + 2 u max|D_c| with u the larger displacement.
+__device__ __forceinline__ bool pair_inside(float3 D, float ui, float uj) {
+  const float u = fmaxf(ui, uj);
+  const float m = fmaxf(fabsf(D.x), fmaxf(fabsf(D.y), fabsf(D.z)));
+  const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
+  return fmaf(2.0f * u, m, fmaf(u, u, D2)) <= 5.35f * 5.35f;
+}
+
+// TAIL = false: every point is inside the switch radius (pair_inside), so
+// the Morse terms skip the per-point branch selection.
+template <int TYPE, bool TAIL = true>  // 0 Pd-Pd, 1 Pd i / H j, 2 H i / Pd j, 3 H-H
 __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, float Fa, float Fb, float3 D, float ui,
                                            float uj, PairAcc &p) {
   const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
@@ -329,7 +352,8 @@ __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, f
       } else if (TYPE == 3) {
         const float fh = fH(r);
         float dphi;
-        morse(kHH, r, phi, dphi);
+        if (TAIL) morse(kHH, r, phi, dphi);
+        else morse_in(kHH, r, phi, dphi);
         g = fmaf((Fa + Fb) * kFH_D, fh, dphi);
       } else {
         float tt;
@@ -337,7 +361,8 @@ __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, f
         const float fpd = dq(sF[i], tt) * (float)kTabInvH;
         const float fhd = fH(r) * kFH_D;
         float dphi;
-        morse(kPdH, r, phi, dphi);
+        if (TAIL) morse(kPdH, r, phi, dphi);
+        else morse_in(kPdH, r, phi, dphi);
         g = (TYPE == 1) ? fmaf(Fa, fhd, fmaf(Fb, fpd, dphi)) : fmaf(Fa, fpd, fmaf(Fb, fhd, dphi));
       }
       ck[q] = g * is;
@@ -363,7 +388,7 @@ __device__ __forceinline__ void add_pair(SiteAcc &A, const PairAcc &p, float3 D,
 }
 
 template <int TPS, bool LIST>
-__global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
+__global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_mixed(MixArgs a) {
   constexpr int kSitesPerBlock = kBlock / TPS;
   const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
@@ -399,16 +424,27 @@ __global__ void __launch_bounds__(kBlock) k_grad_mixed(MixArgs a) {
       const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       PairAcc p;
-      if (iPd) pair_terms<0>(sF, sP, ffi.x, Fb, D, ui, uj, p);
-      else pair_terms<2>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+      if (iPd) {
+        pair_terms<0>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+      } else if (pair_inside(D, ui, uj)) {
+        pair_terms<2, false>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+      } else {
+        pair_terms<2, true>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+      }
       add_pair(A, p, D, a.W, hw);
     });
     walk_neighbors<true, true>(a, m + lane, e, TPS, [&](int4 pj, float xj, float Fb) {  // H neighbors
       const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       PairAcc p;
-      if (iPd) pair_terms<1>(sF, sP, ffi.x, Fb, D, ui, uj, p);
-      else pair_terms<3>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+      const bool in = pair_inside(D, ui, uj);
+      if (iPd) {
+        if (in) pair_terms<1, false>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+        else pair_terms<1, true>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+      } else {
+        if (in) pair_terms<3, false>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+        else pair_terms<3, true>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+      }
       add_pair(A, p, D, a.W * xj, hw * xj);
     });
   }
