@@ -181,14 +181,16 @@ def nucleus_lattice(cells: int, seed: int = 3):
                          seed=seed)
 
 
-def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0):
+def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0, polish_cap: int = 0):
     """Wall time of a2c_gpp_minimize to gatol in FP64 and in mixed precision
     -- the mixed form alone and the mixed form followed by the FP64 polish --
     and the mixed results' distance from the FP64 minimum.  With fp64_cap >
     0 the FP64 run stops after fp64_cap iterations (the full run is too long
     for one GPU session); its time to minimum is then extrapolated as its
     measured seconds per iteration times the iterations the mixed run with
-    polish needed, and labelled so."""
+    polish needed, and labelled so.  With polish_cap > 0 the FP64 polish
+    gets at most polish_cap iterations (the mixed phase is the same
+    deterministic trajectory as the run without polish)."""
     import numpy as np
 
     import a2c_gb300 as A
@@ -209,9 +211,12 @@ def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0):
         t64 = time.perf_counter() - t0
         g.set_precision("mixed")
         runs = {}
-        for name, polish in (("mixed", 1), ("mixed_no_polish", 0)):
+        for name, polish in (("mixed_no_polish", 0), ("mixed", 1)):
+            kwr = dict(kw)
+            if polish and polish_cap:
+                kwr["max_it"] = runs["mixed_no_polish"][0].iters + polish_cap
             t0 = time.perf_counter()
-            r = g.minimize(X, polish=polish, **kw)
+            r = g.minimize(X, polish=polish, **kwr)
             runs[name] = (r, time.perf_counter() - t0)
         g.set_precision("fp64")
         f64_at, g64_at = {}, {}
@@ -725,6 +730,8 @@ def main():
     ap.add_argument("--case-tps", type=int, default=0, help="threads per site in the profile case (0 = library)")
     ap.add_argument("--ttm-fp64-cap", type=int, default=0,
                     help="stop the FP64 time-to-minimum run after this many iterations (0 = run to the end)")
+    ap.add_argument("--ttm-polish-cap", type=int, default=0,
+                    help="at most this many FP64 polish iterations after the mixed phase (0 = no cap)")
     ap.add_argument("--dmd-cells", type=int, default=48, help="coupled-DMD slab edge in cells")
     ap.add_argument("--dmd-steps", type=int, default=100, help="coupled-DMD outer steps")
     ap.add_argument("--dmd-ref-steps", type=int, default=10, help="outer steps of the reduced FP64/mixed comparison")
@@ -739,7 +746,7 @@ def main():
         return run_batch_case(args)
     if args.case == "ttm":
         print(json.dumps({"time_to_minimum": time_to_minimum(args.ttm_cells, 1e-6, dist_env()[2],
-                                                             args.ttm_fp64_cap)}))
+                                                             args.ttm_fp64_cap, args.ttm_polish_cap)}))
         return 0
     if args.warmup < 3:
         args.warmup = 3
