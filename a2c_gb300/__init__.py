@@ -200,6 +200,31 @@ class Gpp:
         N.check(self._L.a2c_gpp_autotune(self._h, int(reps), C.byref(t), ms), "a2c_gpp_autotune")
         return t.value, {k: float(v) for k, v in zip((1, 2, 4, 8), ms)}
 
+    def snapshot_async(self, desc, frame: int, time: float, X0=None, gamma=None, siteid=None, tag=None) -> None:
+        """Writes the context's current state (a2c_gpp_snapshot_async)."""
+        X0, gamma = _opt(X0, np.float64, 4 * self.N), _opt(gamma, np.float64, self.nH)
+        siteid, tag = _opt(siteid, np.int8, self.N), _opt(tag, np.int8, self.N)
+        self._snap_desc = desc
+        N.check(self._L.a2c_gpp_snapshot_async(self._h, C.byref(desc), int(frame), float(time),
+                                               N.ptr(X0) if X0 is not None else None,
+                                               N.ptr(gamma) if gamma is not None else None,
+                                               N.ptr(siteid) if siteid is not None else None,
+                                               N.ptr(tag) if tag is not None else None), "a2c_gpp_snapshot_async")
+
+    def snapshot_wait(self) -> None:
+        N.check(self._L.a2c_gpp_snapshot_wait(self._h), "a2c_gpp_snapshot_wait")
+
+    def set_neighbor_skin(self, skin: float) -> None:
+        N.check(self._L.a2c_gpp_set_neighbor_skin(self._h, float(skin)), "a2c_gpp_set_neighbor_skin")
+
+    def update_neighbors(self, X) -> tuple[int, bool]:
+        """Lists at X through the skin path: (max neighbors, whether the
+        candidate lists were rebuilt)."""
+        m, r = C.c_int(), C.c_int()
+        N.check(self._L.a2c_gpp_update_neighbors(self._h, N.ptr(_f64(X, 4 * self.N)), C.byref(m), C.byref(r)),
+                "a2c_gpp_update_neighbors")
+        return m.value, bool(r.value)
+
     def minimize(self, X, **kw) -> LbfgsResult:
         lp = N.LbfgsParams()
         self._L.a2c_lbfgs_default_params(C.byref(lp))
@@ -238,13 +263,15 @@ class Gpp:
         return xo
 
     def dmd_run(self, X, xH, gamma, full_H, bd_sites, surf_sites, nsteps: int, *, dt: float, nu: float, Qm: float,
-                x_bd: float, gamma_bd: float, xLb: float = 1e-3, xUb: float = 1.0 - 1e-16, **lbfgs) -> dict:
+                x_bd: float, gamma_bd: float, xLb: float = 1e-3, xUb: float = 1.0 - 1e-16,
+                neighbor_update: bool = False, **lbfgs) -> dict:
         """nsteps DMD outer steps on the device (a2c_gpp_dmd_run)."""
         dp = N.DmdParams()
         self._L.a2c_lbfgs_default_params(C.byref(dp.lbfgs))
         for k, v in lbfgs.items():
             setattr(dp.lbfgs, k, v)
         dp.dt, dp.nu, dp.Qm, dp.xLb, dp.xUb, dp.x_bd, dp.gamma_bd = dt, nu, Qm, xLb, xUb, x_bd, gamma_bd
+        dp.neighbor_update = int(bool(neighbor_update))
         X = _f64(X, 4 * self.N).copy()
         xH = _f64(xH, self.nH).copy()
         g = _f64(gamma, self.nH).copy()
@@ -387,6 +414,44 @@ class Batch:
         """Per-instance views of a concatenated 4N array."""
         X = np.asarray(X)
         return [X[4 * self.offsets[k]:4 * self.offsets[k + 1]] for k in range(self.B)]
+
+
+def snapshot_desc(prefix: str, *, fmt: str = "both", precision: int = 2, box=(0.0, 0.0, 0.0), origin=(0.0, 0.0, 0.0),
+                  periodic=(0, 0, 0)):
+    """Descriptor of a snapshot series (a2c_snapshot_desc): files
+    <prefix>_L0_<frame>.vtp / .xyz and <prefix>_L0.pvd."""
+    d = N.SnapshotDesc()
+    d._prefix = str(prefix).encode()  # keeps the bytes alive with the descriptor
+    d.prefix = d._prefix
+    d.format = {"vtp": 1, "xyz": 2, "both": 3}[fmt]
+    d.precision = int(precision)
+    for k in range(3):
+        d.axes[4 * k] = float(box[k])
+        d.origin[k] = float(origin[k])
+        d.periodic[k] = int(bool(periodic[k]))
+    return d
+
+
+def snapshot_begin(desc) -> None:
+    N.check(N.lib().a2c_snapshot_begin(C.byref(desc)), "a2c_snapshot_begin")
+
+
+def _opt(a, dtype, n):
+    return None if a is None else np.ascontiguousarray(a, dtype=dtype).reshape(-1)[:n].copy()
+
+
+def snapshot_write(desc, frame: int, time: float, nPd: int, nH: int, X, xH, X0=None, gamma=None, siteid=None,
+                   tag=None) -> None:
+    n = nPd + nH
+    X = _f64(X, 4 * n)
+    xH = _f64(xH, nH)
+    X0, gamma = _opt(X0, np.float64, 4 * n), _opt(gamma, np.float64, nH)
+    siteid, tag = _opt(siteid, np.int8, n), _opt(tag, np.int8, n)
+    N.check(N.lib().a2c_snapshot_write(C.byref(desc), int(frame), float(time), int(nPd), int(nH), N.ptr(X),
+                                       N.ptr(X0) if X0 is not None else None, N.ptr(xH),
+                                       N.ptr(gamma) if gamma is not None else None,
+                                       N.ptr(siteid) if siteid is not None else None,
+                                       N.ptr(tag) if tag is not None else None), "a2c_snapshot_write")
 
 
 def restart_write(path: str, nPd: int, nH: int, X, xH, gamma, full_H, step: int = 0, time: float = 0.0) -> None:

@@ -50,6 +50,7 @@ class LbfgsParams(C.Structure):
         ("m", C.c_int), ("max_it", C.c_int), ("max_fev", C.c_int), ("max_ls", C.c_int),
         ("gatol", C.c_double), ("c1", C.c_double), ("init_step", C.c_double), ("sigma_lb", C.c_double),
         ("f_noise", C.c_double), ("polish", C.c_int), ("stall_window", C.c_int), ("stall_rtol", C.c_double),
+        ("max_step", C.c_double),
     ]
 
 
@@ -64,9 +65,15 @@ class LatticeSpec(C.Structure):
     ]
 
 
+class SnapshotDesc(C.Structure):
+    _fields_ = [("prefix", C.c_char_p), ("format", C.c_int), ("precision", C.c_int), ("axes", C.c_double * 9),
+                ("origin", C.c_double * 3), ("periodic", C.c_int * 3)]
+
+
 class DmdParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("nu", C.c_double), ("Qm", C.c_double), ("xLb", C.c_double),
-                ("xUb", C.c_double), ("x_bd", C.c_double), ("gamma_bd", C.c_double), ("lbfgs", LbfgsParams)]
+                ("xUb", C.c_double), ("x_bd", C.c_double), ("gamma_bd", C.c_double), ("lbfgs", LbfgsParams),
+                ("neighbor_update", C.c_int)]
 
 
 _lib = None
@@ -101,6 +108,12 @@ def lib() -> C.CDLL:
         "a2c_gpp_get_state": (I, [P, P]),
         "a2c_gpp_build_neighbors": (I, [P, P, C.POINTER(I)]),
         "a2c_gpp_neighbor_total": (I, [P, I, C.POINTER(C.c_int64)]),
+        "a2c_gpp_set_neighbor_skin": (I, [P, D]),
+        "a2c_snapshot_begin": (I, [C.POINTER(SnapshotDesc)]),
+        "a2c_snapshot_write": (I, [C.POINTER(SnapshotDesc), I, D, I, I, P, P, P, P, P, P]),
+        "a2c_gpp_snapshot_async": (I, [P, C.POINTER(SnapshotDesc), I, D, P, P, P, P]),
+        "a2c_gpp_snapshot_wait": (I, [P]),
+        "a2c_gpp_update_neighbors": (I, [P, P, C.POINTER(I), C.POINTER(I)]),
         "a2c_gpp_get_neighbors": (I, [P, I, P, P]),
         "a2c_gpp_get_shell_counts": (I, [P, P]),
         "a2c_gpp_eval": (I, [P, P, C.POINTER(D), P]),
@@ -148,7 +161,8 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_destroy", "a2c_gpp_stream", "a2c_gpp_set_precision", "a2c_gpp_synchronize",
             "a2c_gpp_set_threads_per_site", "a2c_gpp_set_occupancy",
             "a2c_gpp_get_occupancy", "a2c_gpp_set_state", "a2c_gpp_get_state", "a2c_gpp_build_neighbors",
-            "a2c_gpp_neighbor_total", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
+            "a2c_gpp_neighbor_total", "a2c_gpp_set_neighbor_skin", "a2c_gpp_update_neighbors", "a2c_snapshot_begin",
+            "a2c_snapshot_write", "a2c_gpp_snapshot_async", "a2c_gpp_snapshot_wait", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
             "a2c_gpp_eval_device", "a2c_gpp_profile_eval", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
             "a2c_gpp_chem_potential", "a2c_gpp_minimize_stats", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",
             "a2c_lattice_fcc", "a2c_gpp_peak_flops", "a2c_gpp_dmd_run", "a2c_restart_write", "a2c_restart_read",

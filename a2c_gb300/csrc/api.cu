@@ -6,6 +6,8 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "internal.cuh"
@@ -97,6 +99,39 @@ void free_hscratch(a2c_gpp_ctx *c, double *gamma, double *send, double *x, int *
   cudaFreeAsync(full, c->stream);
 }
 
+// The snapshot in flight: pinned copies of the state, the host-side
+// arrays, and the writer thread.
+struct SnapJob {
+  std::thread th;
+  double *pinned = nullptr;
+  size_t cap = 0;
+  cudaEvent_t ev = nullptr;
+  a2c_status result = A2C_OK;
+  std::string prefix;
+  a2c_snapshot_desc desc{};
+  std::vector<double> X0, gamma;
+  std::vector<signed char> siteid, tag;
+};
+
+a2c_status snapshot_join(a2c_gpp_ctx *c) {
+  SnapJob *j = (SnapJob *)c->snap;
+  if (!j) return A2C_OK;
+  if (j->th.joinable()) j->th.join();
+  const a2c_status r = j->result;
+  j->result = A2C_OK;
+  return r;
+}
+
+void snapshot_release(a2c_gpp_ctx *c) {
+  SnapJob *j = (SnapJob *)c->snap;
+  if (!j) return;
+  snapshot_join(c);
+  if (j->pinned) cudaFreeHost(j->pinned);
+  if (j->ev) cudaEventDestroy(j->ev);
+  delete j;
+  c->snap = nullptr;
+}
+
 __global__ void k_fill(double *p, int64_t n, double v) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -132,6 +167,7 @@ void a2c_lbfgs_default_params(a2c_lbfgs_params *p) {
   p->polish = 1;
   p->stall_window = 50;
   p->stall_rtol = 0.0;
+  p->max_step = 0.25;
 }
 
 const char *a2c_status_string(a2c_status s) {
@@ -199,12 +235,14 @@ a2c_status a2c_gpp_create(const a2c_gpp_params *p, a2c_gpp_ctx **out) {
 a2c_status a2c_gpp_destroy(a2c_gpp_ctx *c) {
   if (!c) return A2C_OK;
   DeviceGuard g(c->device);
+  snapshot_release(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
   mixed_free(c);
   lbfgs_free(c);
   for (void *p : {(void *)c->d_X, (void *)c->d_G, (void *)c->d_occ, (void *)c->d_rho, (void *)c->d_Fp,
                   (void *)c->d_Vs, (void *)c->d_Ss, (void *)c->d_red, (void *)c->d_status, (void *)c->d_off,
-                  (void *)c->d_nbr, (void *)c->d_npd, (void *)c->d_shell, (void *)c->d_hh1_off, (void *)c->d_hh1})
+                  (void *)c->d_nbr, (void *)c->d_npd, (void *)c->d_shell, (void *)c->d_hh1_off, (void *)c->d_hh1,
+                  (void *)c->d_ext_off, (void *)c->d_ext_nbr, (void *)c->d_xref})
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -324,6 +362,100 @@ a2c_status a2c_gpp_build_neighbors(a2c_gpp_ctx *c, const double *X, int *max_nei
   c->has_neighbors = false;
   c->has_density = false;
   A2C_TRY(build_neighbors_device(c, X));
+  c->has_neighbors = true;
+  if (max_neighbors) *max_neighbors = c->max_neighbors;
+  return finish(c);
+}
+
+// Skin lists (findLocalNeighbors' refilter of the extended lists,
+// minimizer.cpp:833-1144, on the device).
+a2c_status a2c_gpp_snapshot_async(a2c_gpp_ctx *c, const a2c_snapshot_desc *d, int frame, double time,
+                                  const double *X0, const double *gamma, const signed char *siteid,
+                                  const signed char *tag) {
+  if (!c || !d || !d->prefix || frame < 0 || d->format < 1 || d->format > 3 || d->precision < 0 || d->precision > 2)
+    return A2C_ERR_INVALID;
+  if (!c->has_state) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  if (!c->snap) c->snap = new (std::nothrow) SnapJob();
+  SnapJob *j = (SnapJob *)c->snap;
+  if (!j) return A2C_ERR_NOMEM;
+  const a2c_status prev = snapshot_join(c);
+  const int64_t N = c->N, nPd = c->p.nPd, nH = c->p.nH;
+  const size_t need = (size_t)(4 * N + nH);
+  if (need > j->cap) {
+    if (j->pinned) cudaFreeHost(j->pinned);
+    j->pinned = nullptr;
+    j->cap = 0;
+    if (cudaMallocHost((void **)&j->pinned, sizeof(double) * std::max<size_t>(need, 1)) != cudaSuccess)
+      return A2C_ERR_NOMEM;
+    j->cap = need;
+  }
+  if (!j->ev) A2C_CUDA(cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming));
+  if (N > 0) A2C_CUDA(cudaMemcpyAsync(j->pinned, c->d_X, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, c->stream));
+  if (nH > 0)
+    A2C_CUDA(cudaMemcpyAsync(j->pinned + 4 * N, c->d_occ + nPd, sizeof(double) * nH, cudaMemcpyDeviceToHost,
+                             c->stream));
+  A2C_CUDA(cudaEventRecord(j->ev, c->stream));
+  j->prefix = d->prefix;
+  j->desc = *d;
+  j->desc.prefix = j->prefix.c_str();
+  j->X0.assign(X0 ? X0 : nullptr, X0 ? X0 + 4 * N : nullptr);
+  j->gamma.assign(gamma ? gamma : nullptr, gamma ? gamma + nH : nullptr);
+  j->siteid.assign(siteid ? siteid : nullptr, siteid ? siteid + N : nullptr);
+  j->tag.assign(tag ? tag : nullptr, tag ? tag + N : nullptr);
+  const int dev = c->device;
+  j->th = std::thread([j, dev, frame, time, nPd, nH, N]() {
+    cudaSetDevice(dev);
+    if (cudaEventSynchronize(j->ev) != cudaSuccess) {
+      j->result = A2C_ERR_CUDA;
+      return;
+    }
+    j->result = a2c_snapshot_write(&j->desc, frame, time, (int)nPd, (int)nH, j->pinned,
+                                   j->X0.empty() ? nullptr : j->X0.data(), j->pinned + 4 * N,
+                                   j->gamma.empty() ? nullptr : j->gamma.data(),
+                                   j->siteid.empty() ? nullptr : j->siteid.data(),
+                                   j->tag.empty() ? nullptr : j->tag.data());
+  });
+  return prev;
+}
+
+a2c_status a2c_gpp_snapshot_wait(a2c_gpp_ctx *c) {
+  if (!c) return A2C_ERR_INVALID;
+  return snapshot_join(c);
+}
+
+a2c_status a2c_gpp_set_neighbor_skin(a2c_gpp_ctx *c, double skin) {
+  if (!c || !(skin >= 0.0) || !std::isfinite(skin)) return A2C_ERR_INVALID;
+  for (int d = 0; d < 3; ++d)  // the minimum image must stay unique at rc + skin
+    if (c->p.periodic[d] && !(c->p.box[d] > 2.0 * (c->p.rc + skin))) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  if (skin > 0.0 && !c->d_ext_off) {
+    A2C_TRY(dalloc(&c->d_ext_off, c->N + 1));
+    A2C_TRY(dalloc(&c->d_xref, 4 * c->N));
+  }
+  c->skin = skin;
+  c->has_ext = false;
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_update_neighbors(a2c_gpp_ctx *c, const double *X, int *max_neighbors, int *rebuilt) {
+  if (!c || (!X && c->N > 0)) return A2C_ERR_INVALID;
+  if (!(c->skin > 0.0)) {
+    if (rebuilt) *rebuilt = 1;
+    return a2c_gpp_build_neighbors(c, X, max_neighbors);
+  }
+  DeviceGuard g(c->device);
+  for (int64_t t = 0; t < 4 * c->N; ++t)
+    if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
+  for (int d = 0; d < 3; ++d)
+    if (c->p.periodic[d])
+      for (int64_t s = 0; s < c->N; ++s)
+        if (X[4 * s + d] < -0.5 * c->p.box[d] || X[4 * s + d] > 1.5 * c->p.box[d]) return A2C_ERR_INVALID;
+  A2C_TRY(copy_in(c, c->d_X, X, 4 * c->N));
+  c->has_state = true;
+  c->has_neighbors = false;
+  c->has_density = false;
+  A2C_TRY(update_neighbors_device(c, X, rebuilt));
   c->has_neighbors = true;
   if (max_neighbors) *max_neighbors = c->max_neighbors;
   return finish(c);
@@ -761,9 +893,22 @@ a2c_status a2c_gpp_dmd_run(a2c_gpp_ctx *c, double *X, double *xH, double *gamma,
              cudaMemcpyAsync(dsurf, flags.data(), sizeof(int) * nH, cudaMemcpyHostToDevice, st)))
     s = A2C_ERR_CUDA;
   c->has_state = true;
+  std::vector<double> hX;
   for (int k = 0; k < nsteps && !s; ++k) {
     double f = 0.0, gn = 0.0;
     int it = 0, fev = 0, why = 0;
+    if (k > 0 && dp->neighbor_update) {  // findNeighbors + findLocalNeighbors at the current positions
+      if (c->skin > 0.0) {
+        s = update_neighbors_device(c, nullptr, nullptr);
+      } else {
+        hX.resize((size_t)(4 * c->N));
+        if (cudaMemcpyAsync(hX.data(), c->d_X, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToHost, st) ||
+            cudaStreamSynchronize(st))
+          s = A2C_ERR_CUDA;
+        if (!s) s = build_neighbors_device(c, hX.data());
+      }
+      if (s) break;
+    }
     s = lbfgs_minimize(c, c->d_X, &dp->lbfgs, &f, &it, &fev, &gn, &why);  // minimizer.cpp:548
     if (!s) s = launch_density64(c, c->d_X);                              // minimizer.cpp:607-633
     if (!s) s = launch_chem64(c, c->d_X, dp->gamma_bd, dsend, dfull);     // minimizer.cpp:658-789

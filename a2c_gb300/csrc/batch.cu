@@ -48,6 +48,7 @@ enum : int { kPhaseMixed = 0, kPhaseFp64 = 1 };
 struct Inst {
   double f, fn, alpha, amax, gnorm, coef, gam_num, gam_den, f_noise, stall_rtol, mixed_gnorm;
   int state, phase, npairs, head, it, fev, ls, why, copy, steep, nhist, it0, mixed_iters, fp64_iters;
+  int fresh;  // a new direction awaits its first trial step length
 };
 
 struct Chunk {
@@ -60,7 +61,7 @@ struct Chunk {
 struct Cfg {
   int B, m, ring, max_it, max_fev, max_ls, polish, W;
   int64_t nec, nsc, n;  // element chunks, site chunks, vector length
-  double gatol, c1, init_step, lb;
+  double gatol, c1, init_step, lb, max_step;
   double fn_mixed, fn_fp64, st_mixed, st_fp64;
 };
 
@@ -415,7 +416,7 @@ __global__ void __launch_bounds__(kBlk) k_finish(Dev D, Cfg cf) {
   const int slp = slot(I.head, 0, cf.ring);
   const double cp = I.coef, sc = -cf.init_step / I.amax;
   const double *Sp = D.S + (size_t)slp * cf.n;
-  double s = 0.0;
+  double s = 0.0, mx = 0.0;
   for (int i = threadIdx.x; i < ch.len; i += kBlk) {
     const int64_t t = ch.start + i;
     double v;
@@ -428,9 +429,14 @@ __global__ void __launch_bounds__(kBlk) k_finish(Dev D, Cfg cf) {
     }
     D.d[t] = v;
     s += D.g[t] * v;
+    mx = fmax(mx, fabs(v));
   }
   s = bred<false>(s, sh);
-  if (threadIdx.x == 0) D.part[3 * cf.nec + c] = s;
+  mx = bred<true>(mx, sh);
+  if (threadIdx.x == 0) {
+    D.part[3 * cf.nec + c] = s;
+    D.part[cf.nec + c] = mx;  // the slot of max |pg|, read before this kernel
+  }
   A2C_ECHUNKS_END
 }
 
@@ -451,18 +457,37 @@ __global__ void __launch_bounds__(kBlk) k_dir_end(Dev D, Cfg cf) {
   }
   I.alpha = 1.0;
   I.ls = 0;
+  I.fresh = 1;
   I.state = kLineSearch;
 }
 
 __global__ void __launch_bounds__(kBlk) k_steep(Dev D, Cfg cf) {
+  __shared__ double sh[kBlk / 32];
   A2C_ECHUNKS(D)
   if (I.steep != 2) continue;
   const double sc = -cf.init_step / I.amax;
+  double mx = 0.0;
   for (int i = threadIdx.x; i < ch.len; i += kBlk) {
     const int64_t t = ch.start + i;
-    D.d[t] = D.pg[t] * sc;
+    const double v = D.pg[t] * sc;
+    D.d[t] = v;
+    mx = fmax(mx, fabs(v));
   }
+  mx = bred<true>(mx, sh);
+  if (threadIdx.x == 0) D.part[cf.nec + c] = mx;
   A2C_ECHUNKS_END
+}
+
+// first trial step length: min(1, max_step / max|d|)
+__global__ void __launch_bounds__(kBlk) k_alpha0(Dev D, Cfg cf) {
+  __shared__ double sh[kBlk / 32];
+  const int b = blockIdx.x;
+  Inst &I = D.st[b];
+  if (I.state != kLineSearch || !I.fresh) return;
+  const double dmax = chunk_max(D.part + cf.nec, D.ecb[b], D.ecb[b + 1], sh);
+  if (threadIdx.x != 0) return;
+  I.fresh = 0;
+  if (cf.max_step > 0.0 && dmax > cf.max_step) I.alpha = cf.max_step / dmax;
 }
 
 // ------------------------------------------------------------ trial / decide
@@ -783,6 +808,7 @@ a2c_status tick(a2c_gpp_batch *b, const Dev &D, const Cfg &cf, int tps) {
   k_finish<<<ge, kBlk, 0, s>>>(D, cf);
   k_dir_end<<<B, kBlk, 0, s>>>(D, cf);
   k_steep<<<ge, kBlk, 0, s>>>(D, cf);
+  k_alpha0<<<B, kBlk, 0, s>>>(D, cf);
   A2C_TRY(plan(b, D));
   k_trial<<<ge, kBlk, 0, s>>>(D, cf);
   A2C_TRY(eval_lists(b, b->xn, b->gn, tps));
@@ -1116,6 +1142,7 @@ a2c_status a2c_gpp_batch_minimize(a2c_gpp_batch *b, double *X, const a2c_lbfgs_p
   cf.c1 = lp->c1;
   cf.init_step = lp->init_step;
   cf.lb = lp->sigma_lb;
+  cf.max_step = lp->max_step;
   cf.fn_mixed = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-7;
   cf.fn_fp64 = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-14;
   cf.st_mixed = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-10;

@@ -82,11 +82,19 @@ struct a2c_gpp_ctx {
   int *d_hh1;
   int64_t hh1_cap, hh1_total;
   int max_neighbors;
+  // skin lists: candidates at rc + skin and the positions they were built at
+  double skin;
+  bool has_ext;
+  int64_t *d_ext_off;  // N+1
+  uint32_t *d_ext_nbr;
+  int64_t ext_cap, ext_total;
+  double *d_xref;      // 4N
   // host staging
   double *h_pinned;
   int64_t h_pinned_n;
   a2c::Mixed *mixed;
   a2c::Lbfgs *lbfgs;
+  void *snap;  // the snapshot in flight (api.cu)
   int last_mixed_iters, last_fp64_iters;
   double last_mixed_gnorm;
 };
@@ -130,6 +138,9 @@ a2c_status check_status_word(a2c_gpp_ctx *c);
 
 // k_neighbors.cu
 a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X);
+// skin path (positions in c->d_X; h_X may be null): rebuild the extended
+// lists if needed, then re-filter at rc
+a2c_status update_neighbors_device(a2c_gpp_ctx *c, const double *h_X, int *rebuilt);
 
 // k_mixed.cu
 // ev: optional 5 events recorded before the first launch and after each

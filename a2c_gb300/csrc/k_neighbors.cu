@@ -10,6 +10,14 @@
 // image multiplier m = -rint((q_j - q_i)/L) is fixed at build time and
 // stored in the entry's top bits, as the reference holds its lists fixed
 // through a solve.
+//
+// Skin (Verlet) lists: with a skin s > 0 the cell-list build makes extended
+// candidate lists at rc + s (findNeighbors' _ext lists) and the lists at rc
+// are re-filtered from them on the device with the same acceptance test
+// (findLocalNeighbors, minimizer.cpp:833-1144).  While no site has moved
+// more than s/2 since the extended build, every pair now within rc was
+// within rc + s then, and filtering each sorted extended list in order gives
+// exactly the lists a full build would.
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
@@ -114,6 +122,24 @@ __device__ __forceinline__ void for_candidates(const GridArgs &g, const int64_t 
   }
 }
 
+// Candidate sources: the 27 cells around the site, or its extended list.
+struct CellSrc {
+  const int64_t *cstart;
+  const int *items;
+  template <class Fn>
+  __device__ __forceinline__ void each(const GridArgs &g, int64_t i, Fn fn) const {
+    for_candidates(g, cstart, items, i, fn);
+  }
+};
+struct ExtSrc {
+  const int64_t *off;
+  const uint32_t *nbr;
+  template <class Fn>
+  __device__ __forceinline__ void each(const GridArgs &, int64_t i, Fn fn) const {
+    for (int64_t t = off[i]; t < off[i + 1]; ++t) fn((int64_t)(nbr[t] & kIdMask));
+  }
+};
+
 __global__ void k_cell_count(GridArgs g, int *cell, int *ccount) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= g.N) return;
@@ -130,15 +156,16 @@ __global__ void k_cell_fill(GridArgs g, const int *cell, const int64_t *cstart, 
   items[cstart[c] + slot] = (int)s;
 }
 
-__global__ void __launch_bounds__(kBlock) k_nbr_count(GridArgs g, const int64_t *cstart, const int *items,
-                                                      int64_t *count, int *npd, int64_t *hh1count, int *shell,
-                                                      int *status) {
+// Counts per site; npd, shell and hh1count may be null (extended lists).
+template <class Src>
+__global__ void __launch_bounds__(kBlock) k_nbr_count(GridArgs g, Src src, int64_t *count, int *npd,
+                                                      int64_t *hh1count, int *shell, int *status) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.N) return;
   int64_t n = 0, nP = 0, n1 = 0;
   int sh[3] = {0, 0, 0};
   const bool iPd = i < g.nPd;
-  for_candidates(g, cstart, items, i, [&](int64_t j) {
+  src.each(g, i, [&](int64_t j) {
     uint32_t e;
     double d2;
     if (!pair_test(g, i, j, e, d2)) return;
@@ -156,25 +183,28 @@ __global__ void __launch_bounds__(kBlock) k_nbr_count(GridArgs g, const int64_t 
     }
   });
   count[i] = n;
-  npd[i] = (int)nP;
+  if (npd) npd[i] = (int)nP;
   if (iPd) {
-    shell[3 * i] = sh[0];
-    shell[3 * i + 1] = sh[1];
-    shell[3 * i + 2] = sh[2];
-  } else {
+    if (shell) {
+      shell[3 * i] = sh[0];
+      shell[3 * i + 1] = sh[1];
+      shell[3 * i + 2] = sh[2];
+    }
+  } else if (hh1count) {
     hh1count[i - g.nPd] = n1;
   }
   if (n > kMaxPerSite) atomicOr(status, kStatusOverflow);
 }
 
-__global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, const int64_t *cstart, const int *items,
-                                                     const int64_t *off, uint32_t *nbr, const int64_t *hh1_off,
-                                                     int *hh1, int *status) {
+// Fills the lists (sorted by id); hh1 may be null (extended lists).
+template <class Src>
+__global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, Src src, const int64_t *off, uint32_t *nbr,
+                                                     const int64_t *hh1_off, int *hh1, int *status) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.N) return;
   const int64_t b = off[i], e = off[i + 1];
   int64_t w = b;
-  for_candidates(g, cstart, items, i, [&](int64_t j) {
+  src.each(g, i, [&](int64_t j) {
     uint32_t en;
     double d2;
     if (!pair_test(g, i, j, en, d2)) return;
@@ -196,7 +226,7 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, const int64_t *
     }
     nbr[u + 1] = v;
   }
-  if (i >= g.nPd) {
+  if (hh1 && i >= g.nPd) {
     const int64_t h = i - g.nPd;
     int64_t w1 = hh1_off[h];
     for (int64_t t = b; t < e; ++t) {
@@ -216,6 +246,14 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, const int64_t *
 __global__ void k_max_count(const int64_t *count, int64_t n, int *out) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s < n) atomicMax(out, (int)count[s]);
+}
+
+// flag = 1 if any site moved more than `lim` from its reference position
+__global__ void k_moved(const double *X, const double *Xref, int64_t n, double lim2, int *flag) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double dx = X[4 * s] - Xref[4 * s], dy = X[4 * s + 1] - Xref[4 * s + 1], dz = X[4 * s + 2] - Xref[4 * s + 2];
+  if (dx * dx + dy * dy + dz * dz > lim2) atomicOr(flag, 1);
 }
 
 template <class T>
@@ -239,18 +277,18 @@ struct DevBuf {
   }
 };
 
-}  // namespace
-
-a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X) {
+// Cell grid for cutoff `cut` (cells at least `cut` wide).  h_X (host
+// positions) gives the extents of free directions; with h_X null (a list
+// re-filter, which uses no cells) they are left nominal.
+int64_t make_grid(const a2c_gpp_ctx *c, const double *h_X, double cut, GridArgs &g) {
   const int64_t N = c->N;
   const a2c_gpp_params &p = c->p;
-  cudaStream_t st = c->stream;
-  GridArgs g{};
+  g = GridArgs{};
   g.N = N;
   g.nPd = p.nPd;
   g.X = c->d_X;
-  g.rc = p.rc;
-  g.rc2 = p.rc * p.rc;
+  g.rc = cut;
+  g.rc2 = cut * cut;
   g.A75 = p.a_Pd * p.a_Pd * 0.75;
   g.A125 = p.a_Pd * p.a_Pd * 1.25;
   int64_t ncell = 1;
@@ -261,6 +299,9 @@ a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X) {
     if (g.periodic[d]) {
       g.lo[d] = 0.0;
       ext = p.box[d];
+    } else if (!h_X) {
+      g.lo[d] = 0.0;
+      ext = cut;
     } else {
       double lo = HUGE_VAL, hi = -HUGE_VAL;
       for (int64_t s = 0; s < N; ++s) {
@@ -271,7 +312,7 @@ a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X) {
       g.lo[d] = lo;
       ext = hi - lo;
     }
-    int n = (int)std::floor(ext / (p.rc + 1e-6));
+    int n = (int)std::floor(ext / (cut + 1e-6));
     if (n < 1) n = 1;
     if (n > 512) n = 512;
     g.n[d] = n;
@@ -279,22 +320,97 @@ a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X) {
     g.scan_all[d] = (g.periodic[d] && n < 3) || n < 3 ? 1 : 0;
     ncell *= n;
   }
-  A2C_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
+  return ncell;
+}
 
-  DevBuf cell(st), ccount(st), cstart(st), cfill(st), items(st), counts(st), hh1c(st), maxc(st);
+a2c_status grow(uint32_t **p, int64_t *cap, int64_t need) {
+  if (need <= *cap) return A2C_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  if (cudaMalloc(p, sizeof(uint32_t) * std::max<int64_t>(need, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
+  *cap = need;
+  return A2C_OK;
+}
+a2c_status grow(int **p, int64_t *cap, int64_t need) {
+  if (need <= *cap) return A2C_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  if (cudaMalloc(p, sizeof(int) * std::max<int64_t>(need, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
+  *cap = need;
+  return A2C_OK;
+}
+
+// Count, scan, allocate and fill from one candidate source.  ext = true:
+// the extended lists (no Pd head counts, shells or HH1).
+template <class Src>
+a2c_status make_lists(a2c_gpp_ctx *c, const GridArgs &g, Src src, bool ext) {
+  const int64_t N = c->N;
+  const a2c_gpp_params &p = c->p;
+  cudaStream_t st = c->stream;
+  DevBuf counts(st), hh1c(st), maxc(st);
+  A2C_CUDA(cudaMallocAsync(&counts.p, sizeof(int64_t) * (N + 1), st));
+  A2C_CUDA(cudaMallocAsync(&hh1c.p, sizeof(int64_t) * (p.nH + 1), st));
+  A2C_CUDA(cudaMallocAsync(&maxc.p, sizeof(int), st));
+  A2C_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int64_t) * (N + 1), st));
+  A2C_CUDA(cudaMemsetAsync(hh1c.p, 0, sizeof(int64_t) * (p.nH + 1), st));
+  A2C_CUDA(cudaMemsetAsync(maxc.p, 0, sizeof(int), st));
+  int64_t *off = ext ? c->d_ext_off : c->d_off;
+  if (N > 0) {
+    k_nbr_count<Src><<<grid_for(N, kBlock), kBlock, 0, st>>>(g, src, (int64_t *)counts.p, ext ? nullptr : c->d_npd,
+                                                             ext ? nullptr : (int64_t *)hh1c.p,
+                                                             ext ? nullptr : c->d_shell, c->d_status);
+    A2C_CUDA(cudaGetLastError());
+    k_max_count<<<grid_for(N, 256), 256, 0, st>>>((const int64_t *)counts.p, N, (int *)maxc.p);
+    A2C_CUDA(cudaGetLastError());
+  }
+  A2C_TRY(scan_exclusive((const int64_t *)counts.p, off, N + 1, st));
+  if (!ext) A2C_TRY(scan_exclusive((const int64_t *)hh1c.p, c->d_hh1_off, (int64_t)p.nH + 1, st));
+  int64_t total = 0, total1 = 0;
+  int maxn = 0, stat = 0;
+  A2C_CUDA(cudaMemcpyAsync(&total, off + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  if (!ext) A2C_CUDA(cudaMemcpyAsync(&total1, c->d_hh1_off + p.nH, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaMemcpyAsync(&maxn, maxc.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaMemcpyAsync(&stat, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaStreamSynchronize(st));
+  if (stat & kStatusOverflow) return A2C_ERR_NEIGHBOR_OVERFLOW;
+  if (ext) {
+    A2C_TRY(grow(&c->d_ext_nbr, &c->ext_cap, total));
+    c->ext_total = total;
+  } else {
+    A2C_TRY(grow(&c->d_nbr, &c->nbr_cap, total));
+    A2C_TRY(grow(&c->d_hh1, &c->hh1_cap, total1));
+    c->nbr_total = total;
+    c->hh1_total = total1;
+    c->max_neighbors = maxn;
+  }
+  if (N > 0) {
+    k_nbr_fill<Src><<<grid_for(N, kBlock), kBlock, 0, st>>>(g, src, off, ext ? c->d_ext_nbr : c->d_nbr,
+                                                            c->d_hh1_off, ext ? nullptr : c->d_hh1, c->d_status);
+    A2C_CUDA(cudaGetLastError());
+  }
+  A2C_CUDA(cudaMemcpyAsync(&stat, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaStreamSynchronize(st));
+  if (stat & kStatusBadIndex) return A2C_ERR_STATE;
+  return A2C_OK;
+}
+
+// Lists (rc, or rc + skin for the extended lists) from a cell list.
+a2c_status lists_from_cells(a2c_gpp_ctx *c, const double *h_X, double cut, bool ext) {
+  const int64_t N = c->N;
+  cudaStream_t st = c->stream;
+  GridArgs g;
+  const int64_t ncell = make_grid(c, h_X, cut, g);
+  A2C_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
+  DevBuf cell(st), ccount(st), cstart(st), cfill(st), items(st);
   A2C_CUDA(cudaMallocAsync(&cell.p, sizeof(int) * std::max<int64_t>(N, 1), st));
   A2C_CUDA(cudaMallocAsync(&ccount.p, sizeof(int) * (ncell + 1), st));
   A2C_CUDA(cudaMallocAsync(&cstart.p, sizeof(int64_t) * (ncell + 1), st));
   A2C_CUDA(cudaMallocAsync(&cfill.p, sizeof(int) * (ncell + 1), st));
   A2C_CUDA(cudaMallocAsync(&items.p, sizeof(int) * std::max<int64_t>(N, 1), st));
-  A2C_CUDA(cudaMallocAsync(&counts.p, sizeof(int64_t) * (N + 1), st));
-  A2C_CUDA(cudaMallocAsync(&hh1c.p, sizeof(int64_t) * (p.nH + 1), st));
-  A2C_CUDA(cudaMallocAsync(&maxc.p, sizeof(int), st));
   A2C_CUDA(cudaMemsetAsync(ccount.p, 0, sizeof(int) * (ncell + 1), st));
   A2C_CUDA(cudaMemsetAsync(cfill.p, 0, sizeof(int) * (ncell + 1), st));
-  A2C_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int64_t) * (N + 1), st));
-  A2C_CUDA(cudaMemsetAsync(hh1c.p, 0, sizeof(int64_t) * (p.nH + 1), st));
-  A2C_CUDA(cudaMemsetAsync(maxc.p, 0, sizeof(int), st));
   if (N > 0) {
     k_cell_count<<<grid_for(N, 256), 256, 0, st>>>(g, (int *)cell.p, (int *)ccount.p);
     A2C_CUDA(cudaGetLastError());
@@ -304,49 +420,56 @@ a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X) {
     k_cell_fill<<<grid_for(N, 256), 256, 0, st>>>(g, (const int *)cell.p, (const int64_t *)cstart.p,
                                                    (int *)cfill.p, (int *)items.p);
     A2C_CUDA(cudaGetLastError());
-    k_nbr_count<<<grid_for(N, kBlock), kBlock, 0, st>>>(g, (const int64_t *)cstart.p, (const int *)items.p,
-                                                        (int64_t *)counts.p, c->d_npd, (int64_t *)hh1c.p,
-                                                        c->d_shell, c->d_status);
+  }
+  return make_lists(c, g, CellSrc{(const int64_t *)cstart.p, (const int *)items.p}, ext);
+}
+
+}  // namespace
+
+a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X) {
+  c->has_ext = false;  // a full build invalidates the extended lists
+  return lists_from_cells(c, h_X, c->p.rc, false);
+}
+
+// Skin path: rebuild the extended lists when a site has moved more than
+// skin/2 since they were built (or none exist), then re-filter at rc.
+// Positions are in c->d_X; h_X (may be null) serves the extended build's
+// free-direction extents, else it is copied from the device.
+a2c_status update_neighbors_device(a2c_gpp_ctx *c, const double *h_X, int *rebuilt) {
+  const int64_t N = c->N;
+  cudaStream_t st = c->stream;
+  bool need = !c->has_ext;
+  if (!need && N > 0) {
+    DevBuf flag(st);
+    int moved = 0;
+    A2C_CUDA(cudaMallocAsync(&flag.p, sizeof(int), st));
+    A2C_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
+    const double half = 0.5 * c->skin;
+    k_moved<<<grid_for(N, 256), 256, 0, st>>>(c->d_X, c->d_xref, N, half * half, (int *)flag.p);
     A2C_CUDA(cudaGetLastError());
-    k_max_count<<<grid_for(N, 256), 256, 0, st>>>((const int64_t *)counts.p, N, (int *)maxc.p);
-    A2C_CUDA(cudaGetLastError());
+    A2C_CUDA(cudaMemcpyAsync(&moved, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    A2C_CUDA(cudaStreamSynchronize(st));
+    need = moved != 0;
   }
-  A2C_TRY(scan_exclusive((const int64_t *)counts.p, c->d_off, N + 1, st));
-  A2C_TRY(scan_exclusive((const int64_t *)hh1c.p, c->d_hh1_off, (int64_t)p.nH + 1, st));
-  int64_t total = 0, total1 = 0;
-  int maxn = 0, stat = 0;
-  A2C_CUDA(cudaMemcpyAsync(&total, c->d_off + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  A2C_CUDA(cudaMemcpyAsync(&total1, c->d_hh1_off + p.nH, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  A2C_CUDA(cudaMemcpyAsync(&maxn, maxc.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-  A2C_CUDA(cudaMemcpyAsync(&stat, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
-  A2C_CUDA(cudaStreamSynchronize(st));
-  if (stat & kStatusOverflow) return A2C_ERR_NEIGHBOR_OVERFLOW;
-  if (total > c->nbr_cap) {
-    if (c->d_nbr) cudaFree(c->d_nbr);
-    c->d_nbr = nullptr;
-    c->nbr_cap = 0;
-    if (cudaMalloc(&c->d_nbr, sizeof(uint32_t) * std::max<int64_t>(total, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
-    c->nbr_cap = total;
+  if (need) {
+    std::vector<double> hx;
+    bool free_dim = false;
+    for (int d = 0; d < 3; ++d) free_dim = free_dim || !c->p.periodic[d];
+    if (!h_X && free_dim && N > 0) {
+      hx.resize((size_t)(4 * N));
+      A2C_CUDA(cudaMemcpyAsync(hx.data(), c->d_X, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, st));
+      A2C_CUDA(cudaStreamSynchronize(st));
+      h_X = hx.data();
+    }
+    A2C_TRY(lists_from_cells(c, h_X, c->p.rc + c->skin, true));
+    if (N > 0) A2C_CUDA(cudaMemcpyAsync(c->d_xref, c->d_X, sizeof(double) * 4 * N, cudaMemcpyDeviceToDevice, st));
+    c->has_ext = true;
   }
-  if (total1 > c->hh1_cap) {
-    if (c->d_hh1) cudaFree(c->d_hh1);
-    c->d_hh1 = nullptr;
-    c->hh1_cap = 0;
-    if (cudaMalloc(&c->d_hh1, sizeof(int) * std::max<int64_t>(total1, 1)) != cudaSuccess) return A2C_ERR_NOMEM;
-    c->hh1_cap = total1;
-  }
-  c->nbr_total = total;
-  c->hh1_total = total1;
-  c->max_neighbors = maxn;
-  if (N > 0) {
-    k_nbr_fill<<<grid_for(N, kBlock), kBlock, 0, st>>>(g, (const int64_t *)cstart.p, (const int *)items.p, c->d_off,
-                                                       c->d_nbr, c->d_hh1_off, c->d_hh1, c->d_status);
-    A2C_CUDA(cudaGetLastError());
-  }
-  A2C_CUDA(cudaMemcpyAsync(&stat, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
-  A2C_CUDA(cudaStreamSynchronize(st));
-  if (stat & kStatusBadIndex) return A2C_ERR_STATE;
-  return A2C_OK;
+  if (rebuilt) *rebuilt = need ? 1 : 0;
+  GridArgs g;
+  make_grid(c, nullptr, c->p.rc, g);  // only the cutoff and box are read on this path
+  A2C_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
+  return make_lists(c, g, ExtSrc{c->d_ext_off, c->d_ext_nbr}, false);
 }
 
 }  // namespace a2c

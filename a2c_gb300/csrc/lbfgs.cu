@@ -7,7 +7,9 @@
 //   d  = -H pg by the two-loop recursion over the last m pairs, H0 =
 //        (s.y / y.y) I; zero on the active set; with no pairs (or if d is
 //        not a descent direction) d = -pg * init_step / max|pg|
-//   backtracking projected Armijo search from alpha = 1, halving; when the
+//   backtracking projected Armijo search from alpha = min(1, max_step /
+//   max|d|) (no coordinate or width moves more than max_step in the first
+//   trial), halving; when the
 //   objective change is below its noise level (|f_new - f| <= f_noise |f|)
 //   the step is accepted by the derivative form of the Armijo test,
 //   g_new.s <= (2 c1 - 1) g.s, exact for a quadratic (the approximate-Wolfe
@@ -178,6 +180,19 @@ __global__ void __launch_bounds__(kBlock) k_trial(const double *x, const double 
   }
 }
 
+// part = (0, max |d|)
+__global__ void __launch_bounds__(kBlock) k_absmax(const double *d, int64_t n, double *part) {
+  __shared__ double sh[kBlock / 32];
+  double mx = 0.0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    mx = fmax(mx, fabs(d[t]));
+  mx = bred<true>(mx, sh);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = 0.0;
+    part[2 * blockIdx.x + 1] = mx;
+  }
+}
+
 // S = xn - x, Y = gn - g; part = (s.y, y.y)
 __global__ void __launch_bounds__(kBlock) k_pair(const double *x, const double *xn, const double *g, const double *gn,
                                                   double *S, double *Y, int64_t n, double *part) {
@@ -332,6 +347,13 @@ a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp
         steepest();
       }
       double alpha = 1.0, fn = 0.0;
+      if (lp->max_step > 0.0) {
+        double dm[2];
+        k_absmax<<<gr, kBlock, 0, st>>>(L->d, n, part);
+        k_final_sum_max<<<1, kBlock, 0, st>>>(part, gr, scal + 2);
+        A2C_TRY(fetch(scal + 2, dm, 2));
+        if (dm[1] > lp->max_step) alpha = lp->max_step / dm[1];
+      }
       bool ok = false;
       for (int ls = 0; ls < lp->max_ls; ++ls) {
         k_trial<<<gr, kBlock, 0, st>>>(L->x, L->d, L->g, alpha, lb, L->xn, n, part);

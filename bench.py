@@ -225,6 +225,7 @@ def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0, po
             f64_at[name] = fv
             g64_at[name] = float(np.linalg.norm(gv))
     out["fp64"] = {"seconds": t64, "iters": r64.iters, "nfev": r64.nfev, "reason": r64.reason, "gnorm": r64.gnorm,
+                   "sigma_range_A": [float(r64.X[3::4].min()), float(r64.X[3::4].max())],
                    "f": r64.fmin, "seconds_per_iter": t64 / max(r64.iters, 1)}
     if fp64_cap:
         need = runs["mixed_no_polish"][0].iters
@@ -237,6 +238,7 @@ def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0, po
         dq = float(np.abs(r.X.reshape(-1, 4)[:, :3] - r64.X.reshape(-1, 4)[:, :3]).max())
         ds = float(np.abs(r.X.reshape(-1, 4)[:, 3] - r64.X.reshape(-1, 4)[:, 3]).max())
         out[name] = {"seconds": t, "iters": r.iters, "mixed_iters": r.mixed_iters, "fp64_polish_iters": r.fp64_iters,
+                     "sigma_range_A": [float(r.X[3::4].min()), float(r.X[3::4].max())],
                      "mixed_phase_gnorm": r.mixed_gnorm, "nfev": r.nfev, "reason": r.reason, "gnorm": r.gnorm,
                      "fp64_gnorm_at_result": g64_at[name], "speedup_vs_fp64": t64_ref / t}
         if not fp64_cap:
@@ -523,6 +525,21 @@ def run_ours(args):
     g = A.Gpp(nPd, nH, box=box, periodic=w["periodic"], precision="mixed", device=dev)
     g.set_occupancy(xH)
     g.build_neighbors(X)
+    # neighbor lists: full cell-list build vs the skin refilter (0.5 A skin)
+    nb = {}
+    t0 = time.perf_counter()
+    g.build_neighbors(X)
+    nb["cell_build_ms"] = 1e3 * (time.perf_counter() - t0)
+    g.set_neighbor_skin(0.5)
+    t0 = time.perf_counter()
+    g.update_neighbors(X)
+    nb["skin_candidates_build_ms"] = 1e3 * (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    _, rebuilt = g.update_neighbors(X)
+    nb["skin_refilter_ms"] = 1e3 * (time.perf_counter() - t0)
+    nb["refilter_rebuilt"] = rebuilt
+    g.set_neighbor_skin(0.0)
+    g.build_neighbors(X)
     tot = {k: 0 for k in ("PdPd", "PdH", "HPd", "HH")}
     for lid, k in enumerate(tot):
         o, _ = g.neighbors(lid)
@@ -675,7 +692,7 @@ def run_ours(args):
                 "mixed_error_vs_fp64": {"free_entropy_rel": rel_f, "gradient_rel_2norm": rel_g},
                 "stages_ms_mixed": {"prep": float(np.mean(st_mixed[:, 0])), "pass1": pass1_ms, "pass2": pass2_ms,
                                     "reduce": float(np.mean(st_mixed[:, 3]))},
-                "time_to_minimum": ttm}
+                "time_to_minimum": ttm, "neighbor_lists": nb}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

@@ -96,6 +96,11 @@ typedef struct a2c_lbfgs_params {
   int stall_window; /* stop (A2C_CONVERGED_STALLED) when f fell by no more
                        than stall_rtol*|f| over this many iterations */
   double stall_rtol;/* 0 = 1e-14 (FP64) or 1e-10 (mixed phase) */
+  double max_step;  /* largest change of any coordinate or width in a first
+                       trial step [A]: the line search starts from
+                       min(1, max_step / max|d|); 0 = no cap.  Keeps widths
+                       from being carried over the binding barrier into the
+                       region where -3 kB x ln(sigma) falls without bound */
 } a2c_lbfgs_params;
 
 typedef struct a2c_gpp_ctx a2c_gpp_ctx;
@@ -148,6 +153,17 @@ a2c_status a2c_gpp_set_neighbor_lists(a2c_gpp_ctx *ctx, const double *X, const i
                                       const int *hh_idx, const int64_t *hh1_off, const int *hh1_idx,
                                       const int *PdPdnum);
 /* Sizes for a2c_gpp_get_neighbors: total entries of a list. */
+/* Skin (Verlet) lists, replacing the refilter of findNeighbors' extended
+ * lists in Minimizer::findLocalNeighbors (minimizer.cpp:833-1144).  With
+ * skin > 0, a2c_gpp_update_neighbors keeps candidate lists at rc + skin and
+ * re-filters them at rc on the device; it rebuilds the candidates (cell
+ * list) only when a site has moved more than skin/2 since they were built
+ * (*rebuilt = 1).  The lists it produces are those a2c_gpp_build_neighbors
+ * would build at X.  Periodic boxes must exceed 2 (rc + skin).  skin = 0
+ * (default): every update is a full build. */
+a2c_status a2c_gpp_set_neighbor_skin(a2c_gpp_ctx *ctx, double skin);
+a2c_status a2c_gpp_update_neighbors(a2c_gpp_ctx *ctx, const double *X, int *max_neighbors, int *rebuilt);
+
 a2c_status a2c_gpp_neighbor_total(a2c_gpp_ctx *ctx, int list_id, int64_t *total);
 /* Export a list in the reference's form: offsets[n+1], idx[total] local to
  * the neighbor species, each site's list sorted ascending. */
@@ -258,6 +274,8 @@ typedef struct a2c_dmd_params {
   double xLb, xUb;         /* clamp of the diffusion step */
   double x_bd, gamma_bd;   /* occupancy and chemical potential held on the boundary sites */
   a2c_lbfgs_params lbfgs;  /* the minimization of every step */
+  int neighbor_update;     /* 1: re-derive the neighbor lists (incl. HH1) at the start of every step after the
+                              first, through the skin refilter when a skin is set; 0: keep them fixed */
 } a2c_dmd_params;
 
 /* Runs nsteps outer steps with all state on the device; X (4N), xH, gamma,
@@ -323,6 +341,41 @@ a2c_status a2c_gpp_batch_minimize(a2c_gpp_batch *batch, double *X, const a2c_lbf
 a2c_status a2c_gpp_batch_stats(a2c_gpp_batch *batch, int *ticks, double *seconds);
 /* the autotuner (see a2c_gpp_autotune) over the whole batch at host X */
 a2c_status a2c_gpp_batch_autotune(a2c_gpp_batch *batch, const double *X, int reps, int *tps, float *ms);
+
+/* Solution snapshots in the formats of the reference's Output class
+ * (Output.cpp:60-90, 133-480): per frame a VTK PolyData file
+ * <prefix>_L0_<frame>.vtp (points q; SiteID, MaterialID, Tag,
+ * AtomicFrequency = sigma, MolarFraction = occupancy, ChemicalPotential =
+ * gamma) with an entry in the collection <prefix>_L0.pvd, and/or an
+ * extended-XYZ file <prefix>_L0_<frame>.xyz (species, q, q - q0, site id,
+ * sigma, tag, occupancy, gamma).  One lattice, one species column pair:
+ * Pd sites carry occupancy 1 and gamma 0. */
+typedef struct a2c_snapshot_desc {
+  const char *prefix;   /* path prefix including the file base name */
+  int format;           /* 1 VTP, 2 XYZ, 3 both (OutputData::VTP, XYZ, VTP_and_XYZ) */
+  int precision;        /* 0 %7.4e, 1 %10.6e, 2 %16.10e (OutputData precision LOW, MEDIUM, HIGH) */
+  double axes[9];       /* lattice axes a, b, c for the XYZ header */
+  double origin[3];
+  int periodic[3];
+} a2c_snapshot_desc;
+/* the collection header (Output's constructor); call once before the frames */
+a2c_status a2c_snapshot_begin(const a2c_snapshot_desc *desc);
+/* host arrays: X (4N), X0 (4N, may be NULL: zero displacement), xH (nH),
+ * gamma (nH, may be NULL), siteid / tag (N, may be NULL: species / 0) */
+a2c_status a2c_snapshot_write(const a2c_snapshot_desc *desc, int frame, double time, int nPd, int nH, const double *X,
+                              const double *X0, const double *xH, const double *gamma, const signed char *siteid,
+                              const signed char *tag);
+/* The context's current state (positions, widths, occupancy) written
+ * without stalling the GPU: copied on the context's stream into pinned host
+ * memory, then formatted and written by a host thread while later work
+ * runs.  The host arrays (X0, gamma, siteid, tag; each may be NULL) are
+ * copied before the call returns.  One snapshot is in flight per context;
+ * a new one (or a2c_gpp_snapshot_wait, or destroy) waits for the previous
+ * one, and a2c_gpp_snapshot_wait returns its status. */
+a2c_status a2c_gpp_snapshot_async(a2c_gpp_ctx *ctx, const a2c_snapshot_desc *desc, int frame, double time,
+                                  const double *X0, const double *gamma, const signed char *siteid,
+                                  const signed char *tag);
+a2c_status a2c_gpp_snapshot_wait(a2c_gpp_ctx *ctx);
 
 /* Seeded synthetic fcc Pd lattice with octahedral H sites (stand-in for the
  * reference's SpaceInitializer lattice setup).  Site order: cells z, y, x,

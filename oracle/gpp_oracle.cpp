@@ -963,7 +963,9 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
       head = 0;
       steepest();
     }
-    double alpha = 1.0, fn = 0.0;
+    double dmax = 0.0;
+    for (int64_t t = 0; t < n; ++t) dmax = std::max(dmax, std::fabs(d[(size_t)t]));
+    double alpha = (lp->max_step > 0.0 && dmax > lp->max_step) ? lp->max_step / dmax : 1.0, fn = 0.0;
     bool ok = false;
     for (int ls = 0; ls < lp->max_ls; ++ls) {
       for (int64_t t = 0; t < n; ++t) xn[(size_t)t] = x[(size_t)t] + alpha * d[(size_t)t];

@@ -60,6 +60,7 @@ typedef struct orc_lbfgs {
   double f_noise;   /* relative objective noise for the derivative Armijo form; 0 = 1e-14 */
   int stall_window; /* stop (6) when f fell by <= stall_rtol*|f| over this many iterations */
   double stall_rtol;/* 0 = 1e-14 */
+  double max_step;  /* first trial step length min(1, max_step / max|d|); 0 = no cap */
 } orc_lbfgs;
 
 /* Arithmetic mode: 0 = the reference's (C library exp/pow/log, sequential

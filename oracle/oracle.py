@@ -43,7 +43,7 @@ class OrcParams(C.Structure):
 class OrcLbfgs(C.Structure):
     _fields_ = [("m", C.c_int), ("max_it", C.c_int), ("max_fev", C.c_int), ("max_ls", C.c_int), ("gatol", D),
                 ("c1", D), ("init_step", D), ("sigma_lb", D), ("f_noise", D), ("stall_window", C.c_int),
-                ("stall_rtol", D)]
+                ("stall_rtol", D), ("max_step", D)]
 
 
 def _p(a):
@@ -255,8 +255,10 @@ def macro_results(x, HSurf):
 
 
 def minimize(pb: Problem, X, xH, off, nbr, *, m=5, max_it=10000, max_fev=20000, max_ls=30, gatol=1e-6, c1=1e-4,
-             init_step=1e-2, sigma_lb=1e-6, f_noise=0.0, stall_window=50, stall_rtol=0.0, threads=None):
-    lp = OrcLbfgs(m, max_it, max_fev, max_ls, gatol, c1, init_step, sigma_lb, f_noise, stall_window, stall_rtol)
+             init_step=1e-2, sigma_lb=1e-6, f_noise=0.0, stall_window=50, stall_rtol=0.0, max_step=0.25,
+             threads=None):
+    lp = OrcLbfgs(m, max_it, max_fev, max_ls, gatol, c1, init_step, sigma_lb, f_noise, stall_window, stall_rtol,
+                  max_step)
     X = np.ascontiguousarray(X, dtype=np.float64).copy()
     xH = np.ascontiguousarray(xH, dtype=np.float64)
     f, it, nf, gn, why = C.c_double(), C.c_int(), C.c_int(), C.c_double(), C.c_int()
@@ -381,16 +383,20 @@ def ref_macro_results(x, HSurf):
 
 
 def dmd_run(pb: Problem, X, xH, gamma, full_H, off, nbr, hh1_off, hh1, bd_sites, surf_sites, nsteps, *, dt, nu, Qm,
-            x_bd, gamma_bd, xLb=1e-3, xUb=1.0 - 1e-16, **lbfgs):
-    """The DMD outer loop in the order the device runs it: minimize ->
-    chemical potential -> Dirichlet -> diffuse -> occupancy update -> macro
-    results.  Returns the same fields as a2c_gb300.Gpp.dmd_run."""
+            x_bd, gamma_bd, xLb=1e-3, xUb=1.0 - 1e-16, neighbor_update=False, **lbfgs):
+    """The DMD outer loop in the order the device runs it: (lists rebuilt at
+    the current positions when neighbor_update, from the second step) ->
+    minimize -> chemical potential -> Dirichlet -> diffuse -> occupancy
+    update -> macro results.  Returns the same fields as
+    a2c_gb300.Gpp.dmd_run."""
     X = np.array(X, dtype=np.float64)
     x0 = np.array(xH, dtype=np.float64)
     g = np.array(gamma, dtype=np.float64)
     fh = np.array(full_H, dtype=np.int32)
     out = {"xH_mean": [], "xH_interior": [], "fmin": [], "iters": []}
-    for _ in range(nsteps):
+    for k in range(nsteps):
+        if neighbor_update and k > 0:
+            off, nbr, _, hh1_off, hh1 = neighbors(pb, X)
         r = minimize(pb, X, x0, off, nbr, **lbfgs)
         X = r["X"]
         g, fh = chem_potential(pb, X, x0, off, nbr, gamma_bd, g, fh)

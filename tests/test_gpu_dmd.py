@@ -50,6 +50,29 @@ def test_dmd_fp64_bit_exact_vs_oracle(gpu):
     assert out["xH_mean"][-1] > out["xH_mean"][0]  # hydrogen enters through the held surface
 
 
+def test_dmd_fp64_neighbor_update_bit_exact(gpu):
+    """Lists re-derived every outer step (skin refilter on the device, a
+    full build in the oracle): still bit for bit."""
+    X, xH, bd, box, nPd, nH = slab()
+    per = (1, 1, 0)
+    pb = O.Problem(nPd, nH, T=400.0, box=box, periodic=per)
+    off, nbr, shell, o1, i1 = O.neighbors(pb, X)
+    gamma0 = np.zeros(nH)
+    full0 = np.zeros(nH, dtype=np.int32)
+    kw = dict(gatol=1e-5, max_it=300)
+    with O.arithmetic("device"):
+        ref = O.dmd_run(pb, X, xH, gamma0, full0, off, nbr, o1, i1, bd, bd, 3, gamma_bd=2.0, neighbor_update=True,
+                        **DMD, **kw)
+    with A.Gpp(nPd, nH, T=400.0, box=box, periodic=per) as g:
+        g.set_occupancy(xH)
+        g.set_neighbor_skin(0.5)
+        g.update_neighbors(X)
+        out = g.dmd_run(X, xH, gamma0, full0, bd, bd, 3, gamma_bd=2.0, neighbor_update=True, **DMD, **kw)
+    assert np.array_equal(out["iters"], ref["iters"])
+    for k in ("X", "xH", "gamma", "full_H", "fmin"):
+        assert np.array_equal(out[k], ref[k]), k
+
+
 def test_dmd_mixed_follows_fp64(gpu):
     X, xH, bd, box, nPd, nH = slab()
     per = (1, 1, 0)

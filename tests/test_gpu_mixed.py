@@ -83,3 +83,22 @@ def test_mixed_minimize_close_to_fp64(gpu):
     assert abs(f_at_mixed - r64.fmin) <= 1e-6 * abs(r64.fmin)
     assert abs(f_at_raw - r64.fmin) <= 1e-6 * abs(r64.fmin)
     assert dq < 1e-3
+
+
+def test_minimize_keeps_widths_bound(gpu):
+    """Long minimizations of a hydride-nucleus lattice: without a cap on the
+    first trial step, accepted steps carried some Gaussian widths over the
+    binding barrier (-3 kB x ln sigma falls without bound once a site leaves
+    its neighbors; widths reached 300 A at 32^3 cells).  With the default
+    max_step every width stays physical and both forms converge."""
+    X, xH, _, box, nPd, nH = A.lattice_fcc(16, periodic=(1, 1, 1), pos_std=0.02, sigma=(0.1, 0.1), x_mode=1,
+                                           x_matrix=0.02, x_nucleus=0.60, nucleus_radius=20.0, interface_width=5.0,
+                                           x_half=0.0, seed=3)
+    for prec in ("mixed", "fp64"):
+        with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), precision=prec) as g:
+            g.set_occupancy(xH)
+            g.build_neighbors(X)
+            r = g.minimize(X, gatol=1e-5, max_it=4000, polish=0)
+        sig = r.X[3::4]
+        assert sig.max() < 0.5 and sig.min() > 0.03, (prec, sig.min(), sig.max())
+        assert r.reason in (A.CONVERGED_GATOL, A.CONVERGED_STALLED), (prec, r.reason)
