@@ -95,6 +95,7 @@ struct a2c_gpp_ctx {
   a2c::Mixed *mixed;
   a2c::Lbfgs *lbfgs;
   void *snap;  // the snapshot in flight (api.cu)
+  double *h_small;  // pinned: f and the status word of a host-pointer call
   int last_mixed_iters, last_fp64_iters;
   double last_mixed_gnorm;
 };
@@ -145,7 +146,10 @@ a2c_status update_neighbors_device(a2c_gpp_ctx *c, const double *h_X, int *rebui
 // k_mixed.cu
 // ev: optional 5 events recorded before the first launch and after each
 // stage (prep, pass 1, pass 2, reduction) on the context's stream
-a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev = nullptr);
+// Xcopy: X is the caller's pinned host memory (device-mapped); the prep
+// kernel also copies it to Xcopy and flags non-finite values
+a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev = nullptr,
+                      double *Xcopy = nullptr);
 void mixed_free(a2c_gpp_ctx *c);
 a2c_status mixed_set_threads_per_site(a2c_gpp_ctx *c, int tps);
 int mixed_threads_per_site(a2c_gpp_ctx *c);

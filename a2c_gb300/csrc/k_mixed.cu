@@ -479,6 +479,23 @@ __global__ void k_prep(const double *X, const double *occ, int64_t N, double k0,
   occf[s] = (float)occ[s];
 }
 
+// The same, reading X from the caller's pinned host memory over the
+// coherent host link: also keeps the context's device copy of the state and
+// flags non-finite inputs (what a separate copy and check would do).
+__global__ void k_prep_copy(const double *X, const double *occ, int64_t N, double k0, double k1, double k2, int4 *P,
+                            float *occf, double *Xcopy, int *status) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  const double4 x = *reinterpret_cast<const double4 *>(X + 4 * s);
+  *reinterpret_cast<double4 *>(Xcopy + 4 * s) = x;
+  if (!isfinite(x.x) || !isfinite(x.y) || !isfinite(x.z) || !isfinite(x.w)) atomicOr(status, kStatusNonfinite);
+  const long long u0 = __double2ll_rn(x.x * k0);
+  const long long u1 = __double2ll_rn(x.y * k1);
+  const long long u2 = __double2ll_rn(x.z * k2);
+  P[s] = make_int4((int)(unsigned)u0, (int)(unsigned)u1, (int)(unsigned)u2, __float_as_int((float)x.w));
+  occf[s] = (float)occ[s];
+}
+
 // Batched: positions of the listed sites with their instance's scale.
 __global__ void k_prep_list(const double *X, const double *occ, BatchView bv, int4 *P, float *occf) {
   const int n = *bv.count;
@@ -581,7 +598,7 @@ a2c_status mixed_set_threads_per_site(a2c_gpp_ctx *c, int tps) {
   return A2C_OK;
 }
 
-a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev) {
+a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev, double *Xcopy) {
   A2C_TRY(ensure_mixed(c));
   Mixed *M = c->mixed;
   const int64_t N = c->N;
@@ -609,7 +626,11 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   a.T = c->p.T;
   if (ev) cudaEventRecord(ev[0], c->stream);
   if (N > 0) {
-    k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ);
+    if (Xcopy)
+      k_prep_copy<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ, Xcopy,
+                                                           c->d_status);
+    else
+      k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ);
     A2C_CUDA(cudaGetLastError());
     if (ev) cudaEventRecord(ev[1], c->stream);
     int tps = M->tps ? M->tps : (N < 152 * 2048 ? 4 : 1);

@@ -102,3 +102,37 @@ def test_minimize_keeps_widths_bound(gpu):
         sig = r.X[3::4]
         assert sig.max() < 0.5 and sig.min() > 0.03, (prec, sig.min(), sig.max())
         assert r.reason in (A.CONVERGED_GATOL, A.CONVERGED_STALLED), (prec, r.reason)
+
+
+def test_host_pointer_eval_pinned_equals_pageable(gpu):
+    """a2c_gpp_eval with pinned caller buffers (the prep kernel reads X and
+    pass 2 writes G over the coherent host link) gives the same bits as with
+    pageable buffers (bulk copies); a non-finite pinned input is rejected and
+    the context stays usable."""
+    import torch
+
+    X, xH, _, box, nPd, nH = A.lattice_fcc(6, periodic=(1, 1, 1), pos_std=0.03, sigma=(0.08, 0.14), x_center=0.15,
+                                           x_half=0.15, seed=2)
+    with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), precision="mixed") as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        f0, G0 = g.eval(X)  # pageable numpy buffers
+        Xp = torch.empty(X.size, dtype=torch.float64, pin_memory=True)
+        Gp = torch.empty(X.size, dtype=torch.float64, pin_memory=True)
+        Xp.numpy()[:] = X
+        import ctypes as C
+
+        fv = C.c_double()
+        L = A._native.lib()
+
+        def call():
+            return L.a2c_gpp_eval(g.handle, C.c_void_p(Xp.data_ptr()), C.byref(fv), C.c_void_p(Gp.data_ptr()))
+
+        for _ in range(2):
+            A._native.check(call(), "a2c_gpp_eval")
+            assert fv.value == f0 and np.array_equal(Gp.numpy(), G0)
+        Xp.numpy()[7] = np.nan
+        assert call() == A._native.A2C_ERR_NONFINITE
+        Xp.numpy()[:] = X
+        A._native.check(call(), "a2c_gpp_eval")
+        assert fv.value == f0 and np.array_equal(Gp.numpy(), G0)
