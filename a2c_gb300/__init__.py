@@ -416,6 +416,26 @@ class Batch:
         return [X[4 * self.offsets[k]:4 * self.offsets[k + 1]] for k in range(self.B)]
 
 
+def read_input(path: str) -> dict:
+    """An input file in the reference's syntax (a2c_input_read): the fields
+    the evaluator, the DMD loop and the snapshots use, with the reference's
+    defaults.  Raises A2CError with the parser's message on a bad file."""
+    inp = N.Input()
+    msg = C.create_string_buffer(256)
+    st = N.lib().a2c_input_read(str(path).encode(), C.byref(inp), msg, 256)
+    if st != N.A2C_OK:
+        raise A2CError(st, "a2c_input_read: " + msg.value.decode())
+    out = {}
+    for name, _ in N.Input._fields_:
+        v = getattr(inp, name)
+        if isinstance(v, bytes):
+            v = v.decode()
+        elif hasattr(v, "__len__"):
+            v = list(v)
+        out[name] = v
+    return out
+
+
 def snapshot_desc(prefix: str, *, fmt: str = "both", precision: int = 2, box=(0.0, 0.0, 0.0), origin=(0.0, 0.0, 0.0),
                   periodic=(0, 0, 0)):
     """Descriptor of a snapshot series (a2c_snapshot_desc): files

@@ -70,6 +70,17 @@ class SnapshotDesc(C.Structure):
                 ("origin", C.c_double * 3), ("periodic", C.c_int * 3)]
 
 
+class Input(C.Structure):
+    _fields_ = [("T", C.c_double), ("nu", C.c_double), ("Qm", C.c_double), ("t_subsurf", C.c_double),
+                ("mubd", C.c_double), ("eps", C.c_double), ("rc", C.c_double), ("potential_file", C.c_char * 256),
+                ("dt", C.c_double), ("max_time", C.c_double), ("cfl", C.c_double), ("max_its", C.c_int),
+                ("output_format", C.c_int), ("output_precision", C.c_int), ("output_frequency", C.c_int),
+                ("output_interval", C.c_double), ("output_prefix", C.c_char * 256),
+                ("output_solution", C.c_char * 256), ("lattice_axes", C.c_double * 9),
+                ("lattice_origin", C.c_double * 3), ("lattice_periodic", C.c_int * 3), ("n_assignments", C.c_int),
+                ("n_used", C.c_int)]
+
+
 class DmdParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("nu", C.c_double), ("Qm", C.c_double), ("xLb", C.c_double),
                 ("xUb", C.c_double), ("x_bd", C.c_double), ("gamma_bd", C.c_double), ("lbfgs", LbfgsParams),
@@ -110,6 +121,8 @@ def lib() -> C.CDLL:
         "a2c_gpp_neighbor_total": (I, [P, I, C.POINTER(C.c_int64)]),
         "a2c_gpp_set_neighbor_skin": (I, [P, D]),
         "a2c_snapshot_begin": (I, [C.POINTER(SnapshotDesc)]),
+        "a2c_input_read": (I, [C.c_char_p, C.POINTER(Input), C.c_char_p, I]),
+        "a2c_input_apply": (I, [C.POINTER(Input), C.POINTER(GppParams)]),
         "a2c_snapshot_write": (I, [C.POINTER(SnapshotDesc), I, D, I, I, P, P, P, P, P, P]),
         "a2c_gpp_snapshot_async": (I, [P, C.POINTER(SnapshotDesc), I, D, P, P, P, P]),
         "a2c_gpp_snapshot_wait": (I, [P]),
@@ -161,7 +174,7 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_destroy", "a2c_gpp_stream", "a2c_gpp_set_precision", "a2c_gpp_synchronize",
             "a2c_gpp_set_threads_per_site", "a2c_gpp_set_occupancy",
             "a2c_gpp_get_occupancy", "a2c_gpp_set_state", "a2c_gpp_get_state", "a2c_gpp_build_neighbors",
-            "a2c_gpp_neighbor_total", "a2c_gpp_set_neighbor_skin", "a2c_gpp_update_neighbors", "a2c_snapshot_begin",
+            "a2c_gpp_neighbor_total", "a2c_gpp_set_neighbor_skin", "a2c_gpp_update_neighbors", "a2c_snapshot_begin", "a2c_input_read", "a2c_input_apply",
             "a2c_snapshot_write", "a2c_gpp_snapshot_async", "a2c_gpp_snapshot_wait", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
             "a2c_gpp_eval_device", "a2c_gpp_profile_eval", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
             "a2c_gpp_chem_potential", "a2c_gpp_minimize_stats", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",

@@ -377,6 +377,35 @@ a2c_status a2c_gpp_snapshot_async(a2c_gpp_ctx *ctx, const a2c_snapshot_desc *des
                                   const signed char *tag);
 a2c_status a2c_gpp_snapshot_wait(a2c_gpp_ctx *ctx);
 
+/* Input files in the reference's syntax (parser/Parser.y, parser/Lexer.l:
+ * assignments, "under X { ... }" groups, dotted and indexed names,
+ * integer/double expressions, strings, keywords, comments, "end"), read by a
+ * hand-written parser.  The fields below are filled from the reference's
+ * keys with its defaults (IoData.cpp); other objects of a full input file
+ * (geometry, species, initial conditions, ...) are parsed and counted. */
+typedef struct a2c_input {
+  double T, nu, Qm, t_subsurf, mubd; /* Diffusion.Temperature, AttemptFrequency, ActivationEnergy,
+                                        SubsurfaceThickness, SoluteChemicalPotential */
+  double eps, rc;                    /* Material[0].InteratomicPotential.Tolerance, CutOffDistance */
+  char potential_file[256];          /* Material[0].InteratomicPotential.File */
+  double dt, max_time, cfl;          /* Time.TimeStep, MaxTime, CFL */
+  int max_its;                       /* Time.MaxIts */
+  int output_format;                 /* Output.Format: 1 VTP, 2 XYZ, 3 both (a2c_snapshot_desc.format) */
+  int output_precision;              /* Output.Precision: 0 Low, 1 Medium, 2 High */
+  int output_frequency;              /* Output.Frequency */
+  double output_interval;            /* Output.TimeInterval */
+  char output_prefix[256], output_solution[256]; /* Output.Prefix, Output.Solution */
+  double lattice_axes[9];            /* Lattice[0].OAx ... OCz */
+  double lattice_origin[3];          /* Lattice[0].Ox, Oy, Oz */
+  int lattice_periodic[3];           /* Lattice[0].PeriodicOA/OB/OC */
+  int n_assignments;                 /* assignments in the file */
+  int n_used;                        /* of which filled a field above */
+} a2c_input;
+/* errmsg (may be NULL) receives "syntax error near line N" and the like */
+a2c_status a2c_input_read(const char *path, a2c_input *input, char *errmsg, int errlen);
+/* T, eps, rc of an input into evaluator parameters */
+a2c_status a2c_input_apply(const a2c_input *input, a2c_gpp_params *params);
+
 /* Seeded synthetic fcc Pd lattice with octahedral H sites (stand-in for the
  * reference's SpaceInitializer lattice setup).  Site order: cells z, y, x,
  * then basis; all Pd then all H.  Writes X (4N), xH (nH) and surface flags
