@@ -214,6 +214,10 @@ class Gpp:
     def snapshot_wait(self) -> None:
         N.check(self._L.a2c_gpp_snapshot_wait(self._h), "a2c_gpp_snapshot_wait")
 
+    def set_minimizer(self, host_loop: bool) -> None:
+        """Mixed precision: device-driven graph ticks (default) or the host loop."""
+        N.check(self._L.a2c_gpp_set_minimizer(self._h, int(bool(host_loop))), "a2c_gpp_set_minimizer")
+
     def set_neighbor_skin(self, skin: float) -> None:
         N.check(self._L.a2c_gpp_set_neighbor_skin(self._h, float(skin)), "a2c_gpp_set_neighbor_skin")
 

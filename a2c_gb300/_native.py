@@ -159,6 +159,7 @@ def lib() -> C.CDLL:
         "a2c_gpp_batch_stats": (I, [P, C.POINTER(I), C.POINTER(D)]),
         "a2c_gpp_batch_autotune": (I, [P, P, I, C.POINTER(I), P]),
         "a2c_gpp_autotune": (I, [P, I, C.POINTER(I), P]),
+        "a2c_gpp_set_minimizer": (I, [P, I]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -182,7 +183,7 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_batch_create", "a2c_gpp_batch_destroy", "a2c_gpp_batch_info", "a2c_gpp_batch_set_occupancy",
             "a2c_gpp_batch_build_neighbors", "a2c_gpp_batch_set_threads_per_site", "a2c_gpp_batch_set_graphs",
             "a2c_gpp_batch_eval", "a2c_gpp_batch_minimize", "a2c_gpp_batch_stats", "a2c_gpp_batch_autotune",
-            "a2c_gpp_autotune"]
+            "a2c_gpp_autotune", "a2c_gpp_set_minimizer"]
 
 
 class A2CError(RuntimeError):

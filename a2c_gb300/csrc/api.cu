@@ -237,6 +237,7 @@ a2c_status a2c_gpp_destroy(a2c_gpp_ctx *c) {
   if (!c) return A2C_OK;
   DeviceGuard g(c->device);
   snapshot_release(c);
+  engine_free(c);
   if (c->stream) cudaStreamSynchronize(c->stream);
   mixed_free(c);
   lbfgs_free(c);
@@ -301,6 +302,12 @@ a2c_status a2c_gpp_autotune(a2c_gpp_ctx *c, int reps, int *tps_out, float *ms) {
   if (!s && tps_out) *tps_out = best;
   if (!s) s = check_status_word(c);
   return s;
+}
+
+a2c_status a2c_gpp_set_minimizer(a2c_gpp_ctx *c, int host_loop) {
+  if (!c) return A2C_ERR_INVALID;
+  c->host_loop = host_loop ? 1 : 0;
+  return A2C_OK;
 }
 
 a2c_status a2c_gpp_synchronize(a2c_gpp_ctx *c) {

@@ -698,10 +698,13 @@ struct a2c_gpp_batch {
   double *x = nullptr, *g = nullptr, *pg = nullptr, *d = nullptr, *xn = nullptr, *gn = nullptr;
   double *S = nullptr, *Y = nullptr, *rho = nullptr, *alph = nullptr, *fh = nullptr;
   int *h_cnt = nullptr;  // pinned
-  // the captured tick
+  // the captured tick (and the neighbor array it was captured with: a list
+  // rebuild may reallocate it)
   cudaGraphExec_t exec = nullptr;
   Cfg exec_cfg{};
   int exec_tps = -1;
+  const void *exec_nbr = nullptr;
+  bool borrowed = false;  // c belongs to a context (the one-instance engine)
   // statistics of the last minimization
   int ticks = 0;
   double seconds = 0.0;
@@ -855,6 +858,213 @@ bool same_common(const a2c_gpp_params &a, const a2c_gpp_params &b) {
   return true;
 }
 
+struct DeviceGuard2 {
+  explicit DeviceGuard2(int d) { cudaSetDevice(d); }
+};
+
+// Instance, chunk and list tables of a batch whose system b->c exists;
+// set_occ: Pd occupancy 1, H 0 (a fresh union system).
+a2c_status init_tables(a2c_gpp_batch *b, const a2c_gpp_params *params, int n, bool set_occ) {
+  DeviceGuard2 dg(b->device);
+  const int64_t N = b->c->N;
+  // instance table and chunk tables
+  b->start.assign(n + 1, 0);
+  b->ecb.assign(n + 1, 0);
+  b->scb.assign(n + 1, 0);
+  std::vector<InstGeo> geo(n);
+  std::vector<Chunk> ech, sch;
+  std::vector<uint16_t> inst((size_t)N);
+  std::vector<double> occ((size_t)N, 0.0);
+  for (int k = 0; k < n; ++k) {
+    const a2c_gpp_params &p = params[k];
+    const int64_t s0 = b->start[k], nk = (int64_t)p.nPd + p.nH;
+    b->start[k + 1] = s0 + nk;
+    InstGeo &G = geo[k];
+    for (int d = 0; d < 3; ++d) {
+      G.S[d] = p.periodic[d] ? p.box[d] : 64.0;
+      G.sc[d] = (float)(G.S[d] / 4294967296.0);
+    }
+    G.T = p.T;
+    G.start = (int)s0;
+    G.nPd = p.nPd;
+    G.nH = p.nH;
+    for (int64_t i = 0; i < nk; ++i) inst[(size_t)(s0 + i)] = (uint16_t)k;
+    for (int64_t i = 0; i < p.nPd; ++i) occ[(size_t)(s0 + i)] = 1.0;
+    b->ecb[k] = (int)ech.size();
+    for (int64_t c0 = 0; c0 < 4 * nk; c0 += kChunk)
+      ech.push_back({4 * s0 + c0, (int)std::min<int64_t>(kChunk, 4 * nk - c0), k});
+    b->scb[k] = (int)sch.size();
+    for (int64_t c0 = 0; c0 < nk; c0 += kChunk) sch.push_back({s0 + c0, (int)std::min<int64_t>(kChunk, nk - c0), k});
+  }
+  b->ecb[n] = (int)ech.size();
+  b->scb[n] = (int)sch.size();
+  b->nec = (int64_t)ech.size();
+  b->nsc = (int64_t)sch.size();
+  a2c_status s = A2C_OK;
+  if (!s) s = dmalloc(&b->geo, n);
+  if (!s) s = dmalloc(&b->inst, N);
+  if (!s) s = dmalloc(&b->ech, b->nec);
+  if (!s) s = dmalloc(&b->sch, b->nsc);
+  if (!s) s = dmalloc(&b->d_ecb, n + 1);
+  if (!s) s = dmalloc(&b->d_scb, n + 1);
+  if (!s) s = dmalloc(&b->lm, N);
+  if (!s) s = dmalloc(&b->lf, N);
+  if (!s) s = dmalloc(&b->le, b->nec);
+  if (!s) s = dmalloc(&b->ls, b->nsc);
+  if (!s) s = dmalloc(&b->cnt, 8);
+  if (!s) s = dmalloc(&b->listed, n);
+  if (!s) s = dmalloc(&b->loff, 6 * (int64_t)n);
+  if (!s) s = dmalloc(&b->st, n);
+  if (!s) s = dmalloc(&b->part, 8 * b->nec + 2 * b->nsc);
+  if (!s && cudaMallocHost((void **)&b->h_cnt, 8 * sizeof(int)) != cudaSuccess) s = A2C_ERR_NOMEM;
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    if (!s && bytes && cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) s = A2C_ERR_CUDA;
+  };
+  up(b->geo, geo.data(), sizeof(InstGeo) * n);
+  up(b->inst, inst.data(), sizeof(uint16_t) * N);
+  up(b->ech, ech.data(), sizeof(Chunk) * ech.size());
+  up(b->sch, sch.data(), sizeof(Chunk) * sch.size());
+  up(b->d_ecb, b->ecb.data(), sizeof(int) * (n + 1));
+  up(b->d_scb, b->scb.data(), sizeof(int) * (n + 1));
+  if (set_occ) up(b->c->d_occ, occ.data(), sizeof(double) * N);
+  if (!s && cudaMemset(b->cnt, 0, 8 * sizeof(int)) != cudaSuccess) s = A2C_ERR_CUDA;
+  return s;
+}
+
+// The minimization of every instance; X in/out on the host or (dev) on
+// the device.  Per-instance results into the host arrays (any may be null)
+// and, when `last` is given, the per-instance records.
+a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_params *lp, double *fmin, int *iters,
+                         int *nfev, double *gnorm, int *reason, int *mixed_iters, int *fp64_iters,
+                         std::vector<Inst> *last) {
+  if (!b || !X || !lp) return A2C_ERR_INVALID;
+  if (lp->m < 1 || lp->m > kMaxM || lp->max_ls < 1 || !(lp->sigma_lb > 0.0) || !(lp->init_step > 0.0) ||
+      lp->stall_window < 0 || lp->stall_window > 4096 || lp->max_fev < 1)
+    return A2C_ERR_INVALID;
+  a2c_gpp_ctx *c = b->c;
+  if (!c->has_neighbors) return A2C_ERR_STATE;
+  DeviceGuard2 dg(b->device);
+  const int64_t N = c->N;
+  if (!dev)
+    for (int64_t t = 0; t < 4 * N; ++t)
+      if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
+  A2C_TRY(ensure_lbfgs(b, lp->m, lp->stall_window));
+  cudaStream_t s = c->stream;
+  Cfg cf{};
+  cf.B = b->B;
+  cf.m = lp->m;
+  cf.ring = lp->m + 1;
+  cf.max_it = lp->max_it;
+  cf.max_fev = lp->max_fev;
+  cf.max_ls = lp->max_ls;
+  cf.polish = b->precision == A2C_MIXED ? lp->polish : 0;
+  cf.W = lp->stall_window;
+  cf.nec = b->nec;
+  cf.nsc = b->nsc;
+  cf.n = 4 * N;
+  cf.gatol = lp->gatol;
+  cf.c1 = lp->c1;
+  cf.init_step = lp->init_step;
+  cf.lb = lp->sigma_lb;
+  cf.max_step = lp->max_step;
+  cf.fn_mixed = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-7;
+  cf.fn_fp64 = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-14;
+  cf.st_mixed = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-10;
+  cf.st_fp64 = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-14;
+  const int tps = default_tps(b);
+  if (b->precision == A2C_MIXED) A2C_TRY(mixed_prepare(c));
+  Dev D = dev_view(b);
+  cudaEvent_t e0, e1;
+  A2C_CUDA(cudaEventCreate(&e0));
+  A2C_CUDA(cudaEventCreate(&e1));
+  a2c_status st = A2C_OK;
+  auto fail = [&](a2c_status v) {
+    if (!st) st = v;
+  };
+  if (cudaMemcpyAsync(b->x, X, sizeof(double) * 4 * N, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    fail(A2C_ERR_CUDA);
+  cudaEventRecord(e0, s);
+  k_project_all<<<chunk_grid((4 * N + 255) / 256), 256, 0, s>>>(b->x, 4 * N, cf.lb);
+  k_init_state<<<(b->B + 127) / 128, 128, 0, s>>>(D, cf, b->precision == A2C_MIXED ? kPhaseMixed : kPhaseFp64);
+  if (cudaMemsetAsync(b->listed, 0xff, sizeof(int) * b->B, s) != cudaSuccess) fail(A2C_ERR_CUDA);
+  if (!st) fail(plan(b, D));
+  // the first tick (every instance's first evaluation) runs eagerly: it also
+  // performs the launchers' one-time occupancy queries outside any capture
+  if (!st) fail(tick(b, D, cf, tps));
+  // the captured tick, reused while the configuration is unchanged
+  const bool same = b->exec && b->exec_tps == tps && b->exec_nbr == (const void *)c->d_nbr &&
+                    !std::memcmp(&b->exec_cfg, &cf, sizeof(Cfg));
+  if (!st && b->graphs && !same) {
+    if (b->exec) {
+      cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+    }
+    cudaGraph_t gr = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) fail(A2C_ERR_CUDA);
+    const a2c_status ts = st ? st : tick(b, D, cf, tps);
+    if (cudaStreamEndCapture(s, &gr) != cudaSuccess) fail(A2C_ERR_CUDA);
+    fail(ts);
+    if (!st && cudaGraphInstantiate(&b->exec, gr, 0) != cudaSuccess) fail(A2C_ERR_CUDA);
+    if (gr) cudaGraphDestroy(gr);
+    b->exec_cfg = cf;
+    b->exec_tps = tps;
+    b->exec_nbr = c->d_nbr;
+  }
+  // replay: K ticks, then read how many instances are left
+  const int K = 8;
+  const int64_t max_ticks = 2 * ((int64_t)lp->max_fev + 2) + 2 * K;
+  int64_t ticks = 1;
+  while (!st) {
+    for (int k = 0; k < K; ++k) {
+      if (b->graphs) {
+        if (cudaGraphLaunch(b->exec, s) != cudaSuccess) fail(A2C_ERR_CUDA);
+      } else {
+        fail(tick(b, D, cf, tps));
+      }
+    }
+    ticks += K;
+    if (cudaMemcpyAsync(b->h_cnt, b->cnt, 8 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      fail(A2C_ERR_CUDA);
+    if (st || b->h_cnt[kCntLeft] == 0) break;
+    if (ticks >= max_ticks) {
+      fail(A2C_ERR_STATE);
+      break;
+    }
+  }
+  cudaEventRecord(e1, s);
+  if (!st && cudaMemcpyAsync(X, b->x, sizeof(double) * 4 * N, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             s) != cudaSuccess)
+    fail(A2C_ERR_CUDA);
+  std::vector<Inst> hs((size_t)b->B);
+  if (!st && cudaMemcpyAsync(hs.data(), b->st, sizeof(Inst) * b->B, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    fail(A2C_ERR_CUDA);
+  if (cudaStreamSynchronize(s) != cudaSuccess) fail(A2C_ERR_CUDA);
+  float ms = 0.0f;
+  if (!st && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) b->seconds = 1e-3 * ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->ticks = (int)ticks;
+  // a trial point with a non-finite objective is rejected by the line
+  // search; it is not an error of the minimization
+  cudaMemsetAsync(c->d_status, 0, sizeof(int), s);
+  if (st) return st;
+  for (int k = 0; k < b->B; ++k) {
+    if (fmin) fmin[k] = hs[k].f;
+    if (iters) iters[k] = hs[k].it;
+    if (nfev) nfev[k] = hs[k].fev;
+    if (gnorm) gnorm[k] = hs[k].gnorm;
+    if (reason) reason[k] = hs[k].why;
+    if (mixed_iters) mixed_iters[k] = hs[k].mixed_iters;
+    if (fp64_iters) fp64_iters[k] = hs[k].phase == kPhaseFp64 ? hs[k].fp64_iters : 0;
+  }
+  if (last) last->swap(hs);
+  c->has_state = true;
+  return A2C_OK;
+}
+
+
 }  // namespace
 
 extern "C" {
@@ -889,68 +1099,7 @@ a2c_status a2c_gpp_batch_create(const a2c_gpp_params *params, int n, a2c_gpp_bat
     delete b;
     return s;
   }
-  DeviceGuard dg(b->device);
-  // instance table and chunk tables
-  b->start.assign(n + 1, 0);
-  b->ecb.assign(n + 1, 0);
-  b->scb.assign(n + 1, 0);
-  std::vector<InstGeo> geo(n);
-  std::vector<Chunk> ech, sch;
-  std::vector<uint16_t> inst((size_t)N);
-  std::vector<double> occ((size_t)N, 0.0);
-  for (int k = 0; k < n; ++k) {
-    const a2c_gpp_params &p = params[k];
-    const int64_t s0 = b->start[k], nk = (int64_t)p.nPd + p.nH;
-    b->start[k + 1] = s0 + nk;
-    InstGeo &G = geo[k];
-    for (int d = 0; d < 3; ++d) {
-      G.S[d] = p.periodic[d] ? p.box[d] : 64.0;
-      G.sc[d] = (float)(G.S[d] / 4294967296.0);
-    }
-    G.T = p.T;
-    G.start = (int)s0;
-    G.nPd = p.nPd;
-    G.nH = p.nH;
-    for (int64_t i = 0; i < nk; ++i) inst[(size_t)(s0 + i)] = (uint16_t)k;
-    for (int64_t i = 0; i < p.nPd; ++i) occ[(size_t)(s0 + i)] = 1.0;
-    b->ecb[k] = (int)ech.size();
-    for (int64_t c0 = 0; c0 < 4 * nk; c0 += kChunk)
-      ech.push_back({4 * s0 + c0, (int)std::min<int64_t>(kChunk, 4 * nk - c0), k});
-    b->scb[k] = (int)sch.size();
-    for (int64_t c0 = 0; c0 < nk; c0 += kChunk) sch.push_back({s0 + c0, (int)std::min<int64_t>(kChunk, nk - c0), k});
-  }
-  b->ecb[n] = (int)ech.size();
-  b->scb[n] = (int)sch.size();
-  b->nec = (int64_t)ech.size();
-  b->nsc = (int64_t)sch.size();
-  s = A2C_OK;
-  if (!s) s = dmalloc(&b->geo, n);
-  if (!s) s = dmalloc(&b->inst, N);
-  if (!s) s = dmalloc(&b->ech, b->nec);
-  if (!s) s = dmalloc(&b->sch, b->nsc);
-  if (!s) s = dmalloc(&b->d_ecb, n + 1);
-  if (!s) s = dmalloc(&b->d_scb, n + 1);
-  if (!s) s = dmalloc(&b->lm, N);
-  if (!s) s = dmalloc(&b->lf, N);
-  if (!s) s = dmalloc(&b->le, b->nec);
-  if (!s) s = dmalloc(&b->ls, b->nsc);
-  if (!s) s = dmalloc(&b->cnt, 8);
-  if (!s) s = dmalloc(&b->listed, n);
-  if (!s) s = dmalloc(&b->loff, 6 * (int64_t)n);
-  if (!s) s = dmalloc(&b->st, n);
-  if (!s) s = dmalloc(&b->part, 8 * b->nec + 2 * b->nsc);
-  if (!s && cudaMallocHost((void **)&b->h_cnt, 8 * sizeof(int)) != cudaSuccess) s = A2C_ERR_NOMEM;
-  auto up = [&](void *dst, const void *src, size_t bytes) {
-    if (!s && bytes && cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) s = A2C_ERR_CUDA;
-  };
-  up(b->geo, geo.data(), sizeof(InstGeo) * n);
-  up(b->inst, inst.data(), sizeof(uint16_t) * N);
-  up(b->ech, ech.data(), sizeof(Chunk) * ech.size());
-  up(b->sch, sch.data(), sizeof(Chunk) * sch.size());
-  up(b->d_ecb, b->ecb.data(), sizeof(int) * (n + 1));
-  up(b->d_scb, b->scb.data(), sizeof(int) * (n + 1));
-  up(b->c->d_occ, occ.data(), sizeof(double) * N);
-  if (!s && cudaMemset(b->cnt, 0, 8 * sizeof(int)) != cudaSuccess) s = A2C_ERR_CUDA;
+  s = init_tables(b, params, n, true);
   if (s) {
     a2c_gpp_batch_destroy(b);
     return s;
@@ -970,7 +1119,7 @@ a2c_status a2c_gpp_batch_destroy(a2c_gpp_batch *b) {
                   (void *)b->loff, (void *)b->st, (void *)b->part})
     if (p) cudaFree(p);
   if (b->h_cnt) cudaFreeHost(b->h_cnt);
-  a2c_gpp_destroy(b->c);
+  if (!b->borrowed) a2c_gpp_destroy(b->c);
   delete b;
   return A2C_OK;
 }
@@ -1115,123 +1264,7 @@ a2c_status a2c_gpp_batch_eval(a2c_gpp_batch *b, const double *X, double *f, doub
 a2c_status a2c_gpp_batch_minimize(a2c_gpp_batch *b, double *X, const a2c_lbfgs_params *lp, double *fmin, int *iters,
                                   int *nfev, double *gnorm, int *reason, int *mixed_iters, int *fp64_iters) {
   if (!b || !X || !lp || !fmin || !iters || !nfev || !gnorm || !reason) return A2C_ERR_INVALID;
-  if (lp->m < 1 || lp->m > kMaxM || lp->max_ls < 1 || !(lp->sigma_lb > 0.0) || !(lp->init_step > 0.0) ||
-      lp->stall_window < 0 || lp->stall_window > 4096 || lp->max_fev < 1)
-    return A2C_ERR_INVALID;
-  a2c_gpp_ctx *c = b->c;
-  if (!c->has_neighbors) return A2C_ERR_STATE;
-  DeviceGuard dg(b->device);
-  const int64_t N = c->N;
-  for (int64_t t = 0; t < 4 * N; ++t)
-    if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
-  A2C_TRY(ensure_lbfgs(b, lp->m, lp->stall_window));
-  cudaStream_t s = c->stream;
-  Cfg cf{};
-  cf.B = b->B;
-  cf.m = lp->m;
-  cf.ring = lp->m + 1;
-  cf.max_it = lp->max_it;
-  cf.max_fev = lp->max_fev;
-  cf.max_ls = lp->max_ls;
-  cf.polish = b->precision == A2C_MIXED ? lp->polish : 0;
-  cf.W = lp->stall_window;
-  cf.nec = b->nec;
-  cf.nsc = b->nsc;
-  cf.n = 4 * N;
-  cf.gatol = lp->gatol;
-  cf.c1 = lp->c1;
-  cf.init_step = lp->init_step;
-  cf.lb = lp->sigma_lb;
-  cf.max_step = lp->max_step;
-  cf.fn_mixed = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-7;
-  cf.fn_fp64 = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-14;
-  cf.st_mixed = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-10;
-  cf.st_fp64 = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-14;
-  const int tps = default_tps(b);
-  if (b->precision == A2C_MIXED) A2C_TRY(mixed_prepare(c));
-  Dev D = dev_view(b);
-  cudaEvent_t e0, e1;
-  A2C_CUDA(cudaEventCreate(&e0));
-  A2C_CUDA(cudaEventCreate(&e1));
-  a2c_status st = A2C_OK;
-  auto fail = [&](a2c_status v) {
-    if (!st) st = v;
-  };
-  if (cudaMemcpyAsync(b->x, X, sizeof(double) * 4 * N, cudaMemcpyHostToDevice, s) != cudaSuccess) fail(A2C_ERR_CUDA);
-  cudaEventRecord(e0, s);
-  k_project_all<<<chunk_grid((4 * N + 255) / 256), 256, 0, s>>>(b->x, 4 * N, cf.lb);
-  k_init_state<<<(b->B + 127) / 128, 128, 0, s>>>(D, cf, b->precision == A2C_MIXED ? kPhaseMixed : kPhaseFp64);
-  if (cudaMemsetAsync(b->listed, 0xff, sizeof(int) * b->B, s) != cudaSuccess) fail(A2C_ERR_CUDA);
-  if (!st) fail(plan(b, D));
-  // the first tick (every instance's first evaluation) runs eagerly: it also
-  // performs the launchers' one-time occupancy queries outside any capture
-  if (!st) fail(tick(b, D, cf, tps));
-  // the captured tick, reused while the configuration is unchanged
-  const bool same = b->exec && b->exec_tps == tps && !std::memcmp(&b->exec_cfg, &cf, sizeof(Cfg));
-  if (!st && b->graphs && !same) {
-    if (b->exec) {
-      cudaGraphExecDestroy(b->exec);
-      b->exec = nullptr;
-    }
-    cudaGraph_t gr = nullptr;
-    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) fail(A2C_ERR_CUDA);
-    const a2c_status ts = st ? st : tick(b, D, cf, tps);
-    if (cudaStreamEndCapture(s, &gr) != cudaSuccess) fail(A2C_ERR_CUDA);
-    fail(ts);
-    if (!st && cudaGraphInstantiate(&b->exec, gr, 0) != cudaSuccess) fail(A2C_ERR_CUDA);
-    if (gr) cudaGraphDestroy(gr);
-    b->exec_cfg = cf;
-    b->exec_tps = tps;
-  }
-  // replay: K ticks, then read how many instances are left
-  const int K = 8;
-  const int64_t max_ticks = 2 * ((int64_t)lp->max_fev + 2) + 2 * K;
-  int64_t ticks = 1;
-  while (!st) {
-    for (int k = 0; k < K; ++k) {
-      if (b->graphs) {
-        if (cudaGraphLaunch(b->exec, s) != cudaSuccess) fail(A2C_ERR_CUDA);
-      } else {
-        fail(tick(b, D, cf, tps));
-      }
-    }
-    ticks += K;
-    if (cudaMemcpyAsync(b->h_cnt, b->cnt, 8 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      fail(A2C_ERR_CUDA);
-    if (st || b->h_cnt[kCntLeft] == 0) break;
-    if (ticks >= max_ticks) {
-      fail(A2C_ERR_STATE);
-      break;
-    }
-  }
-  cudaEventRecord(e1, s);
-  if (!st && cudaMemcpyAsync(X, b->x, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-    fail(A2C_ERR_CUDA);
-  std::vector<Inst> hs((size_t)b->B);
-  if (!st && cudaMemcpyAsync(hs.data(), b->st, sizeof(Inst) * b->B, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-    fail(A2C_ERR_CUDA);
-  if (cudaStreamSynchronize(s) != cudaSuccess) fail(A2C_ERR_CUDA);
-  float ms = 0.0f;
-  if (!st && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) b->seconds = 1e-3 * ms;
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  b->ticks = (int)ticks;
-  // a trial point with a non-finite objective is rejected by the line
-  // search; it is not an error of the minimization
-  cudaMemsetAsync(c->d_status, 0, sizeof(int), s);
-  if (st) return st;
-  for (int k = 0; k < b->B; ++k) {
-    fmin[k] = hs[k].f;
-    iters[k] = hs[k].it;
-    nfev[k] = hs[k].fev;
-    gnorm[k] = hs[k].gnorm;
-    reason[k] = hs[k].why;
-    if (mixed_iters) mixed_iters[k] = hs[k].mixed_iters;
-    if (fp64_iters) fp64_iters[k] = hs[k].phase == kPhaseFp64 ? hs[k].fp64_iters : 0;
-  }
-  c->has_state = true;
-  return A2C_OK;
+  return minimize_core(b, X, false, lp, fmin, iters, nfev, gnorm, reason, mixed_iters, fp64_iters, nullptr);
 }
 
 // Autotuner of the mixed form's threads per site over the whole batch at X
@@ -1290,3 +1323,52 @@ a2c_status a2c_gpp_batch_stats(a2c_gpp_batch *b, int *ticks, double *seconds) {
 }
 
 }  // extern "C"
+
+namespace a2c {
+
+// The device-driven minimizer for one context: the context wrapped as a
+// one-instance batch (its buffers and lists borrowed), so an L-BFGS
+// iteration is a captured tick replayed on the device instead of a host
+// loop with a synchronization per scalar.  Created at the first call.
+a2c_status engine_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp, double *fmin, int *iters,
+                           int *nfev, double *gnorm, int *reason) {
+  a2c_gpp_batch *b = (a2c_gpp_batch *)c->engine;
+  if (!b) {
+    b = new (std::nothrow) a2c_gpp_batch();
+    if (!b) return A2C_ERR_NOMEM;
+    b->B = 1;
+    b->device = c->device;
+    b->c = c;
+    b->borrowed = true;
+    b->P.assign(1, c->p);
+    const a2c_status s = init_tables(b, &c->p, 1, false);
+    if (s) {
+      a2c_gpp_batch_destroy(b);
+      return s;
+    }
+    c->engine = b;
+  }
+  b->precision = c->p.precision;
+  b->tps = mixed_threads_per_site(c);
+  std::vector<Inst> last;
+  int it = 0, fev = 0, why = 0;
+  double f = 0.0, gn = 0.0;
+  A2C_TRY(minimize_core(b, dX, true, lp, &f, &it, &fev, &gn, &why, nullptr, nullptr, &last));
+  *fmin = f;
+  *iters = it;
+  *nfev = fev;
+  *gnorm = gn;
+  *reason = why;
+  const Inst &I = last[0];
+  c->last_mixed_iters = b->precision == A2C_MIXED ? I.mixed_iters : 0;
+  c->last_fp64_iters = I.phase == kPhaseFp64 ? I.fp64_iters : 0;
+  c->last_mixed_gnorm = b->precision == A2C_MIXED ? I.mixed_gnorm : 0.0;
+  return A2C_OK;
+}
+
+void engine_free(a2c_gpp_ctx *c) {
+  if (c->engine) a2c_gpp_batch_destroy((a2c_gpp_batch *)c->engine);
+  c->engine = nullptr;
+}
+
+}  // namespace a2c

@@ -95,6 +95,8 @@ struct a2c_gpp_ctx {
   a2c::Mixed *mixed;
   a2c::Lbfgs *lbfgs;
   void *snap;  // the snapshot in flight (api.cu)
+  void *engine;     // the device-driven minimizer (batch.cu), created on first use
+  int host_loop;    // 1: mixed-precision minimization by the host loop (lbfgs.cu)
   double *h_small;  // pinned: f and the status word of a host-pointer call
   int last_mixed_iters, last_fp64_iters;
   double last_mixed_gnorm;
@@ -156,6 +158,11 @@ int mixed_threads_per_site(a2c_gpp_ctx *c);
 // batched: prep + both passes over the listed sites (G, Vs, Ss; no objective)
 a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, int tps);
 a2c_status mixed_prepare(a2c_gpp_ctx *c);  // tables and buffers, before any graph capture
+
+// batch.cu: the one-instance device-driven minimizer of a context
+a2c_status engine_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp, double *fmin, int *iters,
+                           int *nfev, double *gnorm, int *reason);
+void engine_free(a2c_gpp_ctx *c);
 
 // lbfgs.cu
 a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp, double *fmin, int *iters,

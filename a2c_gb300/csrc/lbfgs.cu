@@ -267,6 +267,12 @@ a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp
                           double *gnorm_out, int *reason) {
   if (!lp || lp->m < 1 || lp->m > 48 || lp->max_ls < 1 || !(lp->sigma_lb > 0.0) || !(lp->init_step > 0.0))
     return A2C_ERR_INVALID;
+  // Mixed precision: the same algorithm driven on the device (batch.cu, one
+  // instance; its global sums in the per-instance chunk order) unless the
+  // host loop below is asked for.  The FP64 plain form keeps the host loop,
+  // whose reductions the oracle replays bit for bit.
+  if (c->p.precision == A2C_MIXED && !c->host_loop)
+    return engine_minimize(c, dX, lp, fmin, iters, nfev, gnorm_out, reason);
   A2C_TRY(lbfgs_alloc(c, lp->m));
   Lbfgs *L = c->lbfgs;
   cudaStream_t st = c->stream;

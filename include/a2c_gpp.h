@@ -200,6 +200,13 @@ a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, d
  * evaluation of each candidate in milliseconds. */
 a2c_status a2c_gpp_autotune(a2c_gpp_ctx *ctx, int reps, int *tps, float *ms);
 
+/* Mixed-precision minimization (a2c_gpp_minimize, a2c_gpp_dmd_run) runs
+ * device-driven by default: each L-BFGS iteration is one CUDA-graph replay
+ * of the batched engine with this context as its only instance (global sums
+ * in the per-instance chunk order).  host_loop = 1 selects the host-driven
+ * loop instead (the FP64 plain form always uses it). */
+a2c_status a2c_gpp_set_minimizer(a2c_gpp_ctx *ctx, int host_loop);
+
 a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG);
 /* Profiling aid: one stream-ordered evaluation on device pointers with CUDA
  * events between its launches; stage_ms[4] receives the durations of the

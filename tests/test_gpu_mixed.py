@@ -136,3 +136,42 @@ def test_host_pointer_eval_pinned_equals_pageable(gpu):
         Xp.numpy()[:] = X
         A._native.check(call(), "a2c_gpp_eval")
         assert fv.value == f0 and np.array_equal(Gp.numpy(), G0)
+
+
+def test_device_driven_minimizer_matches_host_loop(gpu):
+    """Mixed-precision a2c_gpp_minimize runs as replayed CUDA-graph ticks of
+    the one-instance batch engine; it reaches the same minimum as the
+    host-driven loop (their global sums differ in order only), and after a
+    neighbor rebuild that reallocates the list array it re-captures."""
+    X, xH, _, box, nPd, nH = A.lattice_fcc(6, periodic=(1, 1, 1), pos_std=0.03, sigma=(0.08, 0.14), x_center=0.15,
+                                           x_half=0.15, seed=2)
+    res = {}
+    for host in (True, False):
+        with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), precision="mixed") as g:
+            g.set_occupancy(xH)
+            g.build_neighbors(X)
+            g.set_minimizer(host)
+            res[host] = g.minimize(X, gatol=1e-5, polish=0)
+            if not host:
+                again = g.minimize(X, gatol=1e-5, polish=0)  # replays the captured tick
+                assert np.array_equal(again.X, res[host].X) and again.iters == res[host].iters
+    for host, r in res.items():
+        assert r.reason in (A.CONVERGED_GATOL, A.CONVERGED_STALLED), (host, r.reason)
+    d = np.abs(res[True].X.reshape(-1, 4)[:, :3] - res[False].X.reshape(-1, 4)[:, :3]).max()
+    assert d < 2e-3, d
+    assert abs(res[True].fmin - res[False].fmin) <= 1e-9 * abs(res[True].fmin)
+    # re-capture after the list array moves: a 3% compression pulls the 4th
+    # Pd-Pd shell (5.50 A) inside rc, so the rebuilt lists need a larger array
+    Y = X.copy()
+    Y.reshape(-1, 4)[:, :3] *= 0.97
+    with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), precision="mixed") as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        g.minimize(X, gatol=1e-4, polish=0)  # captures with the first array
+        g.build_neighbors(Y)
+        r2 = g.minimize(Y, gatol=1e-5, max_it=300, polish=0)
+    with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), precision="mixed") as h:
+        h.set_occupancy(xH)
+        h.build_neighbors(Y)
+        ref = h.minimize(Y, gatol=1e-5, max_it=300, polish=0)
+    assert np.array_equal(r2.X, ref.X) and r2.iters == ref.iters
