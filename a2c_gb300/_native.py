@@ -160,6 +160,8 @@ def lib() -> C.CDLL:
         "a2c_gpp_batch_autotune": (I, [P, P, I, C.POINTER(I), P]),
         "a2c_gpp_autotune": (I, [P, I, C.POINTER(I), P]),
         "a2c_gpp_set_minimizer": (I, [P, I]),
+        "a2c_eam_analytic": (I, [I, P, C.c_int64, P, P]),
+        "a2c_mixed_table_eval": (I, [I, P, C.c_int64, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -183,7 +185,7 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_batch_create", "a2c_gpp_batch_destroy", "a2c_gpp_batch_info", "a2c_gpp_batch_set_occupancy",
             "a2c_gpp_batch_build_neighbors", "a2c_gpp_batch_set_threads_per_site", "a2c_gpp_batch_set_graphs",
             "a2c_gpp_batch_eval", "a2c_gpp_batch_minimize", "a2c_gpp_batch_stats", "a2c_gpp_batch_autotune",
-            "a2c_gpp_autotune", "a2c_gpp_set_minimizer"]
+            "a2c_gpp_autotune", "a2c_gpp_set_minimizer", "a2c_eam_analytic", "a2c_mixed_table_eval"]
 
 
 class A2CError(RuntimeError):

@@ -54,7 +54,7 @@ def _stale(out: Path, deps: list[Path]) -> bool:
 def build(verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+    headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((ROOT / "include").glob("*.h"))
     jobs = []
     objs = []
     nv = nvcc()

@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "internal.cuh"
+#include "tables.h"
 
 namespace a2c {
 
@@ -55,11 +56,6 @@ struct Mixed {
 
 namespace {
 
-constexpr double kTabR0 = 1.0;
-constexpr double kTabInvH = 160.0;
-constexpr int kTabN = 960;  // r in [1, 7): knots on the 5.0 / 5.05 A branch points
-constexpr double kEmbInvH = 64.0;
-constexpr int kEmbN = 4096;  // rho in [0, 64)
 constexpr int kBlock = 256;
 // Pass 2 resident blocks per SM the register allocation must allow (4
 // blocks of 256 threads = 64 registers per thread).

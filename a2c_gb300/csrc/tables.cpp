@@ -16,6 +16,8 @@
 #include <cstdint>
 #include <vector>
 
+#include "tables.h"
+
 namespace a2c {
 namespace tables {
 
@@ -85,6 +87,23 @@ Dual F_H(Dual rho) {
   return y * -c - rho * -0.0296604;
 }
 
+// potential.cpp:105-119 (the tail beyond 5.35 A continues the exponential)
+Dual f_H(Dual r) {
+  if (r.v > 5.35) return 0.009986990526578 * dexp((-0.013075667086408 / 0.009986990526578) * (r - 5.35));
+  return 11.0025 * dexp(-1.30927 * r);
+}
+
+// potential.cpp:162-177 and 185-200: D (b e^{-a (r - r0)} - a e^{-b (r - r0)}),
+// exponential tail beyond 5.35 A
+Dual morse(Dual r, double D, double a, double b, double r0, double fc, double fdc) {
+  if (r.v > 5.35) return fc * dexp((fdc / fc) * (r - 5.35));
+  return D * (b * dexp(-a * (r - r0)) - a * dexp(-b * (r - r0)));
+}
+Dual phi_PdH(Dual r) {
+  return morse(r, 0.2494540, 4.82613, 2.13158, 1.50964, -3.353001113951400e-04, 7.147062196813336e-04);
+}
+Dual phi_H(Dual r) { return morse(r, 0.0661496, 3.67263, 1.47797, 2.51980, -0.003702722457147, 0.005465945471933); }
+
 // cubic Hermite coefficients of [x0, x0+h] in t = (x - x0)/h
 void hermite(Dual p0, Dual p1, double h, float *c) {
   const double c0 = p0.v, c1 = h * p0.d;
@@ -145,3 +164,72 @@ void build_embed_table_raw(int species, double h, int n, float *out) {
 }
 
 }  // namespace a2c
+
+#include "a2c_gpp.h"
+
+// Value and analytic (forward-mode) derivative of an EAM function in FP64,
+// numbered like a2c_gpp_eam_eval's functions: 0 F_Pd, 2 F_H, 4 f_Pd, 6 f_H,
+// 8 phi_Pd, 10 phi_PdH, 12 phi_H.  The reference differentiates by central
+// differences (potential.cpp:40-205); these are the exact derivatives the
+// mixed form's tables are built from.
+extern "C" a2c_status a2c_eam_analytic(int which, const double *x, int64_t n, double *value, double *deriv) {
+  if (!x || !value || !deriv || n < 0 || which < 0 || which > 12 || (which & 1)) return A2C_ERR_INVALID;
+  using a2c::tables::Dual;
+  for (int64_t k = 0; k < n; ++k) {
+    const Dual d{x[k], 1.0};
+    Dual y{0.0, 0.0};
+    switch (which) {
+      case 0: y = a2c::tables::F_Pd(d); break;
+      case 2: y = a2c::tables::F_H(d); break;
+      case 4: y = a2c::tables::f_Pd(d, x[k]); break;
+      case 6: y = a2c::tables::f_H(d); break;
+      case 8: y = a2c::tables::phi_Pd(d, x[k]); break;
+      case 10: y = a2c::tables::phi_PdH(d); break;
+      default: y = a2c::tables::phi_H(d); break;
+    }
+    value[k] = y.v;
+    deriv[k] = y.d;
+  }
+  return A2C_OK;
+}
+
+namespace {
+float hv(const float *c, float t) { return std::fma(std::fma(std::fma(c[3], t, c[2]), t, c[1]), t, c[0]); }
+float hd(const float *c, float t) { return std::fma(std::fma(3.0f * c[3], t, 2.0f * c[2]), t, c[1]); }
+}  // namespace
+
+// The mixed form's FP32 table interpolants evaluated on the host with the
+// kernels' arithmetic (index clamp, cubic Hermite in FP32): which = 0 F_Pd,
+// 2 F_H (embedding tables), 4 f_Pd, 8 phi_Pd (pair tables).  For checking
+// the tables against a2c_eam_analytic.
+extern "C" a2c_status a2c_mixed_table_eval(int which, const double *x, int64_t n, double *value, double *deriv) {
+  if (!x || !value || !deriv || n < 0 || (which != 0 && which != 2 && which != 4 && which != 8)) return A2C_ERR_INVALID;
+  static std::vector<float> pair, embPd, embH;
+  static bool ready = false;
+  if (!ready) {
+    a2c::build_pair_table(a2c::kTabR0, 1.0 / a2c::kTabInvH, a2c::kTabN, pair);
+    a2c::build_embed_table(0, 1.0 / a2c::kEmbInvH, a2c::kEmbN, embPd);
+    a2c::build_embed_table(1, 1.0 / a2c::kEmbInvH, a2c::kEmbN, embH);
+    ready = true;
+  }
+  for (int64_t k = 0; k < n; ++k) {
+    const float s = (float)x[k];
+    if (which == 0 || which == 2) {
+      float u = std::fmin(std::fmax(s * (float)a2c::kEmbInvH, 0.0f), (float)a2c::kEmbN - 0.5f);
+      const int i = (int)u;
+      const float t = u - (float)i;
+      const float *c = (which == 0 ? embPd : embH).data() + 4 * i;
+      value[k] = hv(c, t);
+      deriv[k] = hd(c, t) * (float)a2c::kEmbInvH;
+    } else {
+      float u = (s - (float)a2c::kTabR0) * (float)a2c::kTabInvH;
+      u = std::fmin(std::fmax(u, 0.0f), (float)a2c::kTabN - 0.5f);
+      const int i = (int)u;
+      const float t = u - (float)i;
+      const float *c = pair.data() + 8 * i + (which == 4 ? 0 : 4);
+      value[k] = hv(c, t);
+      deriv[k] = hd(c, t) * (float)a2c::kTabInvH;
+    }
+  }
+  return A2C_OK;
+}

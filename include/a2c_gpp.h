@@ -192,6 +192,16 @@ a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, d
  * last call's contents; nothing in it needs clearing, but calls that
  * overlap on the GPU (two streams, two contexts on one device) race.
  * Stream-ordered on the context's stream, like a2c_gpp_eval_device. */
+/* Host-only checks of the mixed form's functions (no GPU needed).
+ * a2c_eam_analytic: value and exact derivative (forward mode, FP64) of the
+ * EAM function numbered as in a2c_gpp_eam_eval (0 F_Pd, 2 F_H, 4 f_Pd,
+ * 6 f_H, 8 phi_Pd, 10 phi_PdH, 12 phi_H), against which the reference's
+ * central differences (potential.cpp:40-205) converge at second order.
+ * a2c_mixed_table_eval: the FP32 table interpolants (0 F_Pd, 2 F_H, 4 f_Pd,
+ * 8 phi_Pd) with the kernels' arithmetic. */
+a2c_status a2c_eam_analytic(int which, const double *x, int64_t n, double *value, double *deriv);
+a2c_status a2c_mixed_table_eval(int which, const double *x, int64_t n, double *value, double *deriv);
+
 /* Autotuner (no reference counterpart): times the mixed-precision
  * evaluation at the context's current state (set by a2c_gpp_eval /
  * a2c_gpp_set_state) for 1, 2, 4 and 8 threads per site, `reps` timed
