@@ -506,10 +506,13 @@ def peak_flops(precision: int | str = A2C_MIXED, device: int = 0) -> float:
 def lattice_fcc(ncell, *, a: float = 3.89, periodic=(1, 1, 1), pos_std: float = 0.0, sigma=(0.1, 0.1),
                 x_mode: int = 0, x_center: float = 0.05, x_half: float = 0.0, x_matrix: float = 0.02,
                 x_nucleus: float = 0.6, nucleus_radius: float = 80.0, interface_width: float = 5.0,
-                xLb: float = 1e-3, xUb: float = 1.0 - 1e-16, seed: int = 1):
+                xLb: float = 1e-3, xUb: float = 1.0 - 1e-16, seed: int = 1, device_out=None):
     """Seeded fcc Pd + octahedral H lattice (a2c_lattice_fcc).
 
-    Returns (X, xH, surface, box, nPd, nH)."""
+    Returns (X, xH, surface, box, nPd, nH).  With device_out = (dX, dxH,
+    dsurface, stream) -- device pointers, a stream handle -- the lattice is
+    generated on the GPU instead (a2c_lattice_fcc_device) and None is
+    returned."""
     if isinstance(ncell, int):
         ncell = (ncell, ncell, ncell)
     sp = N.LatticeSpec()
@@ -522,6 +525,10 @@ def lattice_fcc(ncell, *, a: float = 3.89, periodic=(1, 1, 1), pos_std: float = 
     sp.x_matrix, sp.x_nucleus, sp.nucleus_radius, sp.interface_width = x_matrix, x_nucleus, nucleus_radius, \
         interface_width
     sp.xLb, sp.xUb, sp.seed = xLb, xUb, seed
+    if device_out is not None:  # (dX, dxH, dsurface) device pointers, stream
+        dX, dxH, dsf, stream = device_out
+        N.check(N.lib().a2c_lattice_fcc_device(C.byref(sp), dX, dxH, dsf, stream), "a2c_lattice_fcc_device")
+        return None
     nc = int(ncell[0]) * int(ncell[1]) * int(ncell[2])
     nPd = nH = 4 * nc
     X = np.empty(4 * (nPd + nH))

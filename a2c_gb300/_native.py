@@ -143,6 +143,7 @@ def lib() -> C.CDLL:
         "a2c_gpp_diffuse": (I, [P, D, D, D, D, D, P, P, P]),
         "a2c_gpp_macro_results": (I, [P, P, P, I, C.POINTER(D), C.POINTER(D)]),
         "a2c_lattice_fcc": (I, [C.POINTER(LatticeSpec), P, P, P]),
+        "a2c_lattice_fcc_device": (I, [C.POINTER(LatticeSpec), P, P, P, P]),
         "a2c_gpp_peak_flops": (I, [I, I, C.POINTER(D)]),
         "a2c_gpp_dmd_run": (I, [P, P, P, P, P, P, I, P, I, C.POINTER(DmdParams), I, P, P, P, P]),
         "a2c_restart_write": (I, [C.c_char_p, I, I, P, P, P, P, I, D]),
@@ -185,7 +186,8 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_batch_create", "a2c_gpp_batch_destroy", "a2c_gpp_batch_info", "a2c_gpp_batch_set_occupancy",
             "a2c_gpp_batch_build_neighbors", "a2c_gpp_batch_set_threads_per_site", "a2c_gpp_batch_set_graphs",
             "a2c_gpp_batch_eval", "a2c_gpp_batch_minimize", "a2c_gpp_batch_stats", "a2c_gpp_batch_autotune",
-            "a2c_gpp_autotune", "a2c_gpp_set_minimizer", "a2c_eam_analytic", "a2c_mixed_table_eval"]
+            "a2c_gpp_autotune", "a2c_gpp_set_minimizer", "a2c_eam_analytic", "a2c_mixed_table_eval",
+            "a2c_lattice_fcc_device"]
 
 
 class A2CError(RuntimeError):

@@ -26,8 +26,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                       "-I", str(ROOT / "include"), "-I", str(CSRC)]
 # translation units whose arithmetic must not be contracted into FMA
-NO_FMA = {"k_fp64.cu", "k_neighbors.cu", "k_misc.cu", "lbfgs.cu", "batch.cu"}
-CU_SOURCES = ["api.cu", "k_fp64.cu", "k_neighbors.cu", "k_misc.cu", "lbfgs.cu", "k_mixed.cu", "k_peak.cu", "batch.cu"]
+NO_FMA = {"k_fp64.cu", "k_neighbors.cu", "k_misc.cu", "lbfgs.cu", "batch.cu", "k_lattice.cu"}
+CU_SOURCES = ["api.cu", "k_fp64.cu", "k_neighbors.cu", "k_misc.cu", "lbfgs.cu", "k_mixed.cu", "k_peak.cu", "batch.cu", "k_lattice.cu"]
 CPP_SOURCES = ["lattice.cpp", "tables.cpp", "host_io.cpp", "snapshot.cpp", "input_reader.cpp"]
 
 

@@ -440,6 +440,14 @@ typedef struct a2c_lattice_spec {
   uint64_t seed;
 } a2c_lattice_spec;
 a2c_status a2c_lattice_fcc(const a2c_lattice_spec *spec, double *X, double *xH, int *surface);
+/* The same lattice generated on the device, one thread per site: device
+ * pointers X (4N), xH and surface (nH; may be NULL), stream-ordered on
+ * `stream` (a cudaStream_t, NULL = default stream).  Lattice positions,
+ * fixed widths and the deterministic occupancy profile are those of
+ * a2c_lattice_fcc; the random draws come from a counter-based SplitMix64
+ * stream (draw k of site s = output 8 s + k), so they follow the same
+ * distributions with other values. */
+a2c_status a2c_lattice_fcc_device(const a2c_lattice_spec *spec, double *X, double *xH, int *surface, void *stream);
 
 #ifdef __cplusplus
 }
