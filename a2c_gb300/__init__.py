@@ -13,12 +13,12 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _native as N
-from ._native import A2CError, A2C_FP64, A2C_MIXED  # noqa: F401
+from ._native import A2CError, A2C_FP64, A2C_MIXED, A2C_PAIRS_BOTH_SIDES, A2C_PAIRS_ONCE  # noqa: F401
 from ._native import (CONVERGED_GATOL, CONVERGED_STALLED, DIVERGED_LS_FAILURE, DIVERGED_MAXFCN,  # noqa: F401
                       DIVERGED_MAXITS, DIVERGED_NAN)
 
 __all__ = ["Gpp", "Batch", "BatchResult", "batch_workload", "lattice_fcc", "peak_flops", "restart_write",
-           "restart_read", "A2CError", "A2C_FP64", "A2C_MIXED", "LbfgsResult"]
+           "restart_read", "A2CError", "A2C_FP64", "A2C_MIXED", "A2C_PAIRS_BOTH_SIDES", "A2C_PAIRS_ONCE", "LbfgsResult"]
 
 
 @dataclass
@@ -107,6 +107,20 @@ class Gpp:
     def set_threads_per_site(self, tps: int) -> None:
         N.check(self._L.a2c_gpp_set_threads_per_site(self._h, int(tps)), "a2c_gpp_set_threads_per_site")
 
+    def set_pair_mode(self, mode: int | str) -> None:
+        """Mixed-precision pass 2: "once" (A2C_PAIRS_ONCE, default; each pair
+        evaluated by one of its sites) or "both" (A2C_PAIRS_BOTH_SIDES)."""
+        if isinstance(mode, str):
+            mode = {"both": A2C_PAIRS_BOTH_SIDES, "once": A2C_PAIRS_ONCE}[mode]
+        N.check(self._L.a2c_gpp_set_pair_mode(self._h, int(mode)), "a2c_gpp_set_pair_mode")
+
+    @property
+    def pair_mode(self) -> int:
+        """The pass 2 mode the current lists run with."""
+        m = C.c_int(0)
+        N.check(self._L.a2c_gpp_get_pair_mode(self._h, C.byref(m)), "a2c_gpp_get_pair_mode")
+        return m.value
+
     def synchronize(self) -> None:
         N.check(self._L.a2c_gpp_synchronize(self._h), "a2c_gpp_synchronize")
 
@@ -149,6 +163,19 @@ class Gpp:
         idx = np.zeros(max(tot.value, 1), dtype=np.int32)
         N.check(self._L.a2c_gpp_get_neighbors(self._h, list_id, N.ptr(off), N.ptr(idx)), "a2c_gpp_get_neighbors")
         return off, idx[: tot.value]
+
+    def set_neighbor_lists(self, X, lists: dict, PdPdnum=None) -> None:
+        """Lists in the reference's form (a2c_gpp_set_neighbor_lists): `lists`
+        maps LIST_PDPD, LIST_PDH, LIST_HPD, LIST_HH, LIST_HH1 to (offsets,
+        local indices); X (4N) fixes periodic images."""
+        arrs = []
+        for lid in (N.LIST_PDPD, N.LIST_PDH, N.LIST_HPD, N.LIST_HH, N.LIST_HH1):
+            o, i = lists[lid]
+            arrs += [np.ascontiguousarray(o, dtype=np.int64), np.ascontiguousarray(i, dtype=np.int32)]
+        Xa = None if X is None else np.ascontiguousarray(X, dtype=np.float64)
+        sh = None if PdPdnum is None else np.ascontiguousarray(PdPdnum, dtype=np.int32)
+        N.check(self._L.a2c_gpp_set_neighbor_lists(self._h, N.ptr(Xa), *[N.ptr(a) for a in arrs], N.ptr(sh)),
+                "a2c_gpp_set_neighbor_lists")
 
     def shell_counts(self) -> np.ndarray:
         s = np.zeros(3 * max(self.nPd, 1), dtype=np.int32)

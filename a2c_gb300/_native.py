@@ -25,6 +25,9 @@ A2C_ERR_NO_DEVICE = 8
 A2C_FP64 = 0
 A2C_MIXED = 1
 
+A2C_PAIRS_BOTH_SIDES = 0
+A2C_PAIRS_ONCE = 1
+
 LIST_PDPD, LIST_PDH, LIST_HPD, LIST_HH, LIST_HH1 = range(5)
 
 CONVERGED_GATOL = 3
@@ -113,6 +116,9 @@ def lib() -> C.CDLL:
         "a2c_gpp_set_precision": (I, [P, I]),
         "a2c_gpp_synchronize": (I, [P]),
         "a2c_gpp_set_threads_per_site": (I, [P, I]),
+        "a2c_gpp_set_pair_mode": (I, [P, I]),
+        "a2c_gpp_set_neighbor_lists": (I, [P] * 13),
+        "a2c_gpp_get_pair_mode": (I, [P, C.POINTER(C.c_int)]),
         "a2c_gpp_set_occupancy": (I, [P, P]),
         "a2c_gpp_get_occupancy": (I, [P, P]),
         "a2c_gpp_set_state": (I, [P, P]),
@@ -176,7 +182,8 @@ def exported_symbols() -> list[str]:
     """Names of the C ABI functions this binding expects the library to export."""
     return ["a2c_gpp_default_params", "a2c_lbfgs_default_params", "a2c_status_string", "a2c_gpp_create",
             "a2c_gpp_destroy", "a2c_gpp_stream", "a2c_gpp_set_precision", "a2c_gpp_synchronize",
-            "a2c_gpp_set_threads_per_site", "a2c_gpp_set_occupancy",
+            "a2c_gpp_set_threads_per_site", "a2c_gpp_set_pair_mode", "a2c_gpp_get_pair_mode", "a2c_gpp_set_neighbor_lists",
+            "a2c_gpp_set_occupancy",
             "a2c_gpp_get_occupancy", "a2c_gpp_set_state", "a2c_gpp_get_state", "a2c_gpp_build_neighbors",
             "a2c_gpp_neighbor_total", "a2c_gpp_set_neighbor_skin", "a2c_gpp_update_neighbors", "a2c_snapshot_begin", "a2c_input_read", "a2c_input_apply",
             "a2c_snapshot_write", "a2c_gpp_snapshot_async", "a2c_gpp_snapshot_wait", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",

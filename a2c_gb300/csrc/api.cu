@@ -260,6 +260,18 @@ a2c_status a2c_gpp_set_threads_per_site(a2c_gpp_ctx *c, int tps) {
   return mixed_set_threads_per_site(c, tps);
 }
 
+a2c_status a2c_gpp_set_pair_mode(a2c_gpp_ctx *c, int mode) {
+  if (!c) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  return mixed_set_pair_mode(c, mode);
+}
+
+a2c_status a2c_gpp_get_pair_mode(a2c_gpp_ctx *c, int *mode) {
+  if (!c || !mode) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  return mixed_get_pair_mode(c, mode);
+}
+
 // Autotuner of the mixed form's work mapping: each threads-per-site choice
 // (1, 2, 4, 8) evaluates the context's current state once untimed and then
 // `reps` times between two events on the context's stream; the fastest
@@ -372,6 +384,7 @@ a2c_status a2c_gpp_build_neighbors(a2c_gpp_ctx *c, const double *X, int *max_nei
   c->has_density = false;
   A2C_TRY(build_neighbors_device(c, X));
   c->has_neighbors = true;
+  A2C_TRY(mixed_lists_changed(c));
   if (max_neighbors) *max_neighbors = c->max_neighbors;
   return finish(c);
 }
@@ -466,6 +479,7 @@ a2c_status a2c_gpp_update_neighbors(a2c_gpp_ctx *c, const double *X, int *max_ne
   c->has_density = false;
   A2C_TRY(update_neighbors_device(c, X, rebuilt));
   c->has_neighbors = true;
+  A2C_TRY(mixed_lists_changed(c));
   if (max_neighbors) *max_neighbors = c->max_neighbors;
   return finish(c);
 }
@@ -560,7 +574,9 @@ a2c_status a2c_gpp_set_neighbor_lists(a2c_gpp_ctx *c, const double *X, const int
   c->nbr_total = total;
   c->hh1_total = total1;
   c->max_neighbors = maxn;
+  ++c->nbr_version;
   c->has_neighbors = true;
+  A2C_TRY(mixed_lists_changed(c));
   c->has_density = false;
   if (X && N > 0) {
     A2C_TRY(copy_in(c, c->d_X, X, 4 * N));

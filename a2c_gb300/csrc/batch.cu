@@ -704,6 +704,7 @@ struct a2c_gpp_batch {
   Cfg exec_cfg{};
   int exec_tps = -1;
   const void *exec_nbr = nullptr;
+  const void *exec_pass2[4] = {};  // the captured pass 2: mode and its index buffers
   bool borrowed = false;  // c belongs to a context (the one-instance engine)
   // statistics of the last minimization
   int ticks = 0;
@@ -993,8 +994,10 @@ a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_
   // performs the launchers' one-time occupancy queries outside any capture
   if (!st) fail(tick(b, D, cf, tps));
   // the captured tick, reused while the configuration is unchanged
+  const void *pass2[4];
+  mixed_graph_key(c, pass2);
   const bool same = b->exec && b->exec_tps == tps && b->exec_nbr == (const void *)c->d_nbr &&
-                    !std::memcmp(&b->exec_cfg, &cf, sizeof(Cfg));
+                    !std::memcmp(b->exec_pass2, pass2, sizeof(pass2)) && !std::memcmp(&b->exec_cfg, &cf, sizeof(Cfg));
   if (!st && b->graphs && !same) {
     if (b->exec) {
       cudaGraphExecDestroy(b->exec);
@@ -1010,6 +1013,7 @@ a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_
     b->exec_cfg = cf;
     b->exec_tps = tps;
     b->exec_nbr = c->d_nbr;
+    std::memcpy(b->exec_pass2, pass2, sizeof(pass2));
   }
   // replay: K ticks, then read how many instances are left
   const int K = 8;
@@ -1196,6 +1200,7 @@ a2c_status a2c_gpp_batch_build_neighbors(a2c_gpp_batch *b, const double *X, int 
   A2C_CUDA(cudaStreamSynchronize(c->stream));
   c->nbr_total = base;
   c->max_neighbors = maxn;
+  ++c->nbr_version;
   c->has_neighbors = true;
   if (max_neighbors) *max_neighbors = maxn;
   return A2C_OK;

@@ -76,6 +76,7 @@ struct a2c_gpp_ctx {
   int64_t *d_off;
   uint32_t *d_nbr;
   int64_t nbr_cap, nbr_total;
+  uint64_t nbr_version;  // bumped whenever the lists above change
   int *d_npd;
   int *d_shell;        // nPd x 3
   int64_t *d_hh1_off;  // nH+1
@@ -158,6 +159,14 @@ int mixed_threads_per_site(a2c_gpp_ctx *c);
 // batched: prep + both passes over the listed sites (G, Vs, Ss; no objective)
 a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, int tps);
 a2c_status mixed_prepare(a2c_gpp_ctx *c);  // tables and buffers, before any graph capture
+// pass 2 pair visiting (A2C_PAIRS_*); the pairs-once index is rebuilt when
+// the lists change (mixed_lists_changed, called after every list build)
+a2c_status mixed_set_pair_mode(a2c_gpp_ctx *c, int mode);
+a2c_status mixed_get_pair_mode(a2c_gpp_ctx *c, int *mode);
+a2c_status mixed_lists_changed(a2c_gpp_ctx *c);
+// what a captured batch tick bakes in of pass 2: the mode in use and the
+// pairs-once index buffers (a graph is re-captured when any of them changes)
+void mixed_graph_key(a2c_gpp_ctx *c, const void *key[4]);
 
 // batch.cu: the one-instance device-driven minimizer of a context
 a2c_status engine_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp, double *fmin, int *iters,

@@ -52,6 +52,18 @@ struct Mixed {
   int grid_cap[9] = {};       // persistent grid size per threads-per-site
   float4 *tabEmb = nullptr;   // per rho interval: F_Pd cubics, then F_H cubics
   int tps = 0;                // threads per site (0 = choose)
+  // Pass 2 with every pair evaluated once (sorted, symmetric lists): per
+  // list entry of a pair the site owns (neighbor id below its own) the slot
+  // of the reverse entry; per site the count of such entries, with the
+  // validation flag after the last site; per entry the contribution the
+  // neighbor's side receives from the owner.
+  int pair_mode = A2C_PAIRS_ONCE;
+  uint32_t *rev = nullptr;
+  int *npre = nullptr;
+  float4 *recv = nullptr;
+  int64_t sym_entries = 0, sym_sites = 0;  // capacities
+  uint64_t sym_version = ~0ull;            // list version the index was built for
+  bool sym_ok = false;
 };
 
 namespace {
@@ -79,6 +91,9 @@ struct MixArgs {
   double *G, *Vs, *Ss;
   double T;
   BatchView bv;  // batched list launch (LIST kernels)
+  const uint32_t *rev;  // pairs evaluated once (k_grad_once, k_grad_recv)
+  const int *npre;
+  float4 *recv;
 };
 
 __device__ __forceinline__ float ex2(float x) {
@@ -215,7 +230,7 @@ __device__ __forceinline__ void walk_neighbors(const MixArgs &a, int64_t begin, 
       if (FP) f1 = __ldg(&a.FF[j1].x);
     }
     if (t2 < end) e2 = __ldg(&a.nbr[t2]);
-    body(p0, x0, f0);
+    body(t, p0, x0, f0);
     p0 = p1;
     x0 = x1;
     f0 = f1;
@@ -246,7 +261,7 @@ __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
     const int4 pi = a.P[s];
     const float ui = kSqrt6 * __int_as_float(pi.w), ui2 = ui * ui;
     const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
-    walk_neighbors<false, false>(a, b + lane, m, TPS, [&](int4 pj, float, float) {  // Pd neighbors: f_Pd
+    walk_neighbors<false, false>(a, b + lane, m, TPS, [&](int64_t, int4 pj, float, float) {  // Pd neighbors: f_Pd
       const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
@@ -266,7 +281,7 @@ __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
       }
       kahan(acc, cmp, part);
     });
-    walk_neighbors<true, false>(a, m + lane, e, TPS, [&](int4 pj, float xj, float) {  // H neighbors: x_j f_H
+    walk_neighbors<true, false>(a, m + lane, e, TPS, [&](int64_t, int4 pj, float xj, float) {  // H neighbors: x_j f_H
       const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
@@ -302,9 +317,13 @@ __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
 // phi'_AB; the pair's gradient contributions are
 //   sum_k c_k r_k = D * sum_k c_k + e_m * sum over the points moving m of c_k delta_k
 //   sigma part    = sqrt(3) sum_m [ D_m (c_{+i} - c_{-i}) + ui (c_{+i} + c_{-i}) ]
-// scaled by W x_j; the energy is 0.5 W x_i x_j sum_k phi(s_k).
+// scaled by W x_j; the energy is 0.5 W x_i x_j sum_k phi(s_k).  c_k is
+// symmetric in the two sites, so the neighbor's side of the same pair is
+// -(D sum_k c_k + e) for its position and, for its width,
+//   sigj = sqrt(3) sum_m [ D_m (c_{+j} - c_{-j}) + uj (c_{+j} + c_{-j}) ]
+// in the notation below (c_{+j}: r = D + uj e_m, c_{-j}: r = D - uj e_m).
 struct PairAcc {
-  float csum, e[3], sig, v;
+  float csum, e[3], sig, v, sigj;
 };
 
 // True when all 12 quadrature points of the pair lie within the 5.35 A
@@ -328,6 +347,7 @@ __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, f
   p.csum = 0.0f;
   p.sig = 0.0f;
   p.v = 0.0f;
+  p.sigj = 0.0f;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     A2C_RADII(c, Dv[c])
@@ -368,6 +388,7 @@ __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, f
     p.csum += (cpi + cmi) + (cmj + cpj);
     p.e[c] = fmaf(ui, cpi - cmi, uj * (cpj - cmj));
     p.sig = fmaf(Dv[c], cpi - cmi, fmaf(ui, cpi + cmi, p.sig));
+    p.sigj = fmaf(Dv[c], cpj - cmj, fmaf(uj, cpj + cmj, p.sigj));
   }
 }
 
@@ -416,7 +437,7 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_mixed(MixA
     const bool iPd = R.iPd;
     const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
     const float hw = 0.5f * a.W * xi;
-    walk_neighbors<false, true>(a, b + lane, m, TPS, [&](int4 pj, float, float Fb) {  // Pd neighbors
+    walk_neighbors<false, true>(a, b + lane, m, TPS, [&](int64_t, int4 pj, float, float Fb) {  // Pd neighbors
       const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       PairAcc p;
@@ -429,7 +450,7 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_mixed(MixA
       }
       add_pair(A, p, D, a.W, hw);
     });
-    walk_neighbors<true, true>(a, m + lane, e, TPS, [&](int4 pj, float xj, float Fb) {  // H neighbors
+    walk_neighbors<true, true>(a, m + lane, e, TPS, [&](int64_t, int4 pj, float xj, float Fb) {  // H neighbors
       const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       PairAcc p;
@@ -461,6 +482,180 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_mixed(MixA
     a.Vs[s] = x * (double)ffi.y + tot[4];
     a.Ss[s] = (double)logf(sigi) * x;
   }
+  }
+}
+
+// ------------------------------------------------- pass 2, pairs once
+// The pair (i, j) with j < i is evaluated by site i alone: i keeps its share
+// (with the pair's whole energy, W x_i x_j sum_k phi) and stores j's share
+// -- W x_i (-(D sum_k c_k + e), sigj), the same c_k seen from j -- in the
+// slot of j's list that holds i (rev).  k_grad_recv then adds to every site
+// the shares stored in its own list, in list order.  Lists are sorted by
+// id, so a site's owned entries are the first npre of its list; Pd ids
+// precede H ids, so a Pd site owns Pd neighbors only and the pair types are
+// Pd-Pd (a Pd site), H-Pd and H-H (an H site).
+__device__ __forceinline__ void send_share(const MixArgs &a, int64_t t, const PairAcc &p, float3 D, float w) {
+  const uint32_t slot = __ldg(&a.rev[t]);
+  a.recv[slot] = make_float4(-w * fmaf(D.x, p.csum, p.e[0]), -w * fmaf(D.y, p.csum, p.e[1]),
+                             -w * fmaf(D.z, p.csum, p.e[2]), w * p.sigj);
+}
+
+template <int TPS, bool LIST>
+__global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_once(MixArgs a) {
+  constexpr int kSitesPerBlock = kBlock / TPS;
+  const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
+  if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
+  __shared__ float4 sF[kTabN], sP[kTabN];
+  for (int i = threadIdx.x; i < kTabN; i += blockDim.x) {
+    sF[i] = __ldg(&a.tabPair[2 * kTabN + i]);  // f_Pd' only
+    sP[i] = __ldg(&a.tabPair[kTabN + i]);
+  }
+  __syncthreads();
+  for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < n;
+       base += (int64_t)gridDim.x * kSitesPerBlock) {
+  const int64_t k = base + threadIdx.x / TPS;
+  const int lane = (int)(threadIdx.x % TPS);
+  const bool live = k < n;
+  SiteRef<LIST> R{};
+  if (live) R = site_ref<LIST>(a, k);
+  const int64_t s = R.s;
+  SiteAcc A;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) A.s[k] = A.c[k] = 0.0f;
+  float xi = 0.0f, sigi = 1.0f;
+  float2 ffi = make_float2(0.0f, 0.0f);
+  if (live) {
+    const int4 pi = a.P[s];
+    sigi = __int_as_float(pi.w);
+    const float ui = kSqrt6 * sigi;
+    xi = a.occ[s];
+    ffi = a.FF[s];
+    const bool iPd = R.iPd;
+    const int64_t b = a.off[s], m = b + a.npd[s], p = b + a.npre[s];
+    const float w = a.W * xi;  // the neighbor's share and the pair energy carry W x_i
+    walk_neighbors<false, true>(a, b + lane, m < p ? m : p, TPS, [&](int64_t t, int4 pj, float, float Fb) {
+      const float3 D = pair_vec(R.sc, pi, pj);
+      const float uj = kSqrt6 * __int_as_float(pj.w);
+      PairAcc q;
+      if (iPd) {
+        pair_terms<0>(sF, sP, ffi.x, Fb, D, ui, uj, q);
+      } else if (pair_inside(D, ui, uj)) {
+        pair_terms<2, false>(sF, sP, ffi.x, Fb, D, ui, uj, q);
+      } else {
+        pair_terms<2, true>(sF, sP, ffi.x, Fb, D, ui, uj, q);
+      }
+      add_pair(A, q, D, a.W, w);
+      send_share(a, t, q, D, w);
+    });
+    walk_neighbors<true, true>(a, m + lane, p, TPS, [&](int64_t t, int4 pj, float xj, float Fb) {  // H site, H j < i
+      const float3 D = pair_vec(R.sc, pi, pj);
+      const float uj = kSqrt6 * __int_as_float(pj.w);
+      PairAcc q;
+      if (pair_inside(D, ui, uj)) pair_terms<3, false>(sF, sP, ffi.x, Fb, D, ui, uj, q);
+      else pair_terms<3, true>(sF, sP, ffi.x, Fb, D, ui, uj, q);
+      add_pair(A, q, D, a.W * xj, w * xj);
+      send_share(a, t, q, D, w);
+    });
+  }
+  double tot[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    float v = A.s[k] - A.c[k];
+#pragma unroll
+    for (int o = TPS / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    tot[k] = (double)v;
+  }
+  if (live && lane == 0) {
+    const double x = xi, sg = sigi, invT = 1.0 / R.T;
+    a.G[4 * s] = tot[0] * (invT * x);
+    a.G[4 * s + 1] = tot[1] * (invT * x);
+    a.G[4 * s + 2] = tot[2] * (invT * x);
+    a.G[4 * s + 3] = tot[3] * (1.7320508075688772 * 1.4142135623730951 * invT * x) - 3.0 * kB / sg * x;
+    a.Vs[s] = x * (double)ffi.y + tot[4];
+    a.Ss[s] = (double)logf(sigi) * x;
+  }
+  }
+}
+
+// The shares a site received (its list entries after the first npre),
+// summed in list order with compensation and added to its gradient.
+template <int TPS, bool LIST>
+__global__ void __launch_bounds__(kBlock) k_grad_recv(MixArgs a) {
+  constexpr int kSitesPerBlock = kBlock / TPS;
+  const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
+  for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < n;
+       base += (int64_t)gridDim.x * kSitesPerBlock) {
+    const int64_t k = base + threadIdx.x / TPS;
+    const int lane = (int)(threadIdx.x % TPS);
+    const bool live = k < n;
+    SiteRef<LIST> R{};
+    if (live) R = site_ref<LIST>(a, k);
+    const int64_t s = R.s;
+    float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f}, cmp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (live) {
+      const int64_t e = a.off[s + 1];
+      for (int64_t t = a.off[s] + a.npre[s] + lane; t < e; t += TPS) {
+        const float4 v = __ldcs(&a.recv[t]);
+        kahan(sum[0], cmp[0], v.x);
+        kahan(sum[1], cmp[1], v.y);
+        kahan(sum[2], cmp[2], v.z);
+        kahan(sum[3], cmp[3], v.w);
+      }
+    }
+    double tot[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      float v = sum[c] - cmp[c];
+#pragma unroll
+      for (int o = TPS / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      tot[c] = (double)v;
+    }
+    if (live && lane == 0) {
+      const double x = a.occ[s], invT = 1.0 / R.T;
+      a.G[4 * s] += tot[0] * (invT * x);
+      a.G[4 * s + 1] += tot[1] * (invT * x);
+      a.G[4 * s + 2] += tot[2] * (invT * x);
+      a.G[4 * s + 3] += tot[3] * (1.7320508075688772 * 1.4142135623730951 * invT * x);
+    }
+  }
+}
+
+// The index of the pairs-once scheme for lists off/nbr over sites [0, N):
+// per site the count of neighbors with a smaller id (npre), per owned entry
+// the slot of the reverse entry (rev).  Sets *bad when a list is not
+// strictly increasing, holds the site itself or an id out of range, or
+// lacks the reverse of an entry (asymmetric lists).
+__global__ void k_sym_index(int64_t N, const int64_t *off, const uint32_t *nbr, uint32_t *rev, int *npre, int *bad) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < N; s += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = off[s], e = off[s + 1];
+    int64_t p = b;
+    bool ok = true;
+    uint32_t prev = 0;
+    for (int64_t t = b; t < e; ++t) {
+      const uint32_t id = nbr[t] & kIdMask;
+      if ((t > b && id <= prev) || (int64_t)id == s || (int64_t)id >= N) ok = false;
+      prev = id;
+      if ((int64_t)id < s) p = t + 1;
+    }
+    npre[s] = (int)(p - b);
+    if (!ok) {
+      atomicOr(bad, 1);
+      continue;
+    }
+    for (int64_t t = b; t < p; ++t) {
+      const int64_t j = nbr[t] & kIdMask;
+      int64_t lo = off[j], hi = off[j + 1];
+      while (lo < hi) {  // first entry of j's list with id >= s
+        const int64_t mid = lo + ((hi - lo) >> 1);
+        if ((int64_t)(nbr[mid] & kIdMask) < s) lo = mid + 1;
+        else hi = mid;
+      }
+      if (lo >= off[j + 1] || (int64_t)(nbr[lo] & kIdMask) != s) {
+        atomicOr(bad, 1);
+        break;
+      }
+      rev[t] = (uint32_t)lo;
+    }
   }
 }
 
@@ -509,22 +704,36 @@ __global__ void k_prep_list(const double *X, const double *occ, BatchView bv, in
 // Persistent grids: as many blocks as fit on the device at once (occupancy
 // query, cached per kernel), capped by the work (for a list launch, by the
 // largest list the system can have).
+// once = true: pass 2 evaluates every pair once (k_grad_once + k_grad_recv;
+// a.rev, a.npre, a.recv set), else from both sides (k_grad_mixed).
+constexpr int kRecvTps = 8;  // lanes per site summing the received shares
 template <int TPS, bool LIST>
-void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev) {
-  static int cap[2] = {0, 0};
+void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, bool once = false) {
+  static int cap[4] = {0, 0, 0, 0};
   if (!cap[0]) {
-    int dev = 0, sms = 0, b0 = 0, b1 = 0;
+    int dev = 0, sms = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_rho_mixed<TPS, LIST>, kBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_grad_mixed<TPS, LIST>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_grad_once<TPS, LIST>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_grad_recv<kRecvTps, LIST>, kBlock, 0);
     cap[0] = std::max(1, sms * b0);
     cap[1] = std::max(1, sms * b1);
+    cap[2] = std::max(1, sms * b2);
+    cap[3] = std::max(1, sms * b3);
   }
   const int64_t need = (a.N * TPS + kBlock - 1) / kBlock;
   k_rho_mixed<TPS, LIST><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[0])), kBlock, 0, st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
-  k_grad_mixed<TPS, LIST><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[1])), kBlock, 0, st>>>(a);
+  if (once) {
+    k_grad_once<TPS, LIST><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[2])), kBlock, 0, st>>>(a);
+    const int64_t need_r = (a.N * kRecvTps + kBlock - 1) / kBlock;
+    k_grad_recv<kRecvTps, LIST>
+        <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need_r, cap[3])), kBlock, 0, st>>>(a);
+  } else {
+    k_grad_mixed<TPS, LIST><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[1])), kBlock, 0, st>>>(a);
+  }
   if (ev) cudaEventRecord(ev[3], st);
 }
 
@@ -574,12 +783,102 @@ a2c_status ensure_mixed(a2c_gpp_ctx *c) {
   return A2C_OK;
 }
 
+// The pairs-once index for the context's current lists (k_sym_index),
+// rebuilt when the lists changed.  Lists it cannot serve (unsorted,
+// asymmetric, or 2^32 entries and more) and a failed allocation leave
+// sym_ok false: pass 2 then visits pairs from both sides.
+a2c_status ensure_sym(a2c_gpp_ctx *c) {
+  Mixed *M = c->mixed;
+  if (M->sym_version == c->nbr_version) return A2C_OK;
+  M->sym_ok = false;
+  const int64_t N = c->N, E = c->nbr_total;
+  cudaStream_t st = c->stream;
+  if (N == 0 || E >= (int64_t)0xffffffffLL) {
+    M->sym_version = c->nbr_version;
+    return A2C_OK;
+  }
+  if (E > M->sym_entries) {
+    if (M->rev) cudaFree(M->rev);
+    if (M->recv) cudaFree(M->recv);
+    M->rev = nullptr;
+    M->recv = nullptr;
+    M->sym_entries = 0;
+    if (cudaMalloc(&M->rev, sizeof(uint32_t) * E) != cudaSuccess ||
+        cudaMalloc(&M->recv, sizeof(float4) * E) != cudaSuccess) {
+      (void)cudaGetLastError();  // out of memory: keep the both-sides pass
+      M->sym_version = c->nbr_version;
+      return A2C_OK;
+    }
+    M->sym_entries = E;
+  }
+  if (N + 1 > M->sym_sites) {
+    if (M->npre) cudaFree(M->npre);
+    M->npre = nullptr;
+    M->sym_sites = 0;
+    if (cudaMalloc(&M->npre, sizeof(int) * (N + 1)) != cudaSuccess) {
+      (void)cudaGetLastError();
+      M->sym_version = c->nbr_version;
+      return A2C_OK;
+    }
+    M->sym_sites = N + 1;
+  }
+  A2C_CUDA(cudaMemsetAsync(M->npre + N, 0, sizeof(int), st));
+  int dev = 0, sms = 0;
+  A2C_CUDA(cudaGetDevice(&dev));
+  A2C_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  k_sym_index<<<(unsigned)std::min<int64_t>(grid_for(N, 256), 8 * (int64_t)sms), 256, 0, st>>>(
+      N, c->d_off, c->d_nbr, M->rev, M->npre, M->npre + N);
+  A2C_CUDA(cudaGetLastError());
+  int bad = 1;
+  A2C_CUDA(cudaMemcpyAsync(&bad, M->npre + N, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaStreamSynchronize(st));
+  M->sym_ok = bad == 0;
+  M->sym_version = c->nbr_version;
+  return A2C_OK;
+}
+
+// Outside a stream capture: bring the pairs-once index up to date.  Under
+// capture the index is used only if it is already current.
+a2c_status refresh_sym(a2c_gpp_ctx *c) {
+  Mixed *M = c->mixed;
+  if (M->pair_mode != A2C_PAIRS_ONCE || M->sym_version == c->nbr_version) return A2C_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  A2C_CUDA(cudaStreamIsCapturing(c->stream, &cs));
+  return cs == cudaStreamCaptureStatusNone ? ensure_sym(c) : A2C_OK;
+}
+
+bool use_once(const a2c_gpp_ctx *c) {
+  const Mixed *M = c->mixed;
+  return M->pair_mode == A2C_PAIRS_ONCE && M->sym_ok && M->sym_version == c->nbr_version;
+}
+
 }  // namespace
+
+a2c_status mixed_lists_changed(a2c_gpp_ctx *c) {
+  if (c->p.precision != A2C_MIXED && !c->mixed) return A2C_OK;
+  A2C_TRY(ensure_mixed(c));
+  return refresh_sym(c);
+}
+
+a2c_status mixed_set_pair_mode(a2c_gpp_ctx *c, int mode) {
+  if (mode != A2C_PAIRS_BOTH_SIDES && mode != A2C_PAIRS_ONCE) return A2C_ERR_INVALID;
+  A2C_TRY(ensure_mixed(c));
+  c->mixed->pair_mode = mode;
+  return A2C_OK;
+}
+
+a2c_status mixed_get_pair_mode(a2c_gpp_ctx *c, int *mode) {
+  A2C_TRY(ensure_mixed(c));
+  if (c->has_neighbors) A2C_TRY(refresh_sym(c));
+  *mode = (c->has_neighbors && use_once(c)) ? A2C_PAIRS_ONCE : A2C_PAIRS_BOTH_SIDES;
+  return A2C_OK;
+}
 
 void mixed_free(a2c_gpp_ctx *c) {
   Mixed *M = c->mixed;
   if (!M) return;
-  for (void *p : {(void *)M->P, (void *)M->occ, (void *)M->FF, (void *)M->tabPair, (void *)M->tabEmb})
+  for (void *p : {(void *)M->P, (void *)M->occ, (void *)M->FF, (void *)M->tabPair, (void *)M->tabEmb,
+                  (void *)M->rev, (void *)M->npre, (void *)M->recv})
     if (p) cudaFree(p);
   delete M;
   c->mixed = nullptr;
@@ -620,6 +919,11 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   a.Vs = c->d_Vs;
   a.Ss = c->d_Ss;
   a.T = c->p.T;
+  if (N > 0) A2C_TRY(refresh_sym(c));
+  const bool once = N > 0 && use_once(c);
+  a.rev = M->rev;
+  a.npre = M->npre;
+  a.recv = M->recv;
   if (ev) cudaEventRecord(ev[0], c->stream);
   if (N > 0) {
     if (Xcopy)
@@ -631,10 +935,10 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
     if (ev) cudaEventRecord(ev[1], c->stream);
     int tps = M->tps ? M->tps : (N < 152 * 2048 ? 4 : 1);
     switch (tps) {
-      case 1: launch_pair_kernels<1, false>(a, c->stream, ev); break;
-      case 2: launch_pair_kernels<2, false>(a, c->stream, ev); break;
-      case 4: launch_pair_kernels<4, false>(a, c->stream, ev); break;
-      default: launch_pair_kernels<8, false>(a, c->stream, ev); break;
+      case 1: launch_pair_kernels<1, false>(a, c->stream, ev, once); break;
+      case 2: launch_pair_kernels<2, false>(a, c->stream, ev, once); break;
+      case 4: launch_pair_kernels<4, false>(a, c->stream, ev, once); break;
+      default: launch_pair_kernels<8, false>(a, c->stream, ev, once); break;
     }
     A2C_CUDA(cudaGetLastError());
   } else if (ev) {
@@ -645,7 +949,19 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   return A2C_OK;
 }
 
-a2c_status mixed_prepare(a2c_gpp_ctx *c) { return ensure_mixed(c); }
+a2c_status mixed_prepare(a2c_gpp_ctx *c) {
+  A2C_TRY(ensure_mixed(c));
+  return refresh_sym(c);
+}
+
+void mixed_graph_key(a2c_gpp_ctx *c, const void *key[4]) {
+  const Mixed *M = c->mixed;
+  const bool once = M && use_once(c);
+  key[0] = once ? (const void *)c : nullptr;
+  key[1] = M ? (const void *)M->rev : nullptr;
+  key[2] = M ? (const void *)M->npre : nullptr;
+  key[3] = M ? (const void *)M->recv : nullptr;
+}
 
 a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, int tps) {
   A2C_TRY(ensure_mixed(c));
@@ -667,6 +983,11 @@ a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const B
   a.Vs = c->d_Vs;
   a.Ss = c->d_Ss;
   a.bv = bv;
+  A2C_TRY(refresh_sym(c));
+  const bool once = use_once(c);
+  a.rev = M->rev;
+  a.npre = M->npre;
+  a.recv = M->recv;
   static int prep_cap = 0;
   if (!prep_cap) {
     int dev = 0, sms = 0;
@@ -677,10 +998,10 @@ a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const B
   k_prep_list<<<(unsigned)std::min<int64_t>(grid_for(N, 256), prep_cap), 256, 0, c->stream>>>(dX, c->d_occ, bv, M->P,
                                                                                                M->occ);
   switch (tps) {
-    case 1: launch_pair_kernels<1, true>(a, c->stream, nullptr); break;
-    case 2: launch_pair_kernels<2, true>(a, c->stream, nullptr); break;
-    case 4: launch_pair_kernels<4, true>(a, c->stream, nullptr); break;
-    default: launch_pair_kernels<8, true>(a, c->stream, nullptr); break;
+    case 1: launch_pair_kernels<1, true>(a, c->stream, nullptr, once); break;
+    case 2: launch_pair_kernels<2, true>(a, c->stream, nullptr, once); break;
+    case 4: launch_pair_kernels<4, true>(a, c->stream, nullptr, once); break;
+    default: launch_pair_kernels<8, true>(a, c->stream, nullptr, once); break;
   }
   A2C_CUDA(cudaGetLastError());
   return A2C_OK;

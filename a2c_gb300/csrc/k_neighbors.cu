@@ -393,6 +393,7 @@ a2c_status make_lists(a2c_gpp_ctx *c, const GridArgs &g, Src src, bool ext) {
   A2C_CUDA(cudaMemcpyAsync(&stat, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
   A2C_CUDA(cudaStreamSynchronize(st));
   if (stat & kStatusBadIndex) return A2C_ERR_STATE;
+  if (!ext) ++c->nbr_version;
   return A2C_OK;
 }
 

@@ -20,6 +20,12 @@ Per neighbor pair (12 pair-points) of site species A and neighbor species B:
             -> Pd-Pd 515, Pd-H / H-Pd 661, H-H 481
 Per site: pass 1 finish 15 (embedding table), pass 2 finish 25.
 
+Pass 2 with every pair evaluated once (A2C_PAIRS_ONCE): each unordered pair
+costs its type's count above plus 28 for the neighbor's share (its width
+sum, 18, and the scaled position share, 10); each received share costs 16
+(four compensated adds) and each site 10 more to finish.  flops_pairs_once
+gives these executed counts; flops() stays the frozen both-sides count.
+
 Algorithmic bytes per atom-eval: the site's own state read twice (16 B),
 its CSR bounds and Pd split (20 B) and neighbor entries (4 B each) read once
 per pass, occupancy and F'(rho) (8 B), written F'/F (8 B), gradient (32 B)
@@ -45,3 +51,17 @@ def flops(n_pdpd: int, n_pdh: int, n_hpd: int, n_hh: int, n_sites: int) -> dict:
 def algorithmic_bytes(n_sites: int, n_entries: int) -> float:
     """Minimal HBM bytes of one evaluation (both passes)."""
     return float(132 * n_sites + 8 * n_entries)
+
+
+PASS2_SHARE = 28  # neighbor's share of a pair evaluated once
+PASS2_RECV = 16   # one received share, compensated
+PASS2_RECV_SITE = 10
+
+
+def flops_pairs_once(n_pdpd: int, n_pdh: int, n_hpd: int, n_hh: int, n_sites: int) -> float:
+    """Executed FLOPs of pass 2 when every pair is evaluated once (by one of
+    its sites) and the other site's share is stored and summed."""
+    pairs = (n_pdpd // 2) * (PASS2_PAIR["PdPd"] + PASS2_SHARE) + n_hpd * (PASS2_PAIR["HPd"] + PASS2_SHARE) + \
+        (n_hh // 2) * (PASS2_PAIR["HH"] + PASS2_SHARE)
+    received = (n_pdpd // 2) + n_pdh + (n_hh // 2)
+    return float(pairs + received * PASS2_RECV + n_sites * (PASS2_SITE + PASS2_RECV_SITE))

@@ -545,6 +545,7 @@ def run_ours(args):
         o, _ = g.neighbors(lid)
         tot[k] = int(o[-1])
     fl = flop_model.flops(tot["PdPd"], tot["PdH"], tot["HPd"], tot["HH"], Ns)
+    fl_once = flop_model.flops_pairs_once(tot["PdPd"], tot["PdH"], tot["HPd"], tot["HH"], Ns)
     n_entries = sum(tot.values())
 
     stream = torch.cuda.ExternalStream(g.stream, device=dev)
@@ -559,14 +560,22 @@ def run_ours(args):
             flush.fill_(1.0)
         return g.profile_eval(dX.data_ptr(), df.data_ptr(), dG.data_ptr())
 
-    # autotune the threads-per-site mapping of the mixed kernels
+    # autotune the threads-per-site mapping and the pass 2 pair mode of the
+    # mixed kernels (pairs once: each pair evaluated by one of its sites;
+    # both: every site gathers over all its pairs)
     tune = {}
-    for tps in (1, 2, 4, 8):
-        g.set_threads_per_site(tps)
-        step_profiled()
-        tune[tps] = min(float(np.sum(step_profiled())) for _ in range(3))
-    best = min(tune, key=tune.get)
+    for mode in ("once", "both"):
+        g.set_pair_mode(mode)
+        for tps in (1, 2, 4, 8):
+            g.set_threads_per_site(tps)
+            step_profiled()
+            tune[f"{mode}/{tps}"] = min(float(np.sum(step_profiled())) for _ in range(3))
+    best_key = min(tune, key=tune.get)
+    mode = best_key.split("/")[0]
+    best = int(best_key.split("/")[1])
+    g.set_pair_mode(mode)
     g.set_threads_per_site(best)
+    once = g.pair_mode == A.A2C_PAIRS_ONCE
 
     def barrier():
         if world > 1:
@@ -591,6 +600,19 @@ def run_ours(args):
     clocks = clk.summary()
     f_mixed = df.item()
     G_mixed = dG.cpu().numpy()
+
+    # the other pair mode at its best mapping, for comparison (not the headline)
+    modes = {mode: {"threads_per_site": best, "pass2_ms": float(np.mean(st_mixed[:, 2])),
+                    "eval_ms": float(np.mean(st_mixed.sum(axis=1)))}}
+    other = "both" if mode == "once" else "once"
+    okey = min((k for k in tune if k.startswith(other)), key=tune.get)
+    g.set_pair_mode(other)
+    g.set_threads_per_site(int(okey.split("/")[1]))
+    st_other = timed(max(3, args.steps // 2), 2)
+    modes[other] = {"threads_per_site": int(okey.split("/")[1]), "pass2_ms": float(np.mean(st_other[:, 2])),
+                    "eval_ms": float(np.mean(st_other.sum(axis=1)))}
+    g.set_pair_mode(mode)
+    g.set_threads_per_site(best)
 
     # FP64 plain form on the same state
     g.set_precision("fp64")
@@ -639,7 +661,8 @@ def run_ours(args):
     pass1_ms = float(np.mean(st_mixed[:, 1]))
     peak32 = A.peak_flops("fp32", dev)
     peak64 = A.peak_flops("fp64", dev)
-    ach = fl["pass2"] / (pass2_ms * 1e-3)
+    exec2 = fl_once if once else fl["pass2"]  # FLOPs the kernels execute
+    ach = exec2 / (pass2_ms * 1e-3)
     pass2_64_ms = float(np.mean(st_64[:, 2]))
     traffic = None
     tfile = ROOT / "profiles" / "traffic.json"
@@ -648,12 +671,17 @@ def run_ours(args):
             traffic = json.loads(tfile.read_text()).get("k_grad_mixed_bytes_per_launch")
         except Exception:
             traffic = None
-    roofline = {"bound": "fp32", "kernel": f"k_grad_mixed<{best}> (pass 2)", "achieved": ach / 1e12,
+    kname = f"k_grad_once<{best}> + k_grad_recv<8> (pass 2, pairs once)" if once else \
+        f"k_grad_mixed<{best}> (pass 2)"
+    roofline = {"bound": "fp32", "kernel": kname, "achieved": ach / 1e12,
                 "peak": peak32 / 1e12, "unit": "TFLOP/s", "frac": ach / peak32,
                 "peak_source": "measured in this run: FP32 FMA-chain kernel (a2c_gpp_peak_flops); "
                                "MEASURED_PEAKS.json holds only HBM and bf16-tensor peaks and no tensor core "
                                "is used here",
-                "flops_per_launch": fl["pass2"], "traffic": traffic,
+                "flops_per_launch": exec2, "flops_counted": "executed" if once else "frozen model",
+                "model_flops_per_launch": fl["pass2"],
+                "model_achieved": fl["pass2"] / (pass2_ms * 1e-3) / 1e12,
+                "model_frac": fl["pass2"] / (pass2_ms * 1e-3) / peak32, "traffic": traffic,
                 "hbm_frac": (flop_model.algorithmic_bytes(Ns, n_entries) / ((pass1_ms + pass2_ms) * 1e-3)) /
                             (measured_peaks().get("hbm_gbs", 6800.0) * 1e9),
                 "pass1": {"ms": pass1_ms, "achieved_tflops": fl["pass1"] / (pass1_ms * 1e-3) / 1e12},
@@ -681,18 +709,18 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": dev_time_mixed * 1e3 / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": config_dict({"parallelism": f"replicas x{world}", "threads_per_site": best,
-                                       "autotune_ms": tune}),
+                                       "pair_mode": mode, "autotune_ms": tune}),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * 4 * Ns,
                         "d2h_bytes_per_step": 8 * 4 * Ns + 8},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-                "gpu_launches": 5 * args.steps,
+                "gpu_launches": (6 if once else 5) * args.steps,
                 "fp64_plain": {"value": value_64, "unit": UNIT, "steps": args.fp64_steps,
                                "ms_per_step": dev_time_64 * 1e3 / args.fp64_steps},
                 "mixed_over_fp64": value / value_64,
                 "mixed_error_vs_fp64": {"free_entropy_rel": rel_f, "gradient_rel_2norm": rel_g},
                 "stages_ms_mixed": {"prep": float(np.mean(st_mixed[:, 0])), "pass1": pass1_ms, "pass2": pass2_ms,
                                     "reduce": float(np.mean(st_mixed[:, 3]))},
-                "time_to_minimum": ttm, "neighbor_lists": nb}
+                "pass2_pair_modes": modes, "time_to_minimum": ttm, "neighbor_lists": nb}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

@@ -119,9 +119,21 @@ a2c_status a2c_gpp_destroy(a2c_gpp_ctx *ctx);
 void *a2c_gpp_stream(a2c_gpp_ctx *ctx);
 a2c_status a2c_gpp_set_precision(a2c_gpp_ctx *ctx, int precision);
 /* Threads per site of the mixed-precision kernels: 1, 2, 4 or 8, or 0 to
- * let the library choose (the autotuner in a2c_gb300/autotune.py measures
- * the candidates and sets the fastest). */
+ * let the library choose (a2c_gpp_autotune measures the candidates and sets
+ * the fastest). */
 a2c_status a2c_gpp_set_threads_per_site(a2c_gpp_ctx *ctx, int tps);
+/* How the mixed-precision pass 2 visits pairs.  A2C_PAIRS_ONCE (default):
+ * each pair is evaluated once, by the site with the larger id, which keeps
+ * its own share and stores the neighbor's share in the neighbor's list slot
+ * of the pair; a second kernel sums each site's received shares in list
+ * order, so results are deterministic.  It needs every list sorted by id
+ * and the lists symmetric, as the library's builds make them; other lists
+ * (a2c_gpp_set_neighbor_lists input that is not) use A2C_PAIRS_BOTH_SIDES: each
+ * site evaluates all of its pairs, the gather of minimizer.cpp:162-351.
+ * a2c_gpp_get_pair_mode reports the mode the current lists run with. */
+enum { A2C_PAIRS_BOTH_SIDES = 0, A2C_PAIRS_ONCE = 1 };
+a2c_status a2c_gpp_set_pair_mode(a2c_gpp_ctx *ctx, int mode);
+a2c_status a2c_gpp_get_pair_mode(a2c_gpp_ctx *ctx, int *mode);
 
 /* Waits for all work queued on the context's stream (for _device calls). */
 a2c_status a2c_gpp_synchronize(a2c_gpp_ctx *ctx);

@@ -142,24 +142,38 @@ def test_device_driven_minimizer_matches_host_loop(gpu):
     """Mixed-precision a2c_gpp_minimize runs as replayed CUDA-graph ticks of
     the one-instance batch engine; it reaches the same minimum as the
     host-driven loop (their global sums differ in order only), and after a
-    neighbor rebuild that reallocates the list array it re-captures."""
+    neighbor rebuild that reallocates the list array it re-captures.
+
+    "The same minimum" is up to the resolution the stopping rule leaves: the
+    bound is four times the distance between two host-loop runs whose
+    evaluators differ by FP32 rounding alone (4 vs 2 threads per site), with
+    floors of 5e-4 A and 1e-9 relative in the free entropy."""
     X, xH, _, box, nPd, nH = A.lattice_fcc(6, periodic=(1, 1, 1), pos_std=0.03, sigma=(0.08, 0.14), x_center=0.15,
                                            x_half=0.15, seed=2)
     res = {}
-    for host in (True, False):
+    for host, tps in ((True, 4), (True, 2), (False, 4)):
         with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), precision="mixed") as g:
             g.set_occupancy(xH)
             g.build_neighbors(X)
+            g.set_threads_per_site(tps)
             g.set_minimizer(host)
-            res[host] = g.minimize(X, gatol=1e-5, polish=0)
+            res[host, tps] = g.minimize(X, gatol=1e-5, polish=0)
             if not host:
                 again = g.minimize(X, gatol=1e-5, polish=0)  # replays the captured tick
-                assert np.array_equal(again.X, res[host].X) and again.iters == res[host].iters
-    for host, r in res.items():
-        assert r.reason in (A.CONVERGED_GATOL, A.CONVERGED_STALLED), (host, r.reason)
-    d = np.abs(res[True].X.reshape(-1, 4)[:, :3] - res[False].X.reshape(-1, 4)[:, :3]).max()
-    assert d < 2e-3, d
-    assert abs(res[True].fmin - res[False].fmin) <= 1e-9 * abs(res[True].fmin)
+                assert np.array_equal(again.X, res[host, tps].X) and again.iters == res[host, tps].iters
+    for key, r in res.items():
+        assert r.reason in (A.CONVERGED_GATOL, A.CONVERGED_STALLED), (key, r.reason)
+
+    def dq(a, b):
+        return np.abs(a.X.reshape(-1, 4)[:, :3] - b.X.reshape(-1, 4)[:, :3]).max()
+
+    host, host2, dev = res[True, 4], res[True, 2], res[False, 4]
+    spread, spread_f = dq(host, host2), abs(host.fmin - host2.fmin)
+    d, d_f = dq(host, dev), abs(host.fmin - dev.fmin)
+    print(f"host vs device-driven: max|dq| {d:.2e} A, |df| {d_f:.2e}; host 4 vs 2 threads/site: {spread:.2e} A, "
+          f"{spread_f:.2e}")
+    assert d < max(4 * spread, 5e-4), (d, spread)
+    assert d_f <= max(4 * spread_f, 1e-9 * abs(host.fmin)), (d_f, spread_f)
     # re-capture after the list array moves: a 3% compression pulls the 4th
     # Pd-Pd shell (5.50 A) inside rc, so the rebuilt lists need a larger array
     Y = X.copy()
