@@ -74,6 +74,10 @@ constexpr int kBlock = 256;
 #ifndef A2C_GRAD_MIN_BLOCKS
 #define A2C_GRAD_MIN_BLOCKS 4
 #endif
+// Pass 1 likewise (5 blocks = 48 registers per thread).
+#ifndef A2C_RHO_MIN_BLOCKS
+#define A2C_RHO_MIN_BLOCKS 5
+#endif
 
 struct MixArgs {
   int64_t N;
@@ -150,9 +154,10 @@ __device__ __forceinline__ float hd(float4 c, float t) { return fmaf(fmaf(3.0f *
 // h times the derivative from its own coefficients (c1, 2 c2, 3 c3)
 __device__ __forceinline__ float dq(float4 d, float t) { return fmaf(fmaf(d.z, t, d.y), t, d.x); }
 
+template <int NTAB = kTabN>
 __device__ __forceinline__ int tab_index(float s, float &t) {
   float x = (s - (float)kTabR0) * (float)kTabInvH;
-  x = fminf(fmaxf(x, 0.0f), (float)kTabN - 0.5f);
+  x = fminf(fmaxf(x, 0.0f), (float)NTAB - 0.5f);
   const int i = (int)x;
   t = x - (float)i;
   return i;
@@ -240,14 +245,38 @@ __device__ __forceinline__ void walk_neighbors(const MixArgs &a, int64_t begin, 
 }
 
 // ---------------------------------------------------------------- pass 1
+// The f_Pd table in shared memory as 8 interleaved copies: interval i of
+// copy c is float4 number 8 i + c, in bank group c.  A 128-bit shared load
+// serves a warp in four phases of 8 consecutive lanes; lane l reads copy
+// l mod 8, so the 8 lanes of a phase always hit 8 different bank groups
+// and a lookup takes the minimum 4 wavefronts, where random intervals in
+// one copy took about 10.  Pass 1 keeps the intervals below 5.8 A (f_Pd <
+// 1e-19 A beyond; the last interval's value stands in there).
+constexpr int kRhoTabN = 768;
+constexpr int kRhoCopies = 8;
+constexpr size_t kRhoSmem = sizeof(float4) * kRhoTabN * kRhoCopies;  // 98,304 B: two blocks per SM
+
+// Pass 2 reads two tables (f_Pd' and phi_Pd).  Interleaved copies cost it
+// occupancy (8 copies of both: one 256-thread block per SM; 4: two), and
+// pass 2 needs the resident warps more than conflict-free lookups: on a
+// GB300 at 262,144 sites pass 2 took 0.329 ms with one copy (four blocks
+// per SM), 0.375 ms with 4 copies and 0.530 ms with 8.  So one copy.
+#ifndef A2C_GRAD_COPIES
+#define A2C_GRAD_COPIES 1
+#endif
+constexpr int kGradCopies = A2C_GRAD_COPIES;
+constexpr int kGradTabN = kGradCopies > 1 ? kRhoTabN : kTabN;
+constexpr size_t kGradSmem = 2 * sizeof(float4) * kGradTabN * kGradCopies;
+
 template <int TPS, bool LIST>
-__global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
+__global__ void __launch_bounds__(kBlock, A2C_RHO_MIN_BLOCKS) k_rho_mixed(MixArgs a) {
   constexpr int kSitesPerBlock = kBlock / TPS;
   const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
-  __shared__ float4 sF[kTabN];
-  for (int i = threadIdx.x; i < kTabN; i += blockDim.x) sF[i] = __ldg(&a.tabPair[i]);
+  extern __shared__ float4 sF8[];
+  for (int i = threadIdx.x; i < kRhoTabN * kRhoCopies; i += blockDim.x) sF8[i] = __ldg(&a.tabPair[i / kRhoCopies]);
   __syncthreads();
+  const float4 *sF = sF8 + (threadIdx.x % kRhoCopies);  // this lane's copy: interval i at sF[8 i]
   for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < n;
        base += (int64_t)gridDim.x * kSitesPerBlock) {
   const int64_t k = base + threadIdx.x / TPS;
@@ -275,8 +304,8 @@ __global__ void __launch_bounds__(kBlock) k_rho_mixed(MixArgs a) {
         for (int q = 0; q < 4; ++q) {
           const float r = s2[q] * rsq(s2[q]);
           float tt;
-          const int i = tab_index(r, tt);
-          part += hv(sF[i], tt);
+          const int i = tab_index<kRhoTabN>(r, tt);
+          part += hv(sF[kRhoCopies * i], tt);
         }
       }
       kahan(acc, cmp, part);
@@ -359,7 +388,7 @@ __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, f
       float g, phi;
       if (TYPE == 0) {
         float tt;
-        const int i = tab_index(r, tt);
+        const int i = kGradCopies * tab_index<kGradTabN>(r, tt);
         const float4 cf = sF[i], cp = sP[i];
         // phi and h phi' share one Horner chain
         const float hp = fmaf(cp.w, tt, cp.z), hq = fmaf(hp, tt, cp.y);
@@ -373,7 +402,7 @@ __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, f
         g = fmaf((Fa + Fb) * kFH_D, fh, dphi);
       } else {
         float tt;
-        const int i = tab_index(r, tt);
+        const int i = kGradCopies * tab_index<kGradTabN>(r, tt);
         const float fpd = dq(sF[i], tt) * (float)kTabInvH;
         const float fhd = fH(r) * kFH_D;
         float dphi;
@@ -409,12 +438,13 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_mixed(MixA
   constexpr int kSitesPerBlock = kBlock / TPS;
   const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
-  __shared__ float4 sF[kTabN], sP[kTabN];
-  for (int i = threadIdx.x; i < kTabN; i += blockDim.x) {
-    sF[i] = __ldg(&a.tabPair[2 * kTabN + i]);  // f_Pd' only
-    sP[i] = __ldg(&a.tabPair[kTabN + i]);
+  extern __shared__ float4 sTab[];  // f_Pd' quadratics, then phi_Pd cubics, kGradCopies-way interleaved
+  for (int i = threadIdx.x; i < kGradTabN * kGradCopies; i += blockDim.x) {
+    sTab[i] = __ldg(&a.tabPair[2 * kTabN + i / kGradCopies]);
+    sTab[kGradTabN * kGradCopies + i] = __ldg(&a.tabPair[kTabN + i / kGradCopies]);
   }
   __syncthreads();
+  const float4 *sF = sTab + threadIdx.x % kGradCopies, *sP = sF + kGradTabN * kGradCopies;
   for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < n;
        base += (int64_t)gridDim.x * kSitesPerBlock) {
   const int64_t k = base + threadIdx.x / TPS;
@@ -505,12 +535,13 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_once(MixAr
   constexpr int kSitesPerBlock = kBlock / TPS;
   const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
-  __shared__ float4 sF[kTabN], sP[kTabN];
-  for (int i = threadIdx.x; i < kTabN; i += blockDim.x) {
-    sF[i] = __ldg(&a.tabPair[2 * kTabN + i]);  // f_Pd' only
-    sP[i] = __ldg(&a.tabPair[kTabN + i]);
+  extern __shared__ float4 sTab[];  // f_Pd' quadratics, then phi_Pd cubics, kGradCopies-way interleaved
+  for (int i = threadIdx.x; i < kGradTabN * kGradCopies; i += blockDim.x) {
+    sTab[i] = __ldg(&a.tabPair[2 * kTabN + i / kGradCopies]);
+    sTab[kGradTabN * kGradCopies + i] = __ldg(&a.tabPair[kTabN + i / kGradCopies]);
   }
   __syncthreads();
+  const float4 *sF = sTab + threadIdx.x % kGradCopies, *sP = sF + kGradTabN * kGradCopies;
   for (int64_t base = (int64_t)blockIdx.x * kSitesPerBlock; base < n;
        base += (int64_t)gridDim.x * kSitesPerBlock) {
   const int64_t k = base + threadIdx.x / TPS;
@@ -714,9 +745,12 @@ void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, boo
     int dev = 0, sms = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_rho_mixed<TPS, LIST>, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_grad_mixed<TPS, LIST>, kBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_grad_once<TPS, LIST>, kBlock, 0);
+    cudaFuncSetAttribute(k_rho_mixed<TPS, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRhoSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_rho_mixed<TPS, LIST>, kBlock, kRhoSmem);
+    cudaFuncSetAttribute(k_grad_mixed<TPS, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
+    cudaFuncSetAttribute(k_grad_once<TPS, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_grad_mixed<TPS, LIST>, kBlock, kGradSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_grad_once<TPS, LIST>, kBlock, kGradSmem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_grad_recv<kRecvTps, LIST>, kBlock, 0);
     cap[0] = std::max(1, sms * b0);
     cap[1] = std::max(1, sms * b1);
@@ -724,15 +758,18 @@ void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, boo
     cap[3] = std::max(1, sms * b3);
   }
   const int64_t need = (a.N * TPS + kBlock - 1) / kBlock;
-  k_rho_mixed<TPS, LIST><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[0])), kBlock, 0, st>>>(a);
+  k_rho_mixed<TPS, LIST>
+      <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[0])), kBlock, kRhoSmem, st>>>(a);
   if (ev) cudaEventRecord(ev[2], st);
   if (once) {
-    k_grad_once<TPS, LIST><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[2])), kBlock, 0, st>>>(a);
+    k_grad_once<TPS, LIST>
+        <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[2])), kBlock, kGradSmem, st>>>(a);
     const int64_t need_r = (a.N * kRecvTps + kBlock - 1) / kBlock;
     k_grad_recv<kRecvTps, LIST>
         <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need_r, cap[3])), kBlock, 0, st>>>(a);
   } else {
-    k_grad_mixed<TPS, LIST><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[1])), kBlock, 0, st>>>(a);
+    k_grad_mixed<TPS, LIST>
+        <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[1])), kBlock, kGradSmem, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[3], st);
 }

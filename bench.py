@@ -746,6 +746,7 @@ def run_profile_case(args):
         g.build_neighbors(X)
         if args.case_tps:
             g.set_threads_per_site(args.case_tps)
+        g.set_pair_mode(args.case_pairs)
         dX = torch.tensor(X, device="cuda")
         dG = torch.empty_like(dX)
         df = torch.empty(1, dtype=torch.float64, device="cuda")
@@ -775,6 +776,8 @@ def main():
                     help="profile: the small untimed case used for ncu captures")
     ap.add_argument("--case-cells", type=int, default=40)
     ap.add_argument("--case-tps", type=int, default=0, help="threads per site in the profile case (0 = library)")
+    ap.add_argument("--case-pairs", choices=["once", "both"], default="once",
+                    help="pass 2 pair mode of the profile case")
     ap.add_argument("--ttm-fp64-cap", type=int, default=0,
                     help="stop the FP64 time-to-minimum run after this many iterations (0 = run to the end)")
     ap.add_argument("--ttm-polish-cap", type=int, default=0,
