@@ -79,6 +79,14 @@ constexpr int kBlock = 256;
 #define A2C_RHO_MIN_BLOCKS 5
 #endif
 
+// Folded exponential constants of f_H, phi_PdH, phi_H (see fH, morse below).
+struct MorseExp {
+  float K1, C1, L1, K2, C2, L2, Kt, Ct, Lt;
+};
+struct ExpTerms {
+  float fK, fC, fdC;
+  MorseExp pdh, hh;
+};
 struct MixArgs {
   int64_t N;
   int nPd;
@@ -89,6 +97,7 @@ struct MixArgs {
   const int64_t *off;
   const uint32_t *nbr;
   const int *npd;
+  ExpTerms ex;
   const float4 *tabPair;
   const float4 *tabEmb;
   float2 *FF;
@@ -154,50 +163,46 @@ __device__ __forceinline__ float hd(float4 c, float t) { return fmaf(fmaf(3.0f *
 // h times the derivative from its own coefficients (c1, 2 c2, 3 c3)
 __device__ __forceinline__ float dq(float4 d, float t) { return fmaf(fmaf(d.z, t, d.y), t, d.x); }
 
+// Interval of the pair tables and the offset t in [-1/2, 1/2] from its
+// midpoint (the tables hold midpoint-centred cubics), without a float-to-int
+// conversion: xm = (s - r0)/h - 1/2, clamped to [-1/2, NTAB - 1], plus
+// 1.5 * 2^23 rounds to 1.5 * 2^23 + rint(xm), whose low bits are the
+// interval (a tie at a knot picks the even neighbor; both cubics agree
+// there).
 template <int NTAB = kTabN>
 __device__ __forceinline__ int tab_index(float s, float &t) {
-  float x = (s - (float)kTabR0) * (float)kTabInvH;
-  x = fminf(fmaxf(x, 0.0f), (float)NTAB - 0.5f);
-  const int i = (int)x;
-  t = x - (float)i;
-  return i;
+  float xm = fmaf(s, (float)kTabInvH, (float)(-kTabR0 * kTabInvH - 0.5));
+  xm = fminf(fmaxf(xm, -0.5f), (float)NTAB - 1.0f);
+  const float y = xm + 12582912.0f;
+  t = xm - (y - 12582912.0f);
+  return __float_as_int(y) - 0x4B400000;
 }
 
-// f_H(r) = C exp(-delta r) (potential.cpp:105-119; its tail is the same
-// exponential); written as A 2^(K (r - 3.5)) to keep the argument small.
-constexpr float kFH_A = (float)(11.0025 * 0.010229853702006403);  // C e^{-3.5 delta}
-constexpr float kFH_K = (float)(-1.30927 * 1.4426950408889634);
-constexpr float kFH_D = -1.30927f;
-__device__ __forceinline__ float fH(float s) { return kFH_A * ex2(kFH_K * (s - 3.5f)); }
-
-// phi_PdH / phi_H (potential.cpp:162-200): D(b e^{-a(r-r0)} - a e^{-b(r-r0)})
-// for r <= 5.35, funRc e^{k(r-5.35)} beyond; value and derivative.
-struct Morse {
-  float A1, K1, R1, A2, K2, R2, rc, At, Kt;
-};
-// Inside the switch radius only (the caller has checked s <= rc).
-__device__ __forceinline__ void morse_in(const Morse &m, float s, float &v, float &d) {
-  const float e1 = m.A1 * ex2(m.K1 * (s - m.R1)), e2 = m.A2 * ex2(m.K2 * (s - m.R2));
-  v = e1 + e2;
-  d = (e1 * m.K1 + e2 * m.K2) * 0.6931471805599453f;
+// f_H, phi_PdH and phi_H as exponentials 2^(K s + C): the prefactor, the
+// shift and the log2(e) scale are folded into K and C on the host, in
+// double (exp_terms), so each term costs one FMA and one ex2.
+//   f_H(r) = C e^{-delta r} (potential.cpp:105-119; its tail beyond 5.35 A
+//     is the same exponential): f_H = 2^(fK s + fC), -f_H' = 2^(fK s + fdC).
+//   phi_PdH, phi_H (potential.cpp:162-200) = D (b e^{-a(r-r0)} - a
+//     e^{-b(r-r0)}) for r <= 5.35 A, funRc e^{k(r-5.35)} beyond:
+//     phi = E1 - E2, phi' = L1 E1 + L2 E2 with E1 = 2^(K1 s + C1) and
+//     E2 = 2^(K2 s + C2) inside; phi = -Et, phi' = Lt Et with
+//     Et = 2^(Kt s + Ct) beyond.  (MorseExp, ExpTerms are declared above.)
+__device__ __forceinline__ float fH(const ExpTerms &x, float s) { return ex2(fmaf(s, x.fK, x.fC)); }
+__device__ __forceinline__ float fHd_neg(const ExpTerms &x, float s) { return ex2(fmaf(s, x.fK, x.fdC)); }
+// Inside the switch radius only (the caller has checked s <= 5.35 A).
+__device__ __forceinline__ void morse_in(const MorseExp &m, float s, float &v, float &d) {
+  const float e1 = ex2(fmaf(s, m.K1, m.C1)), e2 = ex2(fmaf(s, m.K2, m.C2));
+  v = e1 - e2;
+  d = fmaf(m.L1, e1, m.L2 * e2);
 }
-__device__ __forceinline__ void morse(const Morse &m, float s, float &v, float &d) {
-  const bool tail = s > m.rc;
-  const float A1 = tail ? 0.0f : m.A1, A2 = tail ? m.At : m.A2;
-  const float K1 = m.K1, K2 = tail ? m.Kt : m.K2, R2 = tail ? m.rc : m.R2;
-  const float e1 = A1 * ex2(K1 * (s - m.R1)), e2 = A2 * ex2(K2 * (s - R2));
-  v = e1 + e2;
-  d = (e1 * K1 + e2 * K2) * 0.6931471805599453f;
+__device__ __forceinline__ void morse(const MorseExp &m, float s, float &v, float &d) {
+  const bool tail = s > 5.35f;
+  const float e1 = tail ? 0.0f : ex2(fmaf(s, m.K1, m.C1));
+  const float e2 = ex2(fmaf(s, tail ? m.Kt : m.K2, tail ? m.Ct : m.C2));
+  v = e1 - e2;
+  d = fmaf(m.L1, e1, (tail ? m.Lt : m.L2) * e2);
 }
-#define LOG2E 1.4426950408889634
-__constant__ Morse kPdH = {(float)(0.2494540 * 2.13158), (float)(-4.82613 * LOG2E), 1.50964f,
-                           (float)(-0.2494540 * 4.82613), (float)(-2.13158 * LOG2E), 1.50964f, 5.35f,
-                           (float)-3.353001113951400e-04,
-                           (float)(7.147062196813336e-04 / -3.353001113951400e-04 * LOG2E)};
-__constant__ Morse kHH = {(float)(0.0661496 * 1.47797), (float)(-3.67263 * LOG2E), 2.51980f,
-                          (float)(-0.0661496 * 3.67263), (float)(-1.47797 * LOG2E), 2.51980f, 5.35f,
-                          (float)-0.003702722457147, (float)(0.005465945471933 / -0.003702722457147 * LOG2E)};
-#undef LOG2E
 
 constexpr float kSqrt6 = 2.449489742783178f;
 constexpr float kSqrt3 = 1.7320508075688772f;
@@ -321,7 +326,7 @@ __global__ void __launch_bounds__(kBlock, A2C_RHO_MIN_BLOCKS) k_rho_mixed(MixArg
       for (int c = 0; c < 3; ++c) {
         A2C_RADII(c, Dv[c])
 #pragma unroll
-        for (int q = 0; q < 4; ++q) part += fH(s2[q] * rsq(s2[q]));
+        for (int q = 0; q < 4; ++q) part += fH(a.ex, s2[q] * rsq(s2[q]));
       }
       kahan(acc, cmp, part * xj);
     });
@@ -368,8 +373,8 @@ __device__ __forceinline__ bool pair_inside(float3 D, float ui, float uj) {
 // TAIL = false: every point is inside the switch radius (pair_inside), so
 // the Morse terms skip the per-point branch selection.
 template <int TYPE, bool TAIL = true>  // 0 Pd-Pd, 1 Pd i / H j, 2 H i / Pd j, 3 H-H
-__device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, float Fa, float Fb, float3 D, float ui,
-                                           float uj, PairAcc &p) {
+__device__ __forceinline__ void pair_terms(const ExpTerms &x, const float4 *sF, const float4 *sP, float Fa, float Fb,
+                                           float3 D, float ui, float uj, PairAcc &p) {
   const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
   const float Ai = fmaf(ui, ui, D2), Aj = fmaf(uj, uj, D2);
   const float Dv[3] = {D.x, D.y, D.z};
@@ -395,20 +400,20 @@ __device__ __forceinline__ void pair_terms(const float4 *sF, const float4 *sP, f
         phi = fmaf(hq, tt, cp.x);
         g = fmaf(Fa + Fb, dq(cf, tt), fmaf(fmaf(cp.w, tt, hp), tt, hq)) * (float)kTabInvH;
       } else if (TYPE == 3) {
-        const float fh = fH(r);
+        const float nfhd = fHd_neg(x, r);  // -f_H'
         float dphi;
-        if (TAIL) morse(kHH, r, phi, dphi);
-        else morse_in(kHH, r, phi, dphi);
-        g = fmaf((Fa + Fb) * kFH_D, fh, dphi);
+        if (TAIL) morse(x.hh, r, phi, dphi);
+        else morse_in(x.hh, r, phi, dphi);
+        g = fmaf(-(Fa + Fb), nfhd, dphi);
       } else {
         float tt;
         const int i = kGradCopies * tab_index<kGradTabN>(r, tt);
         const float fpd = dq(sF[i], tt) * (float)kTabInvH;
-        const float fhd = fH(r) * kFH_D;
+        const float nfhd = fHd_neg(x, r);
         float dphi;
-        if (TAIL) morse(kPdH, r, phi, dphi);
-        else morse_in(kPdH, r, phi, dphi);
-        g = (TYPE == 1) ? fmaf(Fa, fhd, fmaf(Fb, fpd, dphi)) : fmaf(Fa, fpd, fmaf(Fb, fhd, dphi));
+        if (TAIL) morse(x.pdh, r, phi, dphi);
+        else morse_in(x.pdh, r, phi, dphi);
+        g = (TYPE == 1) ? fmaf(-Fa, nfhd, fmaf(Fb, fpd, dphi)) : fmaf(Fa, fpd, fmaf(-Fb, nfhd, dphi));
       }
       ck[q] = g * is;
       p.v += phi;
@@ -472,11 +477,11 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_mixed(MixA
       const float uj = kSqrt6 * __int_as_float(pj.w);
       PairAcc p;
       if (iPd) {
-        pair_terms<0>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+        pair_terms<0>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, p);
       } else if (pair_inside(D, ui, uj)) {
-        pair_terms<2, false>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+        pair_terms<2, false>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, p);
       } else {
-        pair_terms<2, true>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+        pair_terms<2, true>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, p);
       }
       add_pair(A, p, D, a.W, hw);
     });
@@ -486,11 +491,11 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_mixed(MixA
       PairAcc p;
       const bool in = pair_inside(D, ui, uj);
       if (iPd) {
-        if (in) pair_terms<1, false>(sF, sP, ffi.x, Fb, D, ui, uj, p);
-        else pair_terms<1, true>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+        if (in) pair_terms<1, false>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, p);
+        else pair_terms<1, true>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, p);
       } else {
-        if (in) pair_terms<3, false>(sF, sP, ffi.x, Fb, D, ui, uj, p);
-        else pair_terms<3, true>(sF, sP, ffi.x, Fb, D, ui, uj, p);
+        if (in) pair_terms<3, false>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, p);
+        else pair_terms<3, true>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, p);
       }
       add_pair(A, p, D, a.W * xj, hw * xj);
     });
@@ -569,11 +574,11 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_once(MixAr
       const float uj = kSqrt6 * __int_as_float(pj.w);
       PairAcc q;
       if (iPd) {
-        pair_terms<0>(sF, sP, ffi.x, Fb, D, ui, uj, q);
+        pair_terms<0>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, q);
       } else if (pair_inside(D, ui, uj)) {
-        pair_terms<2, false>(sF, sP, ffi.x, Fb, D, ui, uj, q);
+        pair_terms<2, false>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, q);
       } else {
-        pair_terms<2, true>(sF, sP, ffi.x, Fb, D, ui, uj, q);
+        pair_terms<2, true>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, q);
       }
       add_pair(A, q, D, a.W, w);
       send_share(a, t, q, D, w);
@@ -582,8 +587,8 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_once(MixAr
       const float3 D = pair_vec(R.sc, pi, pj);
       const float uj = kSqrt6 * __int_as_float(pj.w);
       PairAcc q;
-      if (pair_inside(D, ui, uj)) pair_terms<3, false>(sF, sP, ffi.x, Fb, D, ui, uj, q);
-      else pair_terms<3, true>(sF, sP, ffi.x, Fb, D, ui, uj, q);
+      if (pair_inside(D, ui, uj)) pair_terms<3, false>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, q);
+      else pair_terms<3, true>(a.ex, sF, sP, ffi.x, Fb, D, ui, uj, q);
       add_pair(A, q, D, a.W * xj, w * xj);
       send_share(a, t, q, D, w);
     });
@@ -735,6 +740,40 @@ __global__ void k_prep_list(const double *X, const double *occ, BatchView bv, in
 // Persistent grids: as many blocks as fit on the device at once (occupancy
 // query, cached per kernel), capped by the work (for a list launch, by the
 // largest list the system can have).
+// The folded exponential constants (see ExpTerms) from the reference's
+// parameters: f_H C = 11.0025, delta = 1.30927 (potential.cpp:105-119);
+// phi_PdH and phi_H D, a, b, r0 and the tail funRc, funRc' at 5.35 A
+// (potential.cpp:162-200).
+MorseExp morse_exp(double D, double a, double b, double r0, double funRc, double dfunRc) {
+  constexpr double kL2E = 1.4426950408889634, kRc = 5.35;
+  const double K1 = -a * kL2E, K2 = -b * kL2E, k = dfunRc / funRc, Kt = k * kL2E;
+  MorseExp m;
+  m.K1 = (float)K1;
+  m.C1 = (float)(std::log2(D * b) - K1 * r0);
+  m.L1 = (float)(-a);
+  m.K2 = (float)K2;
+  m.C2 = (float)(std::log2(D * a) - K2 * r0);
+  m.L2 = (float)b;
+  m.Kt = (float)Kt;
+  m.Ct = (float)(std::log2(-funRc) - Kt * kRc);
+  m.Lt = (float)(-k);
+  return m;
+}
+ExpTerms exp_terms() {
+  constexpr double kL2E = 1.4426950408889634, kC = 11.0025, kDelta = 1.30927;
+  ExpTerms x;
+  x.fK = (float)(-kDelta * kL2E);
+  x.fC = (float)std::log2(kC);
+  x.fdC = (float)std::log2(kC * kDelta);
+  x.pdh = morse_exp(0.2494540, 4.82613, 2.13158, 1.50964, -3.353001113951400e-04, 7.147062196813336e-04);
+  x.hh = morse_exp(0.0661496, 3.67263, 1.47797, 2.51980, -0.003702722457147, 0.005465945471933);
+  return x;
+}
+const ExpTerms &exp_consts() {
+  static const ExpTerms x = exp_terms();
+  return x;
+}
+
 // once = true: pass 2 evaluates every pair once (k_grad_once + k_grad_recv;
 // a.rev, a.npre, a.recv set), else from both sides (k_grad_mixed).
 constexpr int kRecvTps = 8;  // lanes per site summing the received shares
@@ -949,6 +988,7 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   a.off = c->d_off;
   a.nbr = c->d_nbr;
   a.npd = c->d_npd;
+  a.ex = exp_consts();
   a.tabPair = M->tabPair;
   a.tabEmb = M->tabEmb;
   a.FF = M->FF;
@@ -1013,6 +1053,7 @@ a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const B
   a.off = c->d_off;
   a.nbr = c->d_nbr;
   a.npd = c->d_npd;
+  a.ex = exp_consts();
   a.tabPair = M->tabPair;
   a.tabEmb = M->tabEmb;
   a.FF = M->FF;
@@ -1187,6 +1228,7 @@ extern "C" a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *c, const double *d
   a.off = c->d_off;
   a.nbr = c->d_nbr;
   a.npd = c->d_npd;
+  a.ex = exp_consts();
   a.tabPair = (const float4 *)(base + kNaTabPair);
   a.tabEmb = (const float4 *)(base + kNaTabEmb);
   a.FF = (float2 *)(base + kNaFF);

@@ -14,6 +14,7 @@
 // same way on rho in [0, 64), h = 1/64.
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "tables.h"
@@ -115,6 +116,19 @@ void hermite(Dual p0, Dual p1, double h, float *c) {
   c[3] = (float)c3;
 }
 
+// The same cubic in the offset from the interval's midpoint, t' = t - 1/2
+// in [-1/2, 1/2] (the form the pair kernels index without a float-to-int
+// conversion).
+void hermite_mid(Dual p0, Dual p1, double h, float *c) {
+  const double c0 = p0.v, c1 = h * p0.d;
+  const double c2 = 3.0 * (p1.v - p0.v) - h * (2.0 * p0.d + p1.d);
+  const double c3 = 2.0 * (p0.v - p1.v) + h * (p0.d + p1.d);
+  c[0] = (float)(c0 + 0.5 * c1 + 0.25 * c2 + 0.125 * c3);
+  c[1] = (float)(c1 + c2 + 0.75 * c3);
+  c[2] = (float)(c2 + 1.5 * c3);
+  c[3] = (float)c3;
+}
+
 }  // namespace tables
 
 // Pair table: per interval 8 floats, f_Pd's cubic then phi_Pd's cubic.
@@ -122,8 +136,8 @@ void build_pair_table(double r0, double h, int n, std::vector<float> &out) {
   out.assign((size_t)n * 8, 0.0f);
   for (int i = 0; i < n; ++i) {
     const double xa = r0 + h * i, xb = r0 + h * (i + 1), mid = r0 + h * (i + 0.5);
-    tables::hermite(tables::f_Pd({xa, 1.0}, mid), tables::f_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i]);
-    tables::hermite(tables::phi_Pd({xa, 1.0}, mid), tables::phi_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i + 4]);
+    tables::hermite_mid(tables::f_Pd({xa, 1.0}, mid), tables::f_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i]);
+    tables::hermite_mid(tables::phi_Pd({xa, 1.0}, mid), tables::phi_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i + 4]);
   }
 }
 
@@ -148,8 +162,8 @@ namespace a2c {
 void build_pair_table_raw(double r0, double h, int n, float *out) {
   for (int i = 0; i < n; ++i) {
     const double xa = r0 + h * i, xb = r0 + h * (i + 1), mid = r0 + h * (i + 0.5);
-    tables::hermite(tables::f_Pd({xa, 1.0}, mid), tables::f_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i]);
-    tables::hermite(tables::phi_Pd({xa, 1.0}, mid), tables::phi_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i + 4]);
+    tables::hermite_mid(tables::f_Pd({xa, 1.0}, mid), tables::f_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i]);
+    tables::hermite_mid(tables::phi_Pd({xa, 1.0}, mid), tables::phi_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i + 4]);
   }
 }
 
@@ -222,10 +236,15 @@ extern "C" a2c_status a2c_mixed_table_eval(int which, const double *x, int64_t n
       value[k] = hv(c, t);
       deriv[k] = hd(c, t) * (float)a2c::kEmbInvH;
     } else {
-      float u = (s - (float)a2c::kTabR0) * (float)a2c::kTabInvH;
-      u = std::fmin(std::fmax(u, 0.0f), (float)a2c::kTabN - 0.5f);
-      const int i = (int)u;
-      const float t = u - (float)i;
+      // the pair kernels' indexing (k_mixed.cu tab_index): interval and
+      // midpoint offset by the 1.5 * 2^23 rounding of an FMA result
+      float xm = std::fma(s, (float)a2c::kTabInvH, (float)(-a2c::kTabR0 * a2c::kTabInvH - 0.5));
+      xm = std::fmin(std::fmax(xm, -0.5f), (float)a2c::kTabN - 1.0f);
+      const float y = xm + 12582912.0f;
+      const float t = xm - (y - 12582912.0f);
+      int32_t bits;
+      std::memcpy(&bits, &y, 4);
+      const int i = bits - 0x4B400000;
       const float *c = pair.data() + 8 * i + (which == 4 ? 0 : 4);
       value[k] = hv(c, t);
       deriv[k] = hd(c, t) * (float)a2c::kTabInvH;

@@ -144,14 +144,17 @@ def test_device_driven_minimizer_matches_host_loop(gpu):
     host-driven loop (their global sums differ in order only), and after a
     neighbor rebuild that reallocates the list array it re-captures.
 
-    "The same minimum" is up to the resolution the stopping rule leaves: the
-    bound is four times the distance between two host-loop runs whose
-    evaluators differ by FP32 rounding alone (4 vs 2 threads per site), with
+    "The same minimum" is up to the resolution the stopping rule leaves and
+    up to a uniform translation (a zero mode of the periodic box, along which
+    the FP32 noise of the summed gradient moves each run differently): the
+    bound on the distance of positions, mean displacement removed, is three
+    times the largest distance between host-loop runs whose evaluators
+    differ by FP32 rounding alone (4 vs 1, 2 and 8 threads per site), with
     floors of 5e-4 A and 1e-9 relative in the free entropy."""
     X, xH, _, box, nPd, nH = A.lattice_fcc(6, periodic=(1, 1, 1), pos_std=0.03, sigma=(0.08, 0.14), x_center=0.15,
                                            x_half=0.15, seed=2)
     res = {}
-    for host, tps in ((True, 4), (True, 2), (False, 4)):
+    for host, tps in ((True, 4), (True, 1), (True, 2), (True, 8), (False, 4)):
         with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), precision="mixed") as g:
             g.set_occupancy(xH)
             g.build_neighbors(X)
@@ -165,15 +168,18 @@ def test_device_driven_minimizer_matches_host_loop(gpu):
         assert r.reason in (A.CONVERGED_GATOL, A.CONVERGED_STALLED), (key, r.reason)
 
     def dq(a, b):
-        return np.abs(a.X.reshape(-1, 4)[:, :3] - b.X.reshape(-1, 4)[:, :3]).max()
+        d = a.X.reshape(-1, 4)[:, :3] - b.X.reshape(-1, 4)[:, :3]
+        return np.abs(d - d.mean(axis=0)).max()
 
-    host, host2, dev = res[True, 4], res[True, 2], res[False, 4]
-    spread, spread_f = dq(host, host2), abs(host.fmin - host2.fmin)
+    host, dev = res[True, 4], res[False, 4]
+    others = [res[True, t] for t in (1, 2, 8)]
+    spread = max(dq(host, o) for o in others)
+    spread_f = max(abs(host.fmin - o.fmin) for o in others)
     d, d_f = dq(host, dev), abs(host.fmin - dev.fmin)
-    print(f"host vs device-driven: max|dq| {d:.2e} A, |df| {d_f:.2e}; host 4 vs 2 threads/site: {spread:.2e} A, "
-          f"{spread_f:.2e}")
-    assert d < max(4 * spread, 5e-4), (d, spread)
-    assert d_f <= max(4 * spread_f, 1e-9 * abs(host.fmin)), (d_f, spread_f)
+    print(f"host vs device-driven: max|dq| {d:.2e} A, |df| {d_f:.2e}; host 4 vs 1/2/8 threads/site: "
+          + ", ".join(f"{dq(host, o):.2e} A {abs(host.fmin - o.fmin):.2e}" for o in others))
+    assert d < max(3 * spread, 5e-4), (d, spread)
+    assert d_f <= max(3 * spread_f, 1e-9 * abs(host.fmin)), (d_f, spread_f)
     # re-capture after the list array moves: a 3% compression pulls the 4th
     # Pd-Pd shell (5.50 A) inside rc, so the rebuilt lists need a larger array
     Y = X.copy()
