@@ -704,7 +704,7 @@ struct a2c_gpp_batch {
   Cfg exec_cfg{};
   int exec_tps = -1;
   const void *exec_nbr = nullptr;
-  const void *exec_pass2[4] = {};  // the captured pass 2: mode and its index buffers
+  const void *exec_pass2[5] = {};  // the captured pass 2: mode and its index buffers
   bool borrowed = false;  // c belongs to a context (the one-instance engine)
   // statistics of the last minimization
   int ticks = 0;
@@ -994,7 +994,7 @@ a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_
   // performs the launchers' one-time occupancy queries outside any capture
   if (!st) fail(tick(b, D, cf, tps));
   // the captured tick, reused while the configuration is unchanged
-  const void *pass2[4];
+  const void *pass2[5];
   mixed_graph_key(c, pass2);
   const bool same = b->exec && b->exec_tps == tps && b->exec_nbr == (const void *)c->d_nbr &&
                     !std::memcmp(b->exec_pass2, pass2, sizeof(pass2)) && !std::memcmp(&b->exec_cfg, &cf, sizeof(Cfg));

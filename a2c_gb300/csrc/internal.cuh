@@ -166,7 +166,7 @@ a2c_status mixed_get_pair_mode(a2c_gpp_ctx *c, int *mode);
 a2c_status mixed_lists_changed(a2c_gpp_ctx *c);
 // what a captured batch tick bakes in of pass 2: the mode in use and the
 // pairs-once index buffers (a graph is re-captured when any of them changes)
-void mixed_graph_key(a2c_gpp_ctx *c, const void *key[4]);
+void mixed_graph_key(a2c_gpp_ctx *c, const void *key[5]);
 
 // batch.cu: the one-instance device-driven minimizer of a context
 a2c_status engine_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp, double *fmin, int *iters,

@@ -61,6 +61,7 @@ struct Mixed {
   uint32_t *rev = nullptr;
   int *npre = nullptr;
   float4 *recv = nullptr;
+  double *Gown = nullptr;  // 4 per site: the owner's share of the gradient (k_grad_once)
   int64_t sym_entries = 0, sym_sites = 0;  // capacities
   uint64_t sym_version = ~0ull;            // list version the index was built for
   bool sym_ok = false;
@@ -107,6 +108,7 @@ struct MixArgs {
   const uint32_t *rev;  // pairs evaluated once (k_grad_once, k_grad_recv)
   const int *npre;
   float4 *recv;
+  double *Gown;
 };
 
 __device__ __forceinline__ float ex2(float x) {
@@ -601,12 +603,12 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_once(MixAr
     for (int o = TPS / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     tot[k] = (double)v;
   }
-  if (live && lane == 0) {
+  if (live && lane == 0) {  // the site's own share (16-byte stores: Gown is the library's); k_grad_recv completes G
     const double x = xi, sg = sigi, invT = 1.0 / R.T;
-    a.G[4 * s] = tot[0] * (invT * x);
-    a.G[4 * s + 1] = tot[1] * (invT * x);
-    a.G[4 * s + 2] = tot[2] * (invT * x);
-    a.G[4 * s + 3] = tot[3] * (1.7320508075688772 * 1.4142135623730951 * invT * x) - 3.0 * kB / sg * x;
+    double2 *own = reinterpret_cast<double2 *>(a.Gown + 4 * s);
+    own[0] = make_double2(tot[0] * (invT * x), tot[1] * (invT * x));
+    own[1] = make_double2(tot[2] * (invT * x),
+                          tot[3] * (1.7320508075688772 * 1.4142135623730951 * invT * x) - 3.0 * kB / sg * x);
     a.Vs[s] = x * (double)ffi.y + tot[4];
     a.Ss[s] = (double)logf(sigi) * x;
   }
@@ -614,7 +616,8 @@ __global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_once(MixAr
 }
 
 // The shares a site received (its list entries after the first npre),
-// summed in list order with compensation and added to its gradient.
+// summed in list order with compensation and added to its own share: G is
+// written once (it may be the caller's host-mapped memory).
 template <int TPS, bool LIST>
 __global__ void __launch_bounds__(kBlock) k_grad_recv(MixArgs a) {
   constexpr int kSitesPerBlock = kBlock / TPS;
@@ -646,12 +649,15 @@ __global__ void __launch_bounds__(kBlock) k_grad_recv(MixArgs a) {
       for (int o = TPS / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
       tot[c] = (double)v;
     }
-    if (live && lane == 0) {
+    // lanes 0-3 of the site write one component each: the sites of a warp
+    // store one contiguous run of G (the caller's memory may be host-mapped,
+    // where scattered 8-byte stores are slow)
+    static_assert(TPS >= 4, "one lane per gradient component");
+    if (live && lane < 4) {
       const double x = a.occ[s], invT = 1.0 / R.T;
-      a.G[4 * s] += tot[0] * (invT * x);
-      a.G[4 * s + 1] += tot[1] * (invT * x);
-      a.G[4 * s + 2] += tot[2] * (invT * x);
-      a.G[4 * s + 3] += tot[3] * (1.7320508075688772 * 1.4142135623730951 * invT * x);
+      const double v = lane == 0 ? tot[0] : lane == 1 ? tot[1] : lane == 2 ? tot[2] : tot[3];
+      const double scale = lane == 3 ? 1.7320508075688772 * 1.4142135623730951 * invT * x : invT * x;
+      a.G[4 * s + lane] = a.Gown[4 * s + lane] + v * scale;
     }
   }
 }
@@ -889,9 +895,12 @@ a2c_status ensure_sym(a2c_gpp_ctx *c) {
   }
   if (N + 1 > M->sym_sites) {
     if (M->npre) cudaFree(M->npre);
+    if (M->Gown) cudaFree(M->Gown);
     M->npre = nullptr;
+    M->Gown = nullptr;
     M->sym_sites = 0;
-    if (cudaMalloc(&M->npre, sizeof(int) * (N + 1)) != cudaSuccess) {
+    if (cudaMalloc(&M->npre, sizeof(int) * (N + 1)) != cudaSuccess ||
+        cudaMalloc(&M->Gown, sizeof(double) * 4 * (N + 1)) != cudaSuccess) {
       (void)cudaGetLastError();
       M->sym_version = c->nbr_version;
       return A2C_OK;
@@ -954,7 +963,7 @@ void mixed_free(a2c_gpp_ctx *c) {
   Mixed *M = c->mixed;
   if (!M) return;
   for (void *p : {(void *)M->P, (void *)M->occ, (void *)M->FF, (void *)M->tabPair, (void *)M->tabEmb,
-                  (void *)M->rev, (void *)M->npre, (void *)M->recv})
+                  (void *)M->rev, (void *)M->npre, (void *)M->recv, (void *)M->Gown})
     if (p) cudaFree(p);
   delete M;
   c->mixed = nullptr;
@@ -1001,6 +1010,7 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   a.rev = M->rev;
   a.npre = M->npre;
   a.recv = M->recv;
+  a.Gown = M->Gown;
   if (ev) cudaEventRecord(ev[0], c->stream);
   if (N > 0) {
     if (Xcopy)
@@ -1031,13 +1041,14 @@ a2c_status mixed_prepare(a2c_gpp_ctx *c) {
   return refresh_sym(c);
 }
 
-void mixed_graph_key(a2c_gpp_ctx *c, const void *key[4]) {
+void mixed_graph_key(a2c_gpp_ctx *c, const void *key[5]) {
   const Mixed *M = c->mixed;
   const bool once = M && use_once(c);
   key[0] = once ? (const void *)c : nullptr;
   key[1] = M ? (const void *)M->rev : nullptr;
   key[2] = M ? (const void *)M->npre : nullptr;
   key[3] = M ? (const void *)M->recv : nullptr;
+  key[4] = M ? (const void *)M->Gown : nullptr;
 }
 
 a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, int tps) {
@@ -1066,6 +1077,7 @@ a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const B
   a.rev = M->rev;
   a.npre = M->npre;
   a.recv = M->recv;
+  a.Gown = M->Gown;
   static int prep_cap = 0;
   if (!prep_cap) {
     int dev = 0, sms = 0;

@@ -386,7 +386,7 @@ def run_batch_case(args):
         out["neighbor_build_s"] = time.perf_counter() - t0
         tps, ms = b.autotune(X)
         out["autotune"] = {"threads_per_site": tps, "ms_per_eval": ms}
-        for name, polish in (("mixed_batch", 0), ("mixed_polish_batch", 1)):
+        for name, polish in (("mixed_batch", 0), ("mixed_polish_batch", 1))[:1 if args.batch_mixed_only else 2]:
             t0 = time.perf_counter()
             r = b.minimize(X, polish=polish, **kw)
             wall = time.perf_counter() - t0
@@ -398,6 +398,9 @@ def run_batch_case(args):
                          "fp64_polish_iters_mean": float(r.fp64_iters.mean()),
                          "fp64_polish_iters_max": int(r.fp64_iters.max()), "nfev_max": int(r.nfev.max())}
             print(json.dumps({name: out[name]}), flush=True)
+    if args.batch_mixed_only:  # the mixed batch alone (no polish run, no comparison loops)
+        print(json.dumps(out))
+        return 0
     sub = list(range(0, len(inst), args.batch_stride))
     sub_sites = int(sizes[sub].sum())
     scale = float(sizes.sum()) / sub_sites
@@ -787,6 +790,8 @@ def main():
     ap.add_argument("--dmd-ref-steps", type=int, default=10, help="outer steps of the reduced FP64/mixed comparison")
     ap.add_argument("--batch-n", type=int, default=256, help="instances of the batched case")
     ap.add_argument("--batch-stride", type=int, default=16, help="every k-th instance forms the looped subset")
+    ap.add_argument("--batch-mixed-only", action="store_true",
+                    help="batched case: only the mixed-precision batch minimization")
     args = ap.parse_args()
     if args.case == "profile":
         return run_profile_case(args)
