@@ -567,7 +567,7 @@ def run_ours(args):
     # mixed kernels (pairs once: each pair evaluated by one of its sites;
     # both: every site gathers over all its pairs)
     tune = {}
-    for mode in ("once", "both"):
+    for mode in (("once", "both") if args.pair_mode == "auto" else (args.pair_mode,)):
         g.set_pair_mode(mode)
         for tps in (1, 2, 4, 8):
             g.set_threads_per_site(tps)
@@ -608,14 +608,16 @@ def run_ours(args):
     modes = {mode: {"threads_per_site": best, "pass2_ms": float(np.mean(st_mixed[:, 2])),
                     "eval_ms": float(np.mean(st_mixed.sum(axis=1)))}}
     other = "both" if mode == "once" else "once"
-    okey = min((k for k in tune if k.startswith(other)), key=tune.get)
-    g.set_pair_mode(other)
-    g.set_threads_per_site(int(okey.split("/")[1]))
-    st_other = timed(max(3, args.steps // 2), 2)
-    modes[other] = {"threads_per_site": int(okey.split("/")[1]), "pass2_ms": float(np.mean(st_other[:, 2])),
-                    "eval_ms": float(np.mean(st_other.sum(axis=1)))}
-    g.set_pair_mode(mode)
-    g.set_threads_per_site(best)
+    okeys = [k for k in tune if k.startswith(other)]
+    if okeys:
+        okey = min(okeys, key=tune.get)
+        g.set_pair_mode(other)
+        g.set_threads_per_site(int(okey.split("/")[1]))
+        st_other = timed(max(3, args.steps // 2), 2)
+        modes[other] = {"threads_per_site": int(okey.split("/")[1]), "pass2_ms": float(np.mean(st_other[:, 2])),
+                        "eval_ms": float(np.mean(st_other.sum(axis=1)))}
+        g.set_pair_mode(mode)
+        g.set_threads_per_site(best)
 
     # FP64 plain form on the same state
     g.set_precision("fp64")
@@ -671,7 +673,8 @@ def run_ours(args):
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get("k_grad_mixed_bytes_per_launch")
+            traffic = json.loads(tfile.read_text()).get(
+                "k_grad_once_recv_bytes_per_launch" if once else "k_grad_mixed_bytes_per_launch")
         except Exception:
             traffic = None
     kname = f"k_grad_once<{best}> + k_grad_recv<8> (pass 2, pairs once)" if once else \
@@ -781,6 +784,8 @@ def main():
     ap.add_argument("--case-tps", type=int, default=0, help="threads per site in the profile case (0 = library)")
     ap.add_argument("--case-pairs", choices=["once", "both"], default="once",
                     help="pass 2 pair mode of the profile case")
+    ap.add_argument("--pair-mode", choices=["auto", "once", "both"], default="auto",
+                    help="pass 2 pair mode of the evaluator workload (auto: the faster of the two, measured)")
     ap.add_argument("--ttm-fp64-cap", type=int, default=0,
                     help="stop the FP64 time-to-minimum run after this many iterations (0 = run to the end)")
     ap.add_argument("--ttm-polish-cap", type=int, default=0,
