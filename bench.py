@@ -775,7 +775,7 @@ def run_profile_case(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
