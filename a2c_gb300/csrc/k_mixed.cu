@@ -207,7 +207,6 @@ __device__ __forceinline__ void morse(const MorseExp &m, float s, float &v, floa
 }
 
 constexpr float kSqrt6 = 2.449489742783178f;
-constexpr float kSqrt3 = 1.7320508075688772f;
 
 // The four squared radii of coordinate c for the pair (D, ui, uj):
 // atom i moved by +ui, -ui; atom j moved by -uj, +uj (r = q_i - q_j).
