@@ -467,6 +467,127 @@ def read_input(path: str) -> dict:
     return out
 
 
+GEOMETRY_TYPES = {"plane": 0, "cylinder_cone": 1, "cylinder_sphere": 2, "sphere": 3, "parallelepiped": 4,
+                  "spheroid": 5}
+_INCLUSION = {"intersection": 1, "union": 2}
+LATTICE_SITE_FIELDS = ("q", "q0", "l", "siteid", "matid", "tag", "sigma", "x")
+
+
+def lattice_from_input(path: str, lattice_id: int = 0, max_sites: int = 256, max_geoms: int = 256) -> dict:
+    """Lattice[lattice_id] of an input file (a2c_input_lattice) as a
+    description dict: abc (9), origin, periodic, dmin, sites (list of dicts:
+    l, materialid, tag, atomic_frequency, mean_displacement, x) and geoms
+    (list of dicts: type, order, inclusion, exterior, p)."""
+    desc = N.LatticeDesc()
+    sites = (N.SiteGroup * max(max_sites, 1))()
+    geoms = (N.Geometry * max(max_geoms, 1))()
+    msg = C.create_string_buffer(256)
+    st = N.lib().a2c_input_lattice(str(path).encode(), int(lattice_id), C.byref(desc), sites, max_sites, geoms,
+                                   max_geoms, msg, 256)
+    if st != N.A2C_OK:
+        raise A2CError(st, "a2c_input_lattice: " + msg.value.decode())
+    return {"abc": list(desc.abc), "origin": list(desc.origin), "periodic": list(desc.periodic), "dmin": desc.dmin,
+            "sites": [{"l": list(g.l), "materialid": g.materialid, "tag": g.tag,
+                       "atomic_frequency": g.atomic_frequency, "mean_displacement": list(g.mean_displacement),
+                       "x": g.x} for g in sites[:desc.nsites]],
+            "geoms": [{"type": g.type, "order": g.order, "inclusion": g.inclusion, "exterior": g.exterior,
+                       "p": list(g.p)} for g in geoms[:desc.ngeom]]}
+
+
+def _lattice_struct(desc: dict):
+    d = N.LatticeDesc()
+    for k in range(9):
+        d.abc[k] = float(desc.get("abc", (1, 0, 0, 0, 1, 0, 0, 0, 1))[k])
+    for k in range(3):
+        d.origin[k] = float(desc.get("origin", (0, 0, 0))[k])
+        d.periodic[k] = int(desc.get("periodic", (0, 0, 0))[k])
+    d.dmin = float(desc.get("dmin", 0.0))
+    sites = desc.get("sites", [])
+    geoms = desc.get("geoms", [])
+    sa = (N.SiteGroup * max(len(sites), 1))()
+    for i, g in enumerate(sites):
+        for k in range(3):
+            sa[i].l[k] = float(g["l"][k])
+            sa[i].mean_displacement[k] = float(g.get("mean_displacement", (0, 0, 0))[k])
+        sa[i].materialid = int(g.get("materialid", 0))
+        sa[i].tag = int(g.get("tag", 0))
+        sa[i].atomic_frequency = float(g.get("atomic_frequency", -1.0))
+        sa[i].x = float(g.get("x", -1.0e-3))
+    ga = (N.Geometry * max(len(geoms), 1))()
+    for i, g in enumerate(geoms):
+        t = g["type"]
+        ga[i].type = GEOMETRY_TYPES[t] if isinstance(t, str) else int(t)
+        ga[i].order = int(g.get("order", i))
+        inc = g.get("inclusion", "intersection")
+        ga[i].inclusion = _INCLUSION[inc] if isinstance(inc, str) else int(inc)
+        ga[i].exterior = int(bool(g.get("exterior", False)))
+        for k, v in enumerate(g.get("p", ())):
+            ga[i].p[k] = float(v)
+    d.nsites, d.sites = len(sites), C.cast(sa, C.POINTER(N.SiteGroup))
+    d.ngeom, d.geoms = len(geoms), C.cast(ga, C.POINTER(N.Geometry))
+    return d, (sa, ga)
+
+
+def build_lattice(desc: dict) -> dict:
+    """The sites of one lattice (a2c_lattice_build): arrays q, q0, l (n x 3),
+    siteid, matid, tag, sigma, x, in the reference's order."""
+    d, keep = _lattice_struct(desc)
+    msg = C.create_string_buffer(256)
+    out = N.LatticeSites()
+    st = N.lib().a2c_lattice_build(C.byref(d), C.byref(out), msg, 256)
+    if st != N.A2C_OK:
+        raise A2CError(st, "a2c_lattice_build: " + msg.value.decode())
+    n = int(out.count)
+    arr = {"q": np.zeros((n, 3)), "q0": np.zeros((n, 3)), "l": np.zeros((n, 3)),
+           "siteid": np.zeros(n, np.int32), "matid": np.zeros(n, np.int32), "tag": np.zeros(n, np.int32),
+           "sigma": np.zeros(n), "x": np.zeros(n)}
+    if n:
+        out.capacity = n
+        for name in LATTICE_SITE_FIELDS:
+            setattr(out, name, arr[name].ctypes.data)
+        st = N.lib().a2c_lattice_build(C.byref(d), C.byref(out), msg, 256)
+        if st != N.A2C_OK:
+            raise A2CError(st, "a2c_lattice_build: " + msg.value.decode())
+    del keep
+    return arr
+
+
+def lattice_conflicts(q, q_other, dmin: float) -> np.ndarray:
+    """Mask of the sites of q that stay (a2c_lattice_conflicts): False where
+    a site of q_other lies within dmin in every coordinate."""
+    q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
+    qo = np.ascontiguousarray(q_other, dtype=np.float64).reshape(-1, 3)
+    keep = np.ones(len(q), dtype=np.uint8)
+    nrem = C.c_int64(0)
+    N.check(N.lib().a2c_lattice_conflicts(N.ptr(q), len(q), N.ptr(qo), len(qo), float(dmin), N.ptr(keep),
+                                          C.byref(nrem)), "a2c_lattice_conflicts")
+    return keep.astype(bool)
+
+
+def build_lattices(descs: list) -> list:
+    """All lattices of an input (SpaceInitializer::SetupLatticeVariables,
+    SpaceInitializer.cpp:41-116, without regional initial conditions): each
+    built, then lattice i loses its sites within its dmin (MinDistance, or
+    its shortest lattice vector) of lattice j's sites, for every j != i
+    except j < i with a dmin not above i's (already resolved)."""
+    out = [build_lattice(d) for d in descs]
+    dm = []
+    for d in descs:
+        v = float(d.get("dmin", 0.0))
+        if v <= 0.0:
+            abc = np.asarray(d.get("abc", (1, 0, 0, 0, 1, 0, 0, 0, 1)), dtype=np.float64).reshape(3, 3)
+            v = float(np.min(np.sqrt((abc * abc).sum(axis=1))))
+        dm.append(v)
+    for i in range(len(out)):
+        for j in range(len(out)):
+            if j == i or (j < i and dm[j] <= dm[i]):
+                continue
+            keep = lattice_conflicts(out[i]["q"], out[j]["q"], dm[i])
+            if not keep.all():
+                out[i] = {k: v[keep] for k, v in out[i].items()}
+    return out
+
+
 def snapshot_desc(prefix: str, *, fmt: str = "both", precision: int = 2, box=(0.0, 0.0, 0.0), origin=(0.0, 0.0, 0.0),
                   periodic=(0, 0, 0)):
     """Descriptor of a snapshot series (a2c_snapshot_desc): files

@@ -84,6 +84,28 @@ class Input(C.Structure):
                 ("n_used", C.c_int)]
 
 
+class Geometry(C.Structure):
+    _fields_ = [("type", C.c_int), ("order", C.c_int), ("inclusion", C.c_int), ("exterior", C.c_int),
+                ("p", C.c_double * 12)]
+
+
+class SiteGroup(C.Structure):
+    _fields_ = [("l", C.c_double * 3), ("materialid", C.c_int), ("tag", C.c_int), ("atomic_frequency", C.c_double),
+                ("mean_displacement", C.c_double * 3), ("x", C.c_double)]
+
+
+class LatticeDesc(C.Structure):
+    _fields_ = [("abc", C.c_double * 9), ("origin", C.c_double * 3), ("periodic", C.c_int * 3),
+                ("dmin", C.c_double), ("nsites", C.c_int), ("sites", C.POINTER(SiteGroup)), ("ngeom", C.c_int),
+                ("geoms", C.POINTER(Geometry))]
+
+
+class LatticeSites(C.Structure):
+    _fields_ = [("capacity", C.c_int64), ("count", C.c_int64), ("q", C.c_void_p), ("q0", C.c_void_p),
+                ("l", C.c_void_p), ("siteid", C.c_void_p), ("matid", C.c_void_p), ("tag", C.c_void_p),
+                ("sigma", C.c_void_p), ("x", C.c_void_p)]
+
+
 class DmdParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("nu", C.c_double), ("Qm", C.c_double), ("xLb", C.c_double),
                 ("xUb", C.c_double), ("x_bd", C.c_double), ("gamma_bd", C.c_double), ("lbfgs", LbfgsParams),
@@ -129,6 +151,10 @@ def lib() -> C.CDLL:
         "a2c_snapshot_begin": (I, [C.POINTER(SnapshotDesc)]),
         "a2c_input_read": (I, [C.c_char_p, C.POINTER(Input), C.c_char_p, I]),
         "a2c_input_apply": (I, [C.POINTER(Input), C.POINTER(GppParams)]),
+        "a2c_input_lattice": (I, [C.c_char_p, I, C.POINTER(LatticeDesc), C.POINTER(SiteGroup), I,
+                                  C.POINTER(Geometry), I, C.c_char_p, I]),
+        "a2c_lattice_build": (I, [C.POINTER(LatticeDesc), C.POINTER(LatticeSites), C.c_char_p, I]),
+        "a2c_lattice_conflicts": (I, [P, C.c_int64, P, C.c_int64, D, P, C.POINTER(C.c_int64)]),
         "a2c_snapshot_write": (I, [C.POINTER(SnapshotDesc), I, D, I, I, P, P, P, P, P, P]),
         "a2c_gpp_snapshot_async": (I, [P, C.POINTER(SnapshotDesc), I, D, P, P, P, P]),
         "a2c_gpp_snapshot_wait": (I, [P]),
@@ -186,6 +212,7 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_set_occupancy",
             "a2c_gpp_get_occupancy", "a2c_gpp_set_state", "a2c_gpp_get_state", "a2c_gpp_build_neighbors",
             "a2c_gpp_neighbor_total", "a2c_gpp_set_neighbor_skin", "a2c_gpp_update_neighbors", "a2c_snapshot_begin", "a2c_input_read", "a2c_input_apply",
+            "a2c_input_lattice", "a2c_lattice_build", "a2c_lattice_conflicts",
             "a2c_snapshot_write", "a2c_gpp_snapshot_async", "a2c_gpp_snapshot_wait", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
             "a2c_gpp_eval_device", "a2c_gpp_profile_eval", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
             "a2c_gpp_chem_potential", "a2c_gpp_minimize_stats", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",

@@ -28,7 +28,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 # translation units whose arithmetic must not be contracted into FMA
 NO_FMA = {"k_fp64.cu", "k_neighbors.cu", "k_misc.cu", "lbfgs.cu", "batch.cu", "k_lattice.cu"}
 CU_SOURCES = ["api.cu", "k_fp64.cu", "k_neighbors.cu", "k_misc.cu", "lbfgs.cu", "k_mixed.cu", "k_peak.cu", "batch.cu", "k_lattice.cu"]
-CPP_SOURCES = ["lattice.cpp", "tables.cpp", "host_io.cpp", "snapshot.cpp", "input_reader.cpp"]
+CPP_SOURCES = ["lattice.cpp", "lattice_csg.cpp", "tables.cpp", "host_io.cpp", "snapshot.cpp", "input_reader.cpp"]
 
 
 def nvcc() -> str:

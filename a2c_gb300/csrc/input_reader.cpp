@@ -18,6 +18,7 @@
 // CutOffDistance".  The fields the evaluator and the DMD loop use are then
 // read into a2c_input with the reference's defaults (IoData.cpp); the rest
 // of a full input file (geometry, species, ...) is parsed and counted.
+#include <algorithm>
 #include <cctype>
 #include <climits>
 #include <cmath>
@@ -413,6 +414,172 @@ extern "C" a2c_status a2c_input_read(const char *path, a2c_input *in, char *errm
                       in->lattice_periodic[k]);
     in->n_assignments = p.assignments;
     in->n_used = used;
+  } catch (const Error &e) {
+    return err(e.msg);
+  }
+  if (errmsg && errlen > 0) errmsg[0] = 0;
+  return A2C_OK;
+}
+
+namespace {
+
+// Indices k of the blocks "<prefix><name>[k]." present in the file.
+std::vector<int> block_ids(const std::map<std::string, Value> &m, const std::string &prefix, const char *name) {
+  const std::string head = prefix + name + "[";
+  std::vector<int> ids;
+  for (auto it = m.lower_bound(head); it != m.end() && it->first.compare(0, head.size(), head) == 0; ++it) {
+    const size_t close = it->first.find(']', head.size());
+    if (close == std::string::npos || close == head.size()) continue;
+    const std::string num = it->first.substr(head.size(), close - head.size());
+    if (num.find_first_not_of("0123456789") != std::string::npos) continue;
+    const int k = std::atoi(num.c_str());
+    if (ids.empty() || ids.back() != k) ids.push_back(k);
+  }
+  std::sort(ids.begin(), ids.end());
+  ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+  return ids;
+}
+
+const std::vector<std::pair<const char *, int>> kInclusion = {{"Override", 0}, {"Intersection", 1}, {"Union", 2}};
+const std::vector<std::pair<const char *, int>> kSide = {{"Interior", 0}, {"Exterior", 1}};
+const std::vector<std::pair<const char *, int>> kOnOff = {{"Off", 0}, {"On", 1}};
+
+}  // namespace
+
+// Lattice[id] of an input file (LatticeData, LatticeSiteData and the
+// geometry data of IoData.cpp:9-470: names and defaults).
+extern "C" a2c_status a2c_input_lattice(const char *path, int lattice_id, a2c_lattice_desc *desc,
+                                        a2c_site_group *sites, int max_sites, a2c_geometry *geoms, int max_geoms,
+                                        char *errmsg, int errlen) {
+  if (!path || !desc || lattice_id < 0 || max_sites < 0 || max_geoms < 0 || (max_sites > 0 && !sites) ||
+      (max_geoms > 0 && !geoms))
+    return A2C_ERR_INVALID;
+  auto err = [&](const std::string &msg) {
+    if (errmsg && errlen > 0) std::snprintf(errmsg, (size_t)errlen, "%s", msg.c_str());
+    return A2C_ERR_INVALID;
+  };
+  std::ifstream f(path);
+  if (!f) return err(std::string("cannot open ") + path);
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string src = ss.str();  // the lexer reads it in place
+  try {
+    Parser p(src);
+    p.file();
+    const auto &m = p.values;
+    const std::string L = "Lattice[" + std::to_string(lattice_id) + "].";
+    auto key = [&](const std::string &rest) { return L + rest; };
+    std::memset(desc, 0, sizeof(*desc));
+    const char *ax[9] = {"OAx", "OAy", "OAz", "OBx", "OBy", "OBz", "OCx", "OCy", "OCz"};
+    for (int k = 0; k < 9; ++k) {
+      desc->abc[k] = (k % 4 == 0) ? 1.0 : 0.0;
+      get_num(m, key(ax[k]).c_str(), desc->abc[k]);
+    }
+    const char *org[3] = {"Ox", "Oy", "Oz"};
+    for (int k = 0; k < 3; ++k) get_num(m, key(org[k]).c_str(), desc->origin[k]);
+    const char *per[3] = {"PeriodicOA", "PeriodicOB", "PeriodicOC"};
+    for (int k = 0; k < 3; ++k) get_tok(m, key(per[k]).c_str(), {{"False", 0}, {"True", 1}}, desc->periodic[k]);
+    get_num(m, key("MinDistance").c_str(), desc->dmin);
+    char spec[256] = {0};
+    get_str(m, key("CustomGeometry.GeometrySpecifier").c_str(), spec, sizeof(spec));
+    if (spec[0])  // a plug-in loaded with dlopen (SpaceInitializer.cpp:150-178)
+      throw Error{"Lattice[" + std::to_string(lattice_id) + "]: custom geometry plug-ins are not supported"};
+    // sites: ids 0 .. n-1 (LatticeStructure.cpp:80-87)
+    const std::vector<int> sid = block_ids(m, L, "Site");
+    if ((int)sid.size() > max_sites) throw Error{"more sites than the arrays hold"};
+    for (int s = 0; s < (int)sid.size(); ++s) {
+      if (sid[s] != s) throw Error{"site ids must be 0 .. n-1"};
+      const std::string S = "Site[" + std::to_string(s) + "].";
+      a2c_site_group &g = sites[s];
+      g.l[0] = g.l[1] = g.l[2] = -1.0;
+      g.materialid = -1;
+      g.tag = 0;
+      g.atomic_frequency = -1.0;
+      g.mean_displacement[0] = g.mean_displacement[1] = g.mean_displacement[2] = 0.0;
+      g.x = -1.0e-3;
+      get_num(m, key(S + "La").c_str(), g.l[0]);
+      get_num(m, key(S + "Lb").c_str(), g.l[1]);
+      get_num(m, key(S + "Lc").c_str(), g.l[2]);
+      get_int(m, key(S + "MaterialID").c_str(), g.materialid);
+      get_int(m, key(S + "Tag").c_str(), g.tag);
+      get_num(m, key(S + "AtomicFrequency").c_str(), g.atomic_frequency);
+      get_num(m, key(S + "MeanDisplacementX").c_str(), g.mean_displacement[0]);
+      get_num(m, key(S + "MeanDisplacementY").c_str(), g.mean_displacement[1]);
+      get_num(m, key(S + "MeanDisplacementZ").c_str(), g.mean_displacement[2]);
+      get_num(m, key(S + "LocalSpecies[0].MolarFraction").c_str(), g.x);
+    }
+    desc->nsites = (int)sid.size();
+    desc->sites = sites;
+    // geometries, each with its defaults
+    int ng = 0;
+    auto next = [&](int type) -> a2c_geometry & {
+      if (ng >= max_geoms) throw Error{"more geometries than the array holds"};
+      a2c_geometry &g = geoms[ng++];
+      std::memset(&g, 0, sizeof(g));
+      g.type = type;
+      return g;
+    };
+    auto common = [&](a2c_geometry &g, const std::string &G, bool sided) {
+      get_int(m, key(G + "OperationOrder").c_str(), g.order);
+      get_tok(m, key(G + "Inclusion").c_str(), kInclusion, g.inclusion);
+      if (sided) get_tok(m, key(G + "Side").c_str(), kSide, g.exterior);
+    };
+    auto nums = [&](a2c_geometry &g, const std::string &G, std::initializer_list<const char *> names, int at) {
+      for (const char *nm : names) get_num(m, key(G + nm).c_str(), g.p[at++]);
+    };
+    for (int k : block_ids(m, L, "Plane")) {
+      const std::string G = "Plane[" + std::to_string(k) + "].";
+      a2c_geometry &g = next(A2C_GEOM_PLANE);
+      nums(g, G, {"Point_x", "Point_y", "Point_z", "Normal_x", "Normal_y", "Normal_z"}, 0);
+      common(g, G, false);
+    }
+    for (int k : block_ids(m, L, "CylinderAndCone")) {
+      const std::string G = "CylinderAndCone[" + std::to_string(k) + "].";
+      a2c_geometry &g = next(A2C_GEOM_CYLINDER_CONE);
+      g.p[5] = 1.0;   // axis (0, 0, 1)
+      g.p[6] = 1.0;   // radius
+      g.p[8] = 45.0;  // opening angle
+      nums(g, G, {"BaseCenter_x", "BaseCenter_y", "BaseCenter_z", "Axis_x", "Axis_y", "Axis_z", "CylinderRadius",
+                  "CylinderHeight", "ConeOpeningAngleInDegrees", "ConeHeight"},
+           0);
+      common(g, G, true);
+    }
+    for (int k : block_ids(m, L, "CylinderWithSphericalCaps")) {
+      const std::string G = "CylinderWithSphericalCaps[" + std::to_string(k) + "].";
+      a2c_geometry &g = next(A2C_GEOM_CYLINDER_SPHERE);
+      g.p[5] = 1.0;
+      g.p[6] = 1.0;
+      nums(g, G, {"BaseCenter_x", "BaseCenter_y", "BaseCenter_z", "Axis_x", "Axis_y", "Axis_z", "CylinderRadius",
+                  "CylinderHeight"},
+           0);
+      int front = 0, back = 0;
+      get_tok(m, key(G + "FrontSphericalCap").c_str(), kOnOff, front);
+      get_tok(m, key(G + "BackSphericalCap").c_str(), kOnOff, back);
+      g.p[8] = front;
+      g.p[9] = back;
+      common(g, G, true);
+    }
+    for (int k : block_ids(m, L, "Sphere")) {
+      const std::string G = "Sphere[" + std::to_string(k) + "].";
+      a2c_geometry &g = next(A2C_GEOM_SPHERE);
+      g.p[3] = -1.0;
+      nums(g, G, {"Center_x", "Center_y", "Center_z", "Radius"}, 0);
+      common(g, G, true);
+    }
+    for (int k : block_ids(m, L, "Parallelepiped")) {
+      const std::string G = "Parallelepiped[" + std::to_string(k) + "].";
+      a2c_geometry &g = next(A2C_GEOM_PARALLELEPIPED);
+      nums(g, G, {"Px", "Py", "Pz", "Ax", "Ay", "Az", "Bx", "By", "Bz", "Cx", "Cy", "Cz"}, 0);
+      common(g, G, true);
+    }
+    for (int k : block_ids(m, L, "Spheroid")) {
+      const std::string G = "Spheroid[" + std::to_string(k) + "].";
+      a2c_geometry &g = next(A2C_GEOM_SPHEROID);
+      nums(g, G, {"Center_x", "Center_y", "Center_z", "Axis_x", "Axis_y", "Axis_z", "SemiLength", "Radius"}, 0);
+      common(g, G, true);
+    }
+    desc->ngeom = ng;
+    desc->geoms = geoms;
   } catch (const Error &e) {
     return err(e.msg);
   }

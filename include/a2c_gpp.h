@@ -461,6 +461,71 @@ a2c_status a2c_lattice_fcc(const a2c_lattice_spec *spec, double *X, double *xH, 
  * distributions with other values. */
 a2c_status a2c_lattice_fcc_device(const a2c_lattice_spec *spec, double *X, double *xH, int *surface, void *stream);
 
+/* Lattice set-up from an input file's lattice description: replaces
+ * SpaceInitializer::CreateOneLattice (SpaceInitializer.cpp:119-320) and
+ * CheckAndAddSitesInCell (:603-724).  The lattice cells inside the
+ * bounding box of the interior geometries (FindLatticeDomainBoundingBox,
+ * :726-880, with GeoTools' bounding boxes) are visited c, b, a (slowest to
+ * fastest); each site group of a cell is kept when the geometries, applied
+ * in their operation order as Intersection or Union, contain it.  Sites are
+ * in that order.  Not built: the custom-geometry plug-in (dlopen) and the
+ * regional initial conditions (ApplyRegionalICOnOneLattice). */
+enum {
+  A2C_GEOM_PLANE = 0,            /* p: point[3], normal[3]; contains q where (q-point).n/|n| > 0 */
+  A2C_GEOM_CYLINDER_CONE = 1,    /* p: base centre[3], axis[3], radius, height, opening angle (deg), cone height */
+  A2C_GEOM_CYLINDER_SPHERE = 2,  /* p: base centre[3], axis[3], radius, height, front cap (0/1), back cap (0/1) */
+  A2C_GEOM_SPHERE = 3,           /* p: centre[3], radius */
+  A2C_GEOM_PARALLELEPIPED = 4,   /* p: P[3], A[3], B[3], C[3] (vertices: edges PA, PB, PC, right-handed) */
+  A2C_GEOM_SPHEROID = 5          /* p: centre[3], axis[3], semi-length (along the axis), radius */
+};
+enum { A2C_INCLUSION_INTERSECTION = 1, A2C_INCLUSION_UNION = 2 };
+typedef struct a2c_geometry {
+  int type;       /* A2C_GEOM_* */
+  int order;      /* OperationOrder: 0 .. ngeom-1, each once */
+  int inclusion;  /* A2C_INCLUSION_* */
+  int exterior;   /* Side: 0 Interior, 1 Exterior (not read for planes) */
+  double p[12];
+} a2c_geometry;
+typedef struct a2c_site_group {
+  double l[3];               /* La, Lb, Lc: lattice coordinates in the cell */
+  int materialid, tag;
+  double atomic_frequency;   /* the initial width sigma */
+  double mean_displacement[3];
+  double x;                  /* LocalSpecies[0].MolarFraction (-1e-3: not given, the reference's default) */
+} a2c_site_group;
+typedef struct a2c_lattice_desc {
+  double abc[9];        /* lattice vectors OA, OB, OC */
+  double origin[3];
+  int periodic[3];
+  double dmin;          /* MinDistance (<= 0: the shortest lattice vector, as the reference) */
+  int nsites;
+  const a2c_site_group *sites;
+  int ngeom;
+  const a2c_geometry *geoms;
+} a2c_lattice_desc;
+typedef struct a2c_lattice_sites {
+  int64_t capacity;     /* sites the arrays hold; 0 with NULL arrays counts only */
+  int64_t count;        /* set: sites of the lattice (all of them, also when above capacity) */
+  double *q, *q0, *l;   /* 3 per site: position (q0 + mean displacement), lattice position, lattice coordinates */
+  int *siteid, *matid, *tag;
+  double *sigma, *x;
+} a2c_lattice_sites;
+a2c_status a2c_lattice_build(const a2c_lattice_desc *desc, a2c_lattice_sites *out, char *errmsg, int errlen);
+/* SetupLatticeVariables' removal of sites closer than dmin to another
+ * lattice's sites (SpaceInitializer.cpp:94-112, LatticeVariables.cpp:78-140):
+ * keep[i] = 0 for every site i of q (n sites) with a site of q_other
+ * within dmin in every coordinate (the KD-tree box test of
+ * KDTree.h:244-262), else 1.  Returns the number removed in *n_removed. */
+a2c_status a2c_lattice_conflicts(const double *q, int64_t n, const double *q_other, int64_t n_other, double dmin,
+                                 unsigned char *keep, int64_t *n_removed);
+/* Lattice[id] of an input file as a description: sites (capacity
+ * max_sites) and geometries (max_geoms) are filled from the file's
+ * Site[k] and Plane/Sphere/Parallelepiped/Spheroid/CylinderAndCone/
+ * CylinderWithSphericalCaps[k] blocks with the reference's defaults
+ * (IoData.cpp:9-470); desc->sites / geoms point at the arrays given. */
+a2c_status a2c_input_lattice(const char *path, int lattice_id, a2c_lattice_desc *desc, a2c_site_group *sites,
+                             int max_sites, a2c_geometry *geoms, int max_geoms, char *errmsg, int errlen);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,6 +33,7 @@ def build(ref: bool | None = None) -> None:
         ref = REFERENCE_TREE.is_dir()
     if ref:
         subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), "geo"], check=True)
 
 
 class OrcParams(C.Structure):
@@ -409,4 +410,124 @@ def dmd_run(pb: Problem, X, xH, gamma, full_H, off, nbr, hh1_off, hh1, bd_sites,
         out["iters"].append(r["iters"])
     res = {k: np.array(v) for k, v in out.items()}
     res.update(X=X, xH=x0, gamma=g, full_H=fh)
+    return res
+
+
+# ---------------------------------------------------------------------------
+# Lattice set-up against the reference's geometry code (oracle/_ref/
+# libgeo_ref.so, built from GeoTools by `make -C oracle geo`).
+# ---------------------------------------------------------------------------
+GEO_SO = HERE / "_ref" / "libgeo_ref.so"
+_glib = None
+_GEOM_TYPES = {"plane": 0, "cylinder_cone": 1, "cylinder_sphere": 2, "sphere": 3, "parallelepiped": 4, "spheroid": 5}
+
+
+def geo_available() -> bool:
+    return GEO_SO.exists()
+
+
+def glib() -> C.CDLL:
+    global _glib
+    if _glib is None:
+        if not GEO_SO.exists():
+            raise RuntimeError("reference geometry library not built (oracle/_ref); needs the reference tree")
+        L = C.CDLL(str(GEO_SO))
+        L.geo_ref_distance.argtypes = [I, P, P, I64, P]
+        L.geo_ref_bbox.argtypes = [I, P, P, P, P, P]
+        _glib = L
+    return _glib
+
+
+def _gtype(g) -> int:
+    t = g["type"]
+    return _GEOM_TYPES[t] if isinstance(t, str) else int(t)
+
+
+def ref_geo_distance(g: dict, q) -> np.ndarray:
+    """The reference's signed distance (> 0 outside) of points q (n x 3)."""
+    p = np.zeros(12)
+    p[: len(g["p"])] = g["p"]
+    q = np.ascontiguousarray(q, dtype=np.float64).reshape(-1, 3)
+    out = np.empty(len(q))
+    assert glib().geo_ref_distance(_gtype(g), _p(p), _p(q), len(q), _p(out)) == 0
+    return out
+
+
+def ref_geo_bbox(g: dict, origin, abc):
+    p = np.zeros(12)
+    p[: len(g["p"])] = g["p"]
+    O = np.ascontiguousarray(origin, dtype=np.float64)
+    M = np.ascontiguousarray(abc, dtype=np.float64).reshape(9)
+    lo, hi = np.empty(3), np.empty(3)
+    assert glib().geo_ref_bbox(_gtype(g), _p(p), _p(O), _p(M), _p(lo), _p(hi)) == 0
+    return lo, hi
+
+
+def ref_lattice_sites(desc: dict) -> dict:
+    """The sites of one lattice as the reference makes them, restated:
+    SpaceInitializer::CreateOneLattice (SpaceInitializer.cpp:119-320) with
+    CheckAndAddSitesInCell (:603-724) and FindLatticeDomainBoundingBox
+    (:726-880), on one rank, with the reference's own signed distances and
+    bounding boxes (GeoTools).  Returns the same fields as
+    a2c_gb300.build_lattice, plus "dist_min": per site the smallest |signed
+    distance| to any geometry surface it was tested against."""
+    O = np.asarray(desc["origin"], dtype=np.float64)
+    abc = np.asarray(desc["abc"], dtype=np.float64).reshape(3, 3)
+    geoms = desc["geoms"]
+    order = sorted(range(len(geoms)), key=lambda k: geoms[k]["order"])
+    lmin = np.full(3, np.finfo(float).max)
+    lmax = np.full(3, -np.finfo(float).max)
+    for t in (1, 2, 3, 4, 5):  # cylinder-cones, cylinder-spheres, spheres, parallelepipeds, spheroids
+        for g in geoms:
+            if _gtype(g) != t or g.get("exterior", 0):
+                continue
+            lo, hi = ref_geo_bbox(g, O, abc)
+            lmin = np.minimum(lmin, lo)
+            lmax = np.maximum(lmax, hi)
+    if not (np.all(np.isfinite(lmin)) and np.all(np.isfinite(lmax)) and np.all(lmin < lmax)):
+        raise ValueError("unbounded lattice domain")
+    lo_i = [int(np.floor(v)) for v in lmin]
+    hi_i = [int(np.ceil(v)) + 1 for v in lmax]
+    sites = desc["sites"]
+    cells = [(li, lj, lk) for lk in range(lo_i[2], hi_i[2]) for lj in range(lo_i[1], hi_i[1])
+             for li in range(lo_i[0], hi_i[0])]
+    L, sid = [], []
+    for (li, lj, lk) in cells:
+        for s, sg in enumerate(sites):
+            L.append((sg["l"][0] + li, sg["l"][1] + lj, sg["l"][2] + lk))
+            sid.append(s)
+    L = np.array(L, dtype=np.float64).reshape(-1, 3)
+    sid = np.array(sid, dtype=np.int32)
+    # LatticeStructure::GetXYZ: o + la a + lb b + lc c, left to right
+    q0 = ((O + L[:, :1] * abc[0]) + L[:, 1:2] * abc[1]) + L[:, 2:3] * abc[2]
+    inside = np.ones(len(q0), dtype=bool)
+    dmin = np.full(len(q0), np.inf)
+    inc = {"intersection": 1, "union": 2}
+    for k in order:
+        g = geoms[k]
+        gi = g["inclusion"]
+        intersect = (inc[gi] if isinstance(gi, str) else int(gi)) == 1
+        test = (inside & intersect) | (~inside & (not intersect))
+        if not test.any():
+            continue
+        d = ref_geo_distance(g, q0[test])
+        dmin[test] = np.minimum(dmin[test], np.abs(d))
+        if _gtype(g) == 0:
+            new = d > 0.0
+        else:
+            out = d >= 0.0
+            new = out if g.get("exterior", 0) else ~out
+        inside[test] = new
+    keep = inside
+    disp = np.array([sg.get("mean_displacement", (0.0, 0.0, 0.0)) for sg in sites], dtype=np.float64)
+    res = {"q0": q0[keep], "l": L[keep], "siteid": sid[keep]}
+    res["q"] = res["q0"] + disp[res["siteid"]]
+    res["matid"] = np.array([sites[s].get("materialid", 0) for s in res["siteid"]], dtype=np.int32)
+    res["tag"] = np.array([sites[s].get("tag", 0) for s in res["siteid"]], dtype=np.int32)
+    res["sigma"] = np.array([sites[s].get("atomic_frequency", -1.0) for s in res["siteid"]])
+    res["x"] = np.array([sites[s].get("x", -1.0e-3) for s in res["siteid"]])
+    res["dist_min"] = dmin[keep]
+    res["dist_min_all"] = dmin
+    res["inside_all"] = inside
+    res["l_all"] = L
     return res
