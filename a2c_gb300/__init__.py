@@ -552,6 +552,60 @@ def build_lattice(desc: dict) -> dict:
     return arr
 
 
+def _geoms_from(ga, n):
+    return [{"type": g.type, "order": g.order, "inclusion": g.inclusion, "exterior": g.exterior,
+             "p": list(g.p)} for g in ga[:n]]
+
+
+def regions_from_input(path: str, max_regions: int = 64, max_geoms: int = 256) -> list:
+    """The RegionalInitialCondition[k] blocks of an input file
+    (a2c_input_regions) as dicts: lattice_id, materialid, siteid, tag,
+    atomic_frequency, mean_displacement, x, geoms."""
+    ra = (N.Region * max(max_regions, 1))()
+    ga = (N.Geometry * max(max_geoms, 1))()
+    n = C.c_int(0)
+    msg = C.create_string_buffer(256)
+    st = N.lib().a2c_input_regions(str(path).encode(), ra, max_regions, ga, max_geoms, C.byref(n), msg, 256)
+    if st != N.A2C_OK:
+        raise A2CError(st, "a2c_input_regions: " + msg.value.decode())
+    base = C.addressof(ga)
+    out = []
+    for r in ra[: n.value]:
+        first = (C.cast(r.geoms, C.c_void_p).value - base) // C.sizeof(N.Geometry) if r.ngeom else 0
+        out.append({"lattice_id": r.lattice_id, "materialid": r.materialid, "siteid": r.siteid, "tag": r.tag,
+                    "atomic_frequency": r.atomic_frequency, "mean_displacement": list(r.mean_displacement),
+                    "x": r.x, "geoms": _geoms_from(ga[first:first + r.ngeom], r.ngeom)})
+    return out
+
+
+def apply_region(sites: dict, region: dict) -> dict:
+    """A regional initial condition (a2c_lattice_apply_region) applied to a
+    copy of build_lattice's arrays."""
+    out = {k: np.array(v, copy=True) for k, v in sites.items()}
+    d, keep = _lattice_struct({"sites": [], "geoms": region.get("geoms", [])})
+    r = N.Region()
+    r.lattice_id = int(region.get("lattice_id", -1))
+    r.materialid = int(region.get("materialid", -1))
+    r.siteid = int(region.get("siteid", -1))
+    r.tag = int(region.get("tag", 0))
+    r.atomic_frequency = float(region.get("atomic_frequency", -1.0))
+    for k in range(3):
+        r.mean_displacement[k] = float(region.get("mean_displacement", (0, 0, 0))[k])
+    r.x = float(region.get("x", -1.0e-3))
+    r.ngeom, r.geoms = d.ngeom, d.geoms
+    ls = N.LatticeSites()
+    ls.capacity = ls.count = len(out["q"])
+    for name in LATTICE_SITE_FIELDS:
+        out[name] = np.ascontiguousarray(out[name])
+        setattr(ls, name, out[name].ctypes.data)
+    msg = C.create_string_buffer(256)
+    st = N.lib().a2c_lattice_apply_region(C.byref(r), C.byref(ls), msg, 256)
+    if st != N.A2C_OK:
+        raise A2CError(st, "a2c_lattice_apply_region: " + msg.value.decode())
+    del keep
+    return out
+
+
 def lattice_conflicts(q, q_other, dmin: float) -> np.ndarray:
     """Mask of the sites of q that stay (a2c_lattice_conflicts): False where
     a site of q_other lies within dmin in every coordinate."""
@@ -564,13 +618,20 @@ def lattice_conflicts(q, q_other, dmin: float) -> np.ndarray:
     return keep.astype(bool)
 
 
-def build_lattices(descs: list) -> list:
+def build_lattices(descs: list, regions: list | None = None) -> list:
     """All lattices of an input (SpaceInitializer::SetupLatticeVariables,
-    SpaceInitializer.cpp:41-116, without regional initial conditions): each
-    built, then lattice i loses its sites within its dmin (MinDistance, or
-    its shortest lattice vector) of lattice j's sites, for every j != i
-    except j < i with a dmin not above i's (already resolved)."""
+    SpaceInitializer.cpp:41-116): each built; the regional initial
+    conditions applied in index order (lattice_id < 0: to every lattice);
+    then lattice i loses its sites within its dmin (MinDistance, or its
+    shortest lattice vector) of lattice j's sites, for every j != i except
+    j < i with a dmin not above i's (already resolved)."""
     out = [build_lattice(d) for d in descs]
+    for r in regions or []:
+        lid = int(r.get("lattice_id", -1))
+        if lid >= len(out):
+            raise A2CError(N.A2C_ERR_INVALID, f"RegionalInitialCondition: unknown lattice id {lid}")
+        for k in (range(len(out)) if lid < 0 else [lid]):
+            out[k] = apply_region(out[k], r)
     dm = []
     for d in descs:
         v = float(d.get("dmin", 0.0))

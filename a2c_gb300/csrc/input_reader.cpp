@@ -444,6 +444,85 @@ const std::vector<std::pair<const char *, int>> kInclusion = {{"Override", 0}, {
 const std::vector<std::pair<const char *, int>> kSide = {{"Interior", 0}, {"Exterior", 1}};
 const std::vector<std::pair<const char *, int>> kOnOff = {{"Off", 0}, {"On", 1}};
 
+// The geometry blocks under `prefix` (Plane, CylinderAndCone,
+// CylinderWithSphericalCaps, Sphere, Parallelepiped, Spheroid; IoData.cpp:
+// 9-330, names and defaults) into geoms[ng ..]; returns the new count.
+int read_geometries(const std::map<std::string, Value> &m, const std::string &prefix, a2c_geometry *geoms,
+                    int max_geoms, int ng) {
+  auto key = [&](const std::string &rest) { return prefix + rest; };
+  auto next = [&](int type) -> a2c_geometry & {
+    if (ng >= max_geoms) throw Error{"more geometries than the array holds"};
+    a2c_geometry &g = geoms[ng++];
+    std::memset(&g, 0, sizeof(g));
+    g.type = type;
+    return g;
+  };
+  auto common = [&](a2c_geometry &g, const std::string &G, bool sided) {
+    get_int(m, key(G + "OperationOrder").c_str(), g.order);
+    get_tok(m, key(G + "Inclusion").c_str(), kInclusion, g.inclusion);
+    if (sided) get_tok(m, key(G + "Side").c_str(), kSide, g.exterior);
+  };
+  auto nums = [&](a2c_geometry &g, const std::string &G, std::initializer_list<const char *> names, int at) {
+    for (const char *nm : names) get_num(m, key(G + nm).c_str(), g.p[at++]);
+  };
+  char spec[256] = {0};
+  get_str(m, key("CustomGeometry.GeometrySpecifier").c_str(), spec, sizeof(spec));
+  if (spec[0])  // a plug-in loaded with dlopen (SpaceInitializer.cpp:150-178)
+    throw Error{prefix + "CustomGeometry: geometry plug-ins are not supported"};
+  for (int k : block_ids(m, prefix, "Plane")) {
+    const std::string G = "Plane[" + std::to_string(k) + "].";
+    a2c_geometry &g = next(A2C_GEOM_PLANE);
+    nums(g, G, {"Point_x", "Point_y", "Point_z", "Normal_x", "Normal_y", "Normal_z"}, 0);
+    common(g, G, false);
+  }
+  for (int k : block_ids(m, prefix, "CylinderAndCone")) {
+    const std::string G = "CylinderAndCone[" + std::to_string(k) + "].";
+    a2c_geometry &g = next(A2C_GEOM_CYLINDER_CONE);
+    g.p[5] = 1.0;   // axis (0, 0, 1)
+    g.p[6] = 1.0;   // radius
+    g.p[8] = 45.0;  // opening angle
+    nums(g, G, {"BaseCenter_x", "BaseCenter_y", "BaseCenter_z", "Axis_x", "Axis_y", "Axis_z", "CylinderRadius",
+                "CylinderHeight", "ConeOpeningAngleInDegrees", "ConeHeight"},
+         0);
+    common(g, G, true);
+  }
+  for (int k : block_ids(m, prefix, "CylinderWithSphericalCaps")) {
+    const std::string G = "CylinderWithSphericalCaps[" + std::to_string(k) + "].";
+    a2c_geometry &g = next(A2C_GEOM_CYLINDER_SPHERE);
+    g.p[5] = 1.0;
+    g.p[6] = 1.0;
+    nums(g, G, {"BaseCenter_x", "BaseCenter_y", "BaseCenter_z", "Axis_x", "Axis_y", "Axis_z", "CylinderRadius",
+                "CylinderHeight"},
+         0);
+    int front = 0, back = 0;
+    get_tok(m, key(G + "FrontSphericalCap").c_str(), kOnOff, front);
+    get_tok(m, key(G + "BackSphericalCap").c_str(), kOnOff, back);
+    g.p[8] = front;
+    g.p[9] = back;
+    common(g, G, true);
+  }
+  for (int k : block_ids(m, prefix, "Sphere")) {
+    const std::string G = "Sphere[" + std::to_string(k) + "].";
+    a2c_geometry &g = next(A2C_GEOM_SPHERE);
+    g.p[3] = -1.0;
+    nums(g, G, {"Center_x", "Center_y", "Center_z", "Radius"}, 0);
+    common(g, G, true);
+  }
+  for (int k : block_ids(m, prefix, "Parallelepiped")) {
+    const std::string G = "Parallelepiped[" + std::to_string(k) + "].";
+    a2c_geometry &g = next(A2C_GEOM_PARALLELEPIPED);
+    nums(g, G, {"Px", "Py", "Pz", "Ax", "Ay", "Az", "Bx", "By", "Bz", "Cx", "Cy", "Cz"}, 0);
+    common(g, G, true);
+  }
+  for (int k : block_ids(m, prefix, "Spheroid")) {
+    const std::string G = "Spheroid[" + std::to_string(k) + "].";
+    a2c_geometry &g = next(A2C_GEOM_SPHEROID);
+    nums(g, G, {"Center_x", "Center_y", "Center_z", "Axis_x", "Axis_y", "Axis_z", "SemiLength", "Radius"}, 0);
+    common(g, G, true);
+  }
+  return ng;
+}
+
 }  // namespace
 
 // Lattice[id] of an input file (LatticeData, LatticeSiteData and the
@@ -480,10 +559,6 @@ extern "C" a2c_status a2c_input_lattice(const char *path, int lattice_id, a2c_la
     const char *per[3] = {"PeriodicOA", "PeriodicOB", "PeriodicOC"};
     for (int k = 0; k < 3; ++k) get_tok(m, key(per[k]).c_str(), {{"False", 0}, {"True", 1}}, desc->periodic[k]);
     get_num(m, key("MinDistance").c_str(), desc->dmin);
-    char spec[256] = {0};
-    get_str(m, key("CustomGeometry.GeometrySpecifier").c_str(), spec, sizeof(spec));
-    if (spec[0])  // a plug-in loaded with dlopen (SpaceInitializer.cpp:150-178)
-      throw Error{"Lattice[" + std::to_string(lattice_id) + "]: custom geometry plug-ins are not supported"};
     // sites: ids 0 .. n-1 (LatticeStructure.cpp:80-87)
     const std::vector<int> sid = block_ids(m, L, "Site");
     if ((int)sid.size() > max_sites) throw Error{"more sites than the arrays hold"};
@@ -511,75 +586,62 @@ extern "C" a2c_status a2c_input_lattice(const char *path, int lattice_id, a2c_la
     desc->nsites = (int)sid.size();
     desc->sites = sites;
     // geometries, each with its defaults
-    int ng = 0;
-    auto next = [&](int type) -> a2c_geometry & {
-      if (ng >= max_geoms) throw Error{"more geometries than the array holds"};
-      a2c_geometry &g = geoms[ng++];
-      std::memset(&g, 0, sizeof(g));
-      g.type = type;
-      return g;
-    };
-    auto common = [&](a2c_geometry &g, const std::string &G, bool sided) {
-      get_int(m, key(G + "OperationOrder").c_str(), g.order);
-      get_tok(m, key(G + "Inclusion").c_str(), kInclusion, g.inclusion);
-      if (sided) get_tok(m, key(G + "Side").c_str(), kSide, g.exterior);
-    };
-    auto nums = [&](a2c_geometry &g, const std::string &G, std::initializer_list<const char *> names, int at) {
-      for (const char *nm : names) get_num(m, key(G + nm).c_str(), g.p[at++]);
-    };
-    for (int k : block_ids(m, L, "Plane")) {
-      const std::string G = "Plane[" + std::to_string(k) + "].";
-      a2c_geometry &g = next(A2C_GEOM_PLANE);
-      nums(g, G, {"Point_x", "Point_y", "Point_z", "Normal_x", "Normal_y", "Normal_z"}, 0);
-      common(g, G, false);
-    }
-    for (int k : block_ids(m, L, "CylinderAndCone")) {
-      const std::string G = "CylinderAndCone[" + std::to_string(k) + "].";
-      a2c_geometry &g = next(A2C_GEOM_CYLINDER_CONE);
-      g.p[5] = 1.0;   // axis (0, 0, 1)
-      g.p[6] = 1.0;   // radius
-      g.p[8] = 45.0;  // opening angle
-      nums(g, G, {"BaseCenter_x", "BaseCenter_y", "BaseCenter_z", "Axis_x", "Axis_y", "Axis_z", "CylinderRadius",
-                  "CylinderHeight", "ConeOpeningAngleInDegrees", "ConeHeight"},
-           0);
-      common(g, G, true);
-    }
-    for (int k : block_ids(m, L, "CylinderWithSphericalCaps")) {
-      const std::string G = "CylinderWithSphericalCaps[" + std::to_string(k) + "].";
-      a2c_geometry &g = next(A2C_GEOM_CYLINDER_SPHERE);
-      g.p[5] = 1.0;
-      g.p[6] = 1.0;
-      nums(g, G, {"BaseCenter_x", "BaseCenter_y", "BaseCenter_z", "Axis_x", "Axis_y", "Axis_z", "CylinderRadius",
-                  "CylinderHeight"},
-           0);
-      int front = 0, back = 0;
-      get_tok(m, key(G + "FrontSphericalCap").c_str(), kOnOff, front);
-      get_tok(m, key(G + "BackSphericalCap").c_str(), kOnOff, back);
-      g.p[8] = front;
-      g.p[9] = back;
-      common(g, G, true);
-    }
-    for (int k : block_ids(m, L, "Sphere")) {
-      const std::string G = "Sphere[" + std::to_string(k) + "].";
-      a2c_geometry &g = next(A2C_GEOM_SPHERE);
-      g.p[3] = -1.0;
-      nums(g, G, {"Center_x", "Center_y", "Center_z", "Radius"}, 0);
-      common(g, G, true);
-    }
-    for (int k : block_ids(m, L, "Parallelepiped")) {
-      const std::string G = "Parallelepiped[" + std::to_string(k) + "].";
-      a2c_geometry &g = next(A2C_GEOM_PARALLELEPIPED);
-      nums(g, G, {"Px", "Py", "Pz", "Ax", "Ay", "Az", "Bx", "By", "Bz", "Cx", "Cy", "Cz"}, 0);
-      common(g, G, true);
-    }
-    for (int k : block_ids(m, L, "Spheroid")) {
-      const std::string G = "Spheroid[" + std::to_string(k) + "].";
-      a2c_geometry &g = next(A2C_GEOM_SPHEROID);
-      nums(g, G, {"Center_x", "Center_y", "Center_z", "Axis_x", "Axis_y", "Axis_z", "SemiLength", "Radius"}, 0);
-      common(g, G, true);
-    }
+    const int ng = read_geometries(m, L, geoms, max_geoms, 0);
     desc->ngeom = ng;
     desc->geoms = geoms;
+  } catch (const Error &e) {
+    return err(e.msg);
+  }
+  if (errmsg && errlen > 0) errmsg[0] = 0;
+  return A2C_OK;
+}
+
+// RegionalInitialCondition[k] blocks (RegionalIcData, IoData.cpp:578-624).
+extern "C" a2c_status a2c_input_regions(const char *path, a2c_region *regions, int max_regions,
+                                        a2c_geometry *geoms, int max_geoms, int *n_regions, char *errmsg,
+                                        int errlen) {
+  if (!path || !n_regions || max_regions < 0 || max_geoms < 0 || (max_regions > 0 && !regions) ||
+      (max_geoms > 0 && !geoms))
+    return A2C_ERR_INVALID;
+  auto err = [&](const std::string &msg) {
+    if (errmsg && errlen > 0) std::snprintf(errmsg, (size_t)errlen, "%s", msg.c_str());
+    return A2C_ERR_INVALID;
+  };
+  std::ifstream f(path);
+  if (!f) return err(std::string("cannot open ") + path);
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string src = ss.str();  // the lexer reads it in place
+  try {
+    Parser p(src);
+    p.file();
+    const auto &m = p.values;
+    const std::vector<int> ids = block_ids(m, "", "RegionalInitialCondition");
+    if ((int)ids.size() > max_regions) throw Error{"more regions than the array holds"};
+    int ng = 0;
+    for (int k = 0; k < (int)ids.size(); ++k) {
+      if (ids[k] != k) throw Error{"RegionalInitialCondition ids must be 0 .. n-1"};
+      const std::string R = "RegionalInitialCondition[" + std::to_string(k) + "].";
+      a2c_region &r = regions[k];
+      std::memset(&r, 0, sizeof(r));
+      r.lattice_id = r.materialid = r.siteid = -1;
+      r.atomic_frequency = -1.0;
+      r.x = -1.0e-3;
+      get_int(m, (R + "LatticeID").c_str(), r.lattice_id);
+      get_int(m, (R + "MaterialID").c_str(), r.materialid);
+      get_int(m, (R + "SiteID").c_str(), r.siteid);
+      get_int(m, (R + "Tag").c_str(), r.tag);
+      get_num(m, (R + "AtomicFrequency").c_str(), r.atomic_frequency);
+      get_num(m, (R + "MeanDisplacementX").c_str(), r.mean_displacement[0]);
+      get_num(m, (R + "MeanDisplacementY").c_str(), r.mean_displacement[1]);
+      get_num(m, (R + "MeanDisplacementZ").c_str(), r.mean_displacement[2]);
+      get_num(m, (R + "LocalSpecies[0].MolarFraction").c_str(), r.x);
+      const int ng1 = read_geometries(m, R, geoms, max_geoms, ng);
+      r.ngeom = ng1 - ng;
+      r.geoms = geoms + ng;
+      ng = ng1;
+    }
+    *n_regions = (int)ids.size();
   } catch (const Error &e) {
     return err(e.msg);
   }

@@ -320,6 +320,35 @@ void lattice_box(const std::vector<Geom> &geoms, const Frame &F, V &lmin, V &lma
       throw Fail{"unable to find a bounding box for the lattice domain: it is unbounded"};
 }
 
+// Geometries prepared, and their indices in operation order
+// (SortUserSpecifiedGeometries, SpaceInitializer.cpp:326-600).
+void prepare_ordered(const a2c_geometry *g, int ng, std::vector<Geom> &geoms, std::vector<int> &order) {
+  order.assign(ng, -1);
+  geoms.clear();
+  geoms.reserve(ng);
+  for (int k = 0; k < ng; ++k) {
+    if (g[k].order < 0 || g[k].order >= ng || order[g[k].order] != -1)
+      throw Fail{"geometry " + std::to_string(k) + " has an invalid or conflicting order (" +
+                 std::to_string(g[k].order) + ")"};
+    if (g[k].inclusion != A2C_INCLUSION_INTERSECTION && g[k].inclusion != A2C_INCLUSION_UNION)
+      throw Fail{"unsupported geometry inclusion operator (must be Intersection or Union)"};
+    order[g[k].order] = k;
+    geoms.push_back(prepare(g[k]));
+  }
+}
+
+// Whether the geometries, applied in order from "everything", contain q
+// (CheckAndAddSitesInCell, SpaceInitializer.cpp:622-698).
+bool inside_all(const std::vector<Geom> &geoms, const std::vector<int> &order, const V &q) {
+  bool in = true;
+  for (int k : order) {
+    const Geom &G = geoms[k];
+    const bool intersect = G.g.inclusion == A2C_INCLUSION_INTERSECTION;
+    if ((in && intersect) || (!in && !intersect)) in = contains(G, q);
+  }
+  return in;
+}
+
 a2c_status fail(char *errmsg, int errlen, const std::string &m) {
   if (errmsg && errlen > 0) std::snprintf(errmsg, (size_t)errlen, "%s", m.c_str());
   return A2C_ERR_INVALID;
@@ -349,21 +378,9 @@ extern "C" a2c_status a2c_lattice_build(const a2c_lattice_desc *d, a2c_lattice_s
           throw Fail{"site coordinates must be in [0, 1) (site " + std::to_string(s) + ")"};
       if (d->sites[s].materialid < 0) throw Fail{"site " + std::to_string(s) + " has no material id"};
     }
-    // operation order (SortUserSpecifiedGeometries, SpaceInitializer.cpp:326-600)
-    const int ng = d->ngeom;
-    std::vector<int> order(ng, -1);
+    std::vector<int> order;
     std::vector<Geom> geoms;
-    geoms.reserve(ng);
-    for (int k = 0; k < ng; ++k) {
-      const a2c_geometry &g = d->geoms[k];
-      if (g.order < 0 || g.order >= ng || order[g.order] != -1)
-        throw Fail{"geometry " + std::to_string(k) + " has an invalid or conflicting order (" +
-                   std::to_string(g.order) + ")"};
-      if (g.inclusion != A2C_INCLUSION_INTERSECTION && g.inclusion != A2C_INCLUSION_UNION)
-        throw Fail{"unsupported geometry inclusion operator (must be Intersection or Union)"};
-      order[g.order] = k;
-      geoms.push_back(prepare(g));
-    }
+    prepare_ordered(d->geoms, d->ngeom, geoms, order);
     V lmin, lmax;
     lattice_box(geoms, F, lmin, lmax);
     int lo[3], hi[3];
@@ -379,13 +396,7 @@ extern "C" a2c_status a2c_lattice_build(const a2c_lattice_desc *d, a2c_lattice_s
             const a2c_site_group &sg = d->sites[s];
             const V l = mk(sg.l[0] + li, sg.l[1] + lj, sg.l[2] + lk);
             const V q = F.O + l[0] * F.d[0] + l[1] * F.d[1] + l[2] * F.d[2];  // LatticeStructure::GetXYZ
-            bool in = true;
-            for (int o = 0; o < ng; ++o) {
-              const Geom &G = geoms[order[o]];
-              const bool intersect = G.g.inclusion == A2C_INCLUSION_INTERSECTION;
-              if ((in && intersect) || (!in && !intersect)) in = contains(G, q);
-            }
-            if (!in) continue;
+            if (!inside_all(geoms, order, q)) continue;
             if (n < out->capacity) {
               for (int k = 0; k < 3; ++k) {
                 out->l[3 * n + k] = l[k];
@@ -401,6 +412,32 @@ extern "C" a2c_status a2c_lattice_build(const a2c_lattice_desc *d, a2c_lattice_s
             ++n;
           }
     out->count = n;
+  } catch (const Fail &e) {
+    return fail(errmsg, errlen, e.msg);
+  }
+  if (errmsg && errlen > 0) errmsg[0] = 0;
+  return A2C_OK;
+}
+
+extern "C" a2c_status a2c_lattice_apply_region(const a2c_region *r, a2c_lattice_sites *out, char *errmsg,
+                                               int errlen) {
+  if (!r || !out || r->ngeom < 0 || (r->ngeom > 0 && !r->geoms) || out->count < 0)
+    return fail(errmsg, errlen, "invalid arguments");
+  if (out->count > 0 && (!out->q || !out->siteid || !out->matid || !out->tag || !out->sigma || !out->x))
+    return fail(errmsg, errlen, "site arrays missing");
+  try {
+    std::vector<int> order;
+    std::vector<Geom> geoms;
+    prepare_ordered(r->geoms, r->ngeom, geoms, order);
+    for (int64_t i = 0; i < out->count; ++i) {
+      if (out->matid[i] != r->materialid || out->siteid[i] != r->siteid) continue;
+      double *q = out->q + 3 * i;
+      if (!inside_all(geoms, order, mk(q[0], q[1], q[2]))) continue;
+      for (int k = 0; k < 3; ++k) q[k] += r->mean_displacement[k];
+      out->sigma[i] = r->atomic_frequency;
+      out->tag[i] = r->tag;
+      if (r->x >= 0.0) out->x[i] = r->x;
+    }
   } catch (const Fail &e) {
     return fail(errmsg, errlen, e.msg);
   }

@@ -518,6 +518,31 @@ a2c_status a2c_lattice_build(const a2c_lattice_desc *desc, a2c_lattice_sites *ou
  * KDTree.h:244-262), else 1.  Returns the number removed in *n_removed. */
 a2c_status a2c_lattice_conflicts(const double *q, int64_t n, const double *q_other, int64_t n_other, double dmin,
                                  unsigned char *keep, int64_t *n_removed);
+/* A regional initial condition (RegionalIcData; applied by
+ * SpaceInitializer::ApplyRegionalICOnOneLattice, SpaceInitializer.cpp:
+ * 883-1040): on the sites of material materialid and site group siteid
+ * whose current position q the geometries contain (the rule of
+ * a2c_lattice_build), q moves by mean_displacement, sigma becomes
+ * atomic_frequency (as given: the reference sets it also when left at its
+ * -1 default), tag becomes tag, and x becomes x when x >= 0 (the first
+ * LocalSpecies' MolarFraction; one species per site here).  lattice_id < 0:
+ * every lattice. */
+typedef struct a2c_region {
+  int lattice_id, materialid, siteid, tag;
+  double atomic_frequency;
+  double mean_displacement[3];
+  double x;
+  int ngeom;
+  const a2c_geometry *geoms;
+} a2c_region;
+/* Applies one region to out->count sites (arrays as a2c_lattice_build
+ * filled them), in place. */
+a2c_status a2c_lattice_apply_region(const a2c_region *region, a2c_lattice_sites *sites, char *errmsg, int errlen);
+/* The RegionalInitialCondition[k] blocks of an input file, k = 0 .. n-1,
+ * into regions[] (max_regions) with their geometries stored in geoms[]
+ * (max_geoms in all); *n_regions receives n. */
+a2c_status a2c_input_regions(const char *path, a2c_region *regions, int max_regions, a2c_geometry *geoms,
+                             int max_geoms, int *n_regions, char *errmsg, int errlen);
 /* Lattice[id] of an input file as a description: sites (capacity
  * max_sites) and geometries (max_geoms) are filled from the file's
  * Site[k] and Plane/Sphere/Parallelepiped/Spheroid/CylinderAndCone/

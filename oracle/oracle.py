@@ -531,3 +531,36 @@ def ref_lattice_sites(desc: dict) -> dict:
     res["inside_all"] = inside
     res["l_all"] = L
     return res
+
+
+def ref_apply_region(sites: dict, region: dict) -> dict:
+    """A regional initial condition as the reference applies it, restated:
+    SpaceInitializer::ApplyRegionalICOnOneLattice (SpaceInitializer.cpp:
+    883-1040) with the reference's own signed distances, on a copy."""
+    out = {k: np.array(v, copy=True) for k, v in sites.items()}
+    sel = (out["matid"] == region.get("materialid", -1)) & (out["siteid"] == region.get("siteid", -1))
+    idx = np.nonzero(sel)[0]
+    geoms = region.get("geoms", [])
+    inside = np.ones(len(idx), dtype=bool)
+    inc = {"intersection": 1, "union": 2}
+    for k in sorted(range(len(geoms)), key=lambda k: geoms[k]["order"]):
+        g = geoms[k]
+        gi = g["inclusion"]
+        intersect = (inc[gi] if isinstance(gi, str) else int(gi)) == 1
+        test = (inside & intersect) | (~inside & (not intersect))
+        if not test.any():
+            continue
+        d = ref_geo_distance(g, out["q"][idx[test]])
+        if _gtype(g) == 0:
+            new = d > 0.0
+        else:
+            o = d >= 0.0
+            new = o if g.get("exterior", 0) else ~o
+        inside[test] = new
+    hit = idx[inside]
+    out["q"][hit] += np.asarray(region.get("mean_displacement", (0.0, 0.0, 0.0)), dtype=np.float64)
+    out["sigma"][hit] = region.get("atomic_frequency", -1.0)
+    out["tag"][hit] = region.get("tag", 0)
+    if region.get("x", -1.0e-3) >= 0.0:
+        out["x"][hit] = region["x"]
+    return out

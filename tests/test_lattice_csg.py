@@ -266,4 +266,77 @@ def test_input_file_rejects_plugin(tmp_path):
                  '  under CustomGeometry { GeometrySpecifier = "libgeom.so"; } }\n')
     with pytest.raises(A.A2CError) as e:
         A.lattice_from_input(str(f), 0)
-    assert "custom geometry" in str(e.value)
+    assert "plug-ins are not supported" in str(e.value)
+
+
+def region(geoms, **kw):
+    r = {"lattice_id": -1, "materialid": 0, "siteid": 0, "tag": 5, "atomic_frequency": 0.2,
+         "mean_displacement": (0.0, 0.0, 0.05), "x": 0.8, "geoms": geoms}
+    r.update(kw)
+    return r
+
+
+@needs_ref
+def test_regions_follow_the_reference():
+    a = A_PD
+    d = dict(cubic(), sites=sites(FCC + OCT, x=0.01), geoms=[box((-0.2, -0.2, -0.2), [[5 * a, 0, 0],
+                                                                                     [0, 5 * a, 0],
+                                                                                     [0, 0, 5 * a]])])
+    s = A.build_lattice(d)
+    regs = [region([sphere((9.0, 9.0, 9.0), 6.0)]),
+            region([sphere((9.0, 9.0, 9.0), 7.0), sphere((9.0, 9.0, 9.0), 3.0, order=1, exterior=1),
+                    plane((0, 0, 8.0), (0, 0, 1), order=2, inclusion="union")], siteid=5, x=-1.0e-3, tag=9),
+            region([box((0.5, 0.5, 0.5), [[8, 0, 0], [0, 8, 0], [0, 0, 8]])], materialid=1)]  # no such material
+    ours, ref = s, s
+    for r in regs:
+        ours = A.apply_region(ours, r)
+        ref = O.ref_apply_region(ref, r)
+        for k in A.LATTICE_SITE_FIELDS:
+            assert np.array_equal(ours[k], ref[k]), k
+    changed = ours["tag"] != s["tag"]
+    assert changed.any() and set(ours["tag"][changed]) <= {5, 9}
+    assert np.array_equal(ours["sigma"][ours["tag"] == 5], np.full((ours["tag"] == 5).sum(), 0.2))
+
+
+def test_regions_from_input(tmp_path):
+    f = tmp_path / "input.st"
+    f.write_text(textwrap.dedent("""
+        under Lattice[0] {
+          OAx = 3.89; OBy = 3.89; OCz = 3.89; MinDistance = 1.0;
+          under Site[0] { La = 0.0; Lb = 0.0; Lc = 0.0; MaterialID = 0; AtomicFrequency = 0.1; }
+          under Site[1] { La = 0.5; Lb = 0.5; Lc = 0.5; MaterialID = 0; AtomicFrequency = 0.1;
+                          under LocalSpecies[0] { SpeciesID = 1; MolarFraction = 0.01; } }
+          under Sphere[0] { Center_x = 8.0; Center_y = 8.0; Center_z = 8.0; Radius = 8.5;
+                            Side = Interior; Inclusion = Intersection; OperationOrder = 0; }
+        }
+        under RegionalInitialCondition[0] {
+          LatticeID = 0; MaterialID = 0; SiteID = 1; Tag = 4; AtomicFrequency = 0.12;
+          MeanDisplacementZ = 0.02;
+          under LocalSpecies[0] { SpeciesID = 1; MolarFraction = 0.75; }
+          under Sphere[0] { Center_x = 8.0; Center_y = 8.0; Center_z = 8.0; Radius = 4.0;
+                            Side = Interior; Inclusion = Intersection; OperationOrder = 0; }
+        }
+        under RegionalInitialCondition[1] {
+          MaterialID = 0; SiteID = 0; Tag = 2;
+          under Plane[0] { Point_z = 8.0; Normal_z = 1.0; Inclusion = Intersection; }
+        }
+    """))
+    regs = A.regions_from_input(str(f))
+    assert len(regs) == 2
+    r0, r1 = regs
+    assert (r0["lattice_id"], r0["materialid"], r0["siteid"], r0["tag"]) == (0, 0, 1, 4)
+    assert r0["atomic_frequency"] == 0.12 and r0["mean_displacement"] == [0.0, 0.0, 0.02] and r0["x"] == 0.75
+    assert len(r0["geoms"]) == 1 and r0["geoms"][0]["type"] == A.GEOMETRY_TYPES["sphere"]
+    assert r1["lattice_id"] == -1 and r1["atomic_frequency"] == -1.0 and r1["x"] == -1.0e-3  # defaults
+    assert r1["geoms"][0]["type"] == A.GEOMETRY_TYPES["plane"] and r1["geoms"][0]["p"][5] == 1.0
+    [lat] = A.build_lattices([A.lattice_from_input(str(f), 0)], regs)
+    base = A.build_lattice(A.lattice_from_input(str(f), 0))
+    hit = (lat["siteid"] == 1) & (lat["tag"] == 4)
+    assert hit.any() and np.all(lat["x"][hit] == 0.75) and np.all(lat["sigma"][hit] == 0.12)
+    assert np.allclose(lat["q"][hit] - base["q"][hit], (0, 0, 0.02), rtol=0, atol=1e-15)
+    top = (lat["siteid"] == 0) & (lat["q"][:, 2] > 8.0)
+    assert np.all(lat["tag"][top] == 2) and np.all(lat["sigma"][top] == -1.0)  # set as given, as the reference
+    if O.geo_available():
+        ref = O.ref_apply_region(O.ref_apply_region(base, r0), r1)
+        for k in A.LATTICE_SITE_FIELDS:
+            assert np.array_equal(lat[k], ref[k]), k
