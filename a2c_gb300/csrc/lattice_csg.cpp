@@ -384,10 +384,17 @@ extern "C" a2c_status a2c_lattice_build(const a2c_lattice_desc *d, a2c_lattice_s
     V lmin, lmax;
     lattice_box(geoms, F, lmin, lmax);
     int lo[3], hi[3];
+    double cells = 1.0;
     for (int i = 0; i < 3; ++i) {
+      // the reference's guard (a long long that is never infinite) cannot
+      // fire; here the cell range must fit int and the scan a few 1e10 sites
+      if (std::fabs(lmin[i]) > 1.0e9 || std::fabs(lmax[i]) > 1.0e9)
+        throw Fail{"the bounding box of the lattice domain is too large"};
       lo[i] = (int)std::floor(lmin[i]);
       hi[i] = (int)std::ceil(lmax[i]) + 1;  // one past the last cell
+      cells *= (double)(hi[i] - lo[i]);
     }
+    if (cells * (double)d->nsites > 4.0e10) throw Fail{"the bounding box of the lattice domain is too large"};
     int64_t n = 0;
     for (int lk = lo[2]; lk < hi[2]; ++lk)
       for (int lj = lo[1]; lj < hi[1]; ++lj)
@@ -468,10 +475,14 @@ extern "C" a2c_status a2c_lattice_conflicts(const double *q, int64_t n, const do
       lo[k] = std::min(lo[k], q_other[3 * j + k]);
       hi[k] = std::max(hi[k], q_other[3 * j + k]);
     }
+  // cells of about dmin, at most ~2 per point of q_other (any grid gives
+  // the same answer: every cell meeting the query cube is searched)
+  const double budget = std::max(1.0, std::min(2.0 * (double)n_other, 16.0 * 1024 * 1024));
+  const double per_axis = std::cbrt(budget);
   int64_t dim[3];
   for (int k = 0; k < 3; ++k) {
-    dim[k] = (int64_t)std::floor((hi[k] - lo[k]) / dmin) + 1;
-    dim[k] = std::max<int64_t>(1, std::min<int64_t>(dim[k], 1024));
+    const double want = std::floor((hi[k] - lo[k]) / dmin) + 1.0;
+    dim[k] = (int64_t)std::max(1.0, std::min(want, per_axis));
   }
   auto cell_of = [&](double x, int k) {
     int64_t c = (int64_t)std::floor((x - lo[k]) / (hi[k] - lo[k] > 0 ? (hi[k] - lo[k]) / dim[k] : 1.0));

@@ -181,6 +181,7 @@ def test_attributes_and_displacement():
     ({"sites": [{"l": (1.0, 0.0, 0.0), "materialid": 0}]}, "[0, 1)"),
     ({"sites": []}, "no lattice sites"),
     ({"geoms": [box((0, 0, 0), [[0, 5, 0], [5, 0, 0], [0, 0, 5]])]}, "right-hand"),
+    ({"geoms": [sphere((0, 0, 0), 1.0e12)]}, "too large"),
 ])
 def test_errors(bad, msg):
     d = dict(cubic(), sites=sites(FCC), geoms=[sphere((0, 0, 0), 5.0)])
@@ -201,6 +202,13 @@ def test_conflicts_box_test():
         assert np.array_equal(keep, ~(cheb <= dmin).any(axis=1))
     # exactly dmin apart in one coordinate: a conflict (<= dmin)
     assert not A.lattice_conflicts([[0.0, 0.0, 0.0]], [[1.5, 0.0, 0.0]], 1.5)[0]
+    # all other sites in one plane (a zero-width axis) and a grid far coarser than dmin
+    qo = np.c_[rng.uniform(0, 50, (500, 2)), np.zeros(500)]
+    q = np.c_[rng.uniform(0, 50, (800, 2)), rng.uniform(-0.5, 0.5, 800)]
+    for dmin in (0.05, 0.7):
+        keep = A.lattice_conflicts(q, qo, dmin)
+        cheb = np.abs(q[:, None, :] - qo[None, :, :]).max(axis=2)
+        assert np.array_equal(keep, ~(cheb <= dmin).any(axis=1))
 
 
 def test_separate_pd_and_h_lattices_min_distance():
