@@ -10,6 +10,7 @@
 //   calculateMacroResults                                (calculateresults.cpp:8)
 //   readResults (+ writeResults, which the reference tree lacks)
 //                                                        (readresults.cpp:10)
+//   SetupLatticeVariables (the lattices of an input file) (SpaceInitializer.cpp:41)
 // The vector type V3 is the caller's (anything with operator[](int) over
 // three doubles, such as a2c's Vec3D) and the input type is anything with the
 // reference's `input.file.*` fields (T0, eps, rc, a_Pd, xLb, xUb, v, Qm,
@@ -19,6 +20,8 @@
 // throws.  No PETSc or MPI: one process drives one GPU.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <vector>
@@ -325,6 +328,124 @@ inline int writeResults(Input &input, int file_num, vector<V3> &q_Pd, vector<V3>
   detail::pack(q_Pd, q_H, sigma_Pd, sigma_H, X);
   return (int)a2c_restart_write(path, (int)q_Pd.size(), (int)q_H.size(), X.data(), x.data(), gamma.data(),
                                 full_H.data(), file_num, time);
+}
+
+// The sites of one lattice (the LatticeVariables fields the set-up fills).
+struct LatticeSites {
+  vector<double> q, q0, l;  // 3 per site
+  vector<int> siteid, matid, tag;
+  vector<double> sigma, x;
+  int64_t size() const { return (int64_t)siteid.size(); }
+};
+
+namespace detail {
+inline a2c_lattice_sites view(LatticeSites &s, int64_t n) {
+  a2c_lattice_sites v{};
+  v.capacity = v.count = n;
+  v.q = s.q.data();
+  v.q0 = s.q0.data();
+  v.l = s.l.data();
+  v.siteid = s.siteid.data();
+  v.matid = s.matid.data();
+  v.tag = s.tag.data();
+  v.sigma = s.sigma.data();
+  v.x = s.x.data();
+  return v;
+}
+inline void keep_only(LatticeSites &s, const vector<unsigned char> &keep) {
+  int64_t w = 0;
+  for (int64_t i = 0; i < s.size(); ++i) {
+    if (!keep[(size_t)i]) continue;
+    for (int k = 0; k < 3; ++k) {
+      s.q[3 * w + k] = s.q[3 * i + k];
+      s.q0[3 * w + k] = s.q0[3 * i + k];
+      s.l[3 * w + k] = s.l[3 * i + k];
+    }
+    s.siteid[w] = s.siteid[i];
+    s.matid[w] = s.matid[i];
+    s.tag[w] = s.tag[i];
+    s.sigma[w] = s.sigma[i];
+    s.x[w] = s.x[i];
+    ++w;
+  }
+  s.q.resize(3 * w);
+  s.q0.resize(3 * w);
+  s.l.resize(3 * w);
+  s.siteid.resize(w);
+  s.matid.resize(w);
+  s.tag.resize(w);
+  s.sigma.resize(w);
+  s.x.resize(w);
+}
+}  // namespace detail
+
+// SpaceInitializer::SetupLatticeVariables (SpaceInitializer.cpp:41-116) for
+// Lattice[0 .. n_lattices-1] and the RegionalInitialCondition blocks of an
+// input file: every lattice built, the regions applied in index order,
+// then the MinDistance removals in the reference's order.  errmsg (may be
+// null) receives the reader's or builder's message.
+inline int SetupLatticeVariables(const char *input_file, int n_lattices, vector<LatticeSites> &LVS,
+                                 char *errmsg = nullptr, int errlen = 0) {
+  const int kMax = 1024;
+  LVS.assign((size_t)std::max(n_lattices, 0), LatticeSites());
+  vector<double> dmin((size_t)std::max(n_lattices, 0));
+  for (int k = 0; k < n_lattices; ++k) {
+    a2c_lattice_desc d;
+    vector<a2c_site_group> sg(kMax);
+    vector<a2c_geometry> geo(kMax);
+    a2c_status s = a2c_input_lattice(input_file, k, &d, sg.data(), kMax, geo.data(), kMax, errmsg, errlen);
+    if (s) return (int)s;
+    a2c_lattice_sites cnt{};
+    if ((s = a2c_lattice_build(&d, &cnt, errmsg, errlen))) return (int)s;
+    LatticeSites &L = LVS[(size_t)k];
+    const int64_t n = cnt.count;
+    L.q.resize(3 * n);
+    L.q0.resize(3 * n);
+    L.l.resize(3 * n);
+    L.siteid.resize(n);
+    L.matid.resize(n);
+    L.tag.resize(n);
+    L.sigma.resize(n);
+    L.x.resize(n);
+    a2c_lattice_sites v = detail::view(L, n);
+    if (n > 0 && (s = a2c_lattice_build(&d, &v, errmsg, errlen))) return (int)s;
+    double m = d.dmin;
+    if (m <= 0.0) {  // LatticeStructure.cpp:56-58: the shortest lattice vector
+      m = -1.0;
+      for (int i = 0; i < 3; ++i) {
+        const double *a = d.abc + 3 * i;
+        const double len = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        m = (m < 0.0 || len < m) ? len : m;
+      }
+    }
+    dmin[(size_t)k] = m;
+  }
+  vector<a2c_region> reg(kMax);
+  vector<a2c_geometry> rgeo(kMax);
+  int nreg = 0;
+  a2c_status s = a2c_input_regions(input_file, reg.data(), kMax, rgeo.data(), kMax, &nreg, errmsg, errlen);
+  if (s) return (int)s;
+  for (int r = 0; r < nreg; ++r) {
+    if (reg[(size_t)r].lattice_id >= n_lattices) return (int)A2C_ERR_INVALID;
+    for (int k = 0; k < n_lattices; ++k) {
+      if (reg[(size_t)r].lattice_id >= 0 && reg[(size_t)r].lattice_id != k) continue;
+      a2c_lattice_sites v = detail::view(LVS[(size_t)k], LVS[(size_t)k].size());
+      if ((s = a2c_lattice_apply_region(&reg[(size_t)r], &v, errmsg, errlen))) return (int)s;
+    }
+  }
+  for (int i = 0; i < n_lattices; ++i)
+    for (int j = 0; j < n_lattices; ++j) {
+      if (j == i || (j < i && dmin[(size_t)j] <= dmin[(size_t)i])) continue;  // already resolved
+      LatticeSites &A = LVS[(size_t)i];
+      const LatticeSites &B = LVS[(size_t)j];
+      vector<unsigned char> keep((size_t)std::max<int64_t>(A.size(), 1));
+      int64_t removed = 0;
+      if ((s = a2c_lattice_conflicts(A.q.data(), A.size(), B.q.data(), B.size(), dmin[(size_t)i], keep.data(),
+                                     &removed)))
+        return (int)s;
+      if (removed) detail::keep_only(A, keep);
+    }
+  return 0;
 }
 
 }  // namespace a2c_gb300
