@@ -650,10 +650,11 @@ def build_lattices(descs: list, regions: list | None = None) -> list:
 
 
 def snapshot_desc(prefix: str, *, fmt: str = "both", precision: int = 2, box=(0.0, 0.0, 0.0), origin=(0.0, 0.0, 0.0),
-                  periodic=(0, 0, 0)):
+                  periodic=(0, 0, 0), lattice_id: int = 0):
     """Descriptor of a snapshot series (a2c_snapshot_desc): files
-    <prefix>_L0_<frame>.vtp / .xyz and <prefix>_L0.pvd."""
+    <prefix>_L<lattice_id>_<frame>.vtp / .xyz and <prefix>_L<lattice_id>.pvd."""
     d = N.SnapshotDesc()
+    d.lattice_id = int(lattice_id)
     d._prefix = str(prefix).encode()  # keeps the bytes alive with the descriptor
     d.prefix = d._prefix
     d.format = {"vtp": 1, "xyz": 2, "both": 3}[fmt]

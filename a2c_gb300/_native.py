@@ -70,7 +70,7 @@ class LatticeSpec(C.Structure):
 
 class SnapshotDesc(C.Structure):
     _fields_ = [("prefix", C.c_char_p), ("format", C.c_int), ("precision", C.c_int), ("axes", C.c_double * 9),
-                ("origin", C.c_double * 3), ("periodic", C.c_int * 3)]
+                ("origin", C.c_double * 3), ("periodic", C.c_int * 3), ("lattice_id", C.c_int)]
 
 
 class Input(C.Structure):

@@ -13,19 +13,23 @@
 
 namespace {
 
-// "%s_L0_%04d" -- the reference pads the frame number to four digits by an
+// "%s_L%d_%04d" -- the reference pads the frame number to four digits by an
 // if-chain and prints it plainly from 1000 on, which is what %04d does too
-std::string frame_name(const char *base, int frame, const char *ext) {
+std::string frame_name(const char *base, int lattice, int frame, const char *ext) {
   char buf[64];
-  std::snprintf(buf, sizeof(buf), "_L0_%04d.%s", frame, ext);
+  std::snprintf(buf, sizeof(buf), "_L%d_%04d.%s", lattice, frame, ext);
   return std::string(base) + buf;
+}
+
+std::string collection_name(const a2c_snapshot_desc *d) {
+  return std::string(d->prefix) + "_L" + std::to_string(d->lattice_id) + ".pvd";
 }
 
 const char *fmt1(int precision) { return precision == 2 ? "%16.10e" : precision == 1 ? "%10.6e" : "%7.4e"; }
 
 bool valid(const a2c_snapshot_desc *d) {
   return d && d->prefix && d->prefix[0] && (d->format >= 1 && d->format <= 3) && d->precision >= 0 &&
-         d->precision <= 2;
+         d->precision <= 2 && d->lattice_id >= 0;
 }
 
 const char *basename_of(const char *path) {
@@ -40,7 +44,7 @@ extern "C" {
 a2c_status a2c_snapshot_begin(const a2c_snapshot_desc *d) {
   if (!valid(d)) return A2C_ERR_INVALID;
   if (!(d->format & 1)) return A2C_OK;  // no VTP, no collection file
-  const std::string f = std::string(d->prefix) + "_L0.pvd";
+  const std::string f = collection_name(d);
   FILE *p = std::fopen(f.c_str(), "w");
   if (!p) return A2C_ERR_INVALID;
   std::fprintf(p, "<?xml version=\"1.0\"?>\n");
@@ -67,7 +71,7 @@ a2c_status a2c_snapshot_write(const a2c_snapshot_desc *d, int frame, double time
   const char *f = fmt1(d->precision);
   std::string sep = d->precision == 2 ? "  " : " ";
   if (d->format & 1) {
-    const std::string full = frame_name(d->prefix, frame, "vtp");
+    const std::string full = frame_name(d->prefix, d->lattice_id, frame, "vtp");
     FILE *v = std::fopen(full.c_str(), "w");
     if (!v) return A2C_ERR_INVALID;
     std::fprintf(v, "<?xml version=\"1.0\"?>\n");
@@ -112,7 +116,7 @@ a2c_status a2c_snapshot_write(const a2c_snapshot_desc *d, int frame, double time
     std::fclose(v);
     if (!ok) return A2C_ERR_INVALID;
     // one more entry in the collection: overwrite its closing 27 bytes
-    const std::string pf = std::string(d->prefix) + "_L0.pvd";
+    const std::string pf = collection_name(d);
     FILE *p = std::fopen(pf.c_str(), "r+");
     if (!p) return A2C_ERR_STATE;  // a2c_snapshot_begin first
     std::fseek(p, -27, SEEK_END);
@@ -124,7 +128,7 @@ a2c_status a2c_snapshot_write(const a2c_snapshot_desc *d, int frame, double time
     if (!okp) return A2C_ERR_INVALID;
   }
   if (d->format & 2) {
-    const std::string full = frame_name(d->prefix, frame, "xyz");
+    const std::string full = frame_name(d->prefix, d->lattice_id, frame, "xyz");
     FILE *x = std::fopen(full.c_str(), "w");
     if (!x) return A2C_ERR_INVALID;
     std::fprintf(x, "%ld\n", np);

@@ -373,10 +373,10 @@ a2c_status a2c_gpp_batch_autotune(a2c_gpp_batch *batch, const double *X, int rep
 
 /* Solution snapshots in the formats of the reference's Output class
  * (Output.cpp:60-90, 133-480): per frame a VTK PolyData file
- * <prefix>_L0_<frame>.vtp (points q; SiteID, MaterialID, Tag,
+ * <prefix>_L<k>_<frame>.vtp (points q; SiteID, MaterialID, Tag,
  * AtomicFrequency = sigma, MolarFraction = occupancy, ChemicalPotential =
- * gamma) with an entry in the collection <prefix>_L0.pvd, and/or an
- * extended-XYZ file <prefix>_L0_<frame>.xyz (species, q, q - q0, site id,
+ * gamma) with an entry in the collection <prefix>_L<k>.pvd, and/or an
+ * extended-XYZ file <prefix>_L<k>_<frame>.xyz (species, q, q - q0, site id,
  * sigma, tag, occupancy, gamma).  One lattice, one species column pair:
  * Pd sites carry occupancy 1 and gamma 0. */
 typedef struct a2c_snapshot_desc {
@@ -386,6 +386,7 @@ typedef struct a2c_snapshot_desc {
   double axes[9];       /* lattice axes a, b, c for the XYZ header */
   double origin[3];
   int periodic[3];
+  int lattice_id;       /* the k of _L<k> in the file names (Output.cpp:74, 143); 0 for the evaluator's lattice */
 } a2c_snapshot_desc;
 /* the collection header (Output's constructor); call once before the frames */
 a2c_status a2c_snapshot_begin(const a2c_snapshot_desc *desc);

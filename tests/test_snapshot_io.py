@@ -78,3 +78,22 @@ def test_frame_names_and_errors(tmp_path):
     dx = A.snapshot_desc(str(tmp_path / "b"), fmt="xyz", precision=0)
     A.snapshot_write(dx, 3, 0.0, 8, 8, X, xH)  # XYZ needs no collection
     assert (tmp_path / "b_L0_0003.xyz").exists() and not (tmp_path / "b_L0.pvd").exists()
+
+
+def test_lattice_id_in_names(tmp_path):
+    """Output.cpp names every file by its lattice (_L<k>): two lattices of
+    one run keep separate collections."""
+    X, xH, gam, _ = state()
+    for k, (nPd, nH) in enumerate(((8, 0), (0, 8))):
+        d = A.snapshot_desc(str(tmp_path / "sol"), lattice_id=k)
+        A.snapshot_begin(d)
+        Xk = X[: 4 * 8] if nPd else X[4 * 8:]
+        A.snapshot_write(d, 5, 0.25, nPd, nH, Xk, xH if nH else xH[:0])
+    for k in (0, 1):
+        assert (tmp_path / f"sol_L{k}_0005.vtp").exists() and (tmp_path / f"sol_L{k}_0005.xyz").exists()
+        coll = open(tmp_path / f"sol_L{k}.pvd").read()
+        assert f'file="sol_L{k}_0005.vtp"' in coll
+    rows = open(tmp_path / "sol_L1_0005.xyz").read().splitlines()[2:]
+    assert all(r.split()[0] == "H" for r in rows) and len(rows) == 8
+    with pytest.raises(A.A2CError):
+        A.snapshot_begin(A.snapshot_desc(str(tmp_path / "bad"), lattice_id=-1))
