@@ -688,6 +688,24 @@ def snapshot_write(desc, frame: int, time: float, nPd: int, nH: int, X, xH, X0=N
                                        N.ptr(tag) if tag is not None else None), "a2c_snapshot_write")
 
 
+def snapshot_write_lattice(desc, frame: int, time: float, sites: dict, gamma=None, material_names=None) -> None:
+    """Snapshot of a set-up lattice (build_lattice's arrays) with its own
+    site groups, materials, tags, widths and occupancies
+    (a2c_snapshot_write_lattice); material_names label the XYZ species."""
+    n = len(sites["q"])
+    arr = {k: np.ascontiguousarray(sites[k]) for k in LATTICE_SITE_FIELDS}
+    ls = N.LatticeSites()
+    ls.capacity = ls.count = n
+    for name in LATTICE_SITE_FIELDS:
+        setattr(ls, name, arr[name].ctypes.data)
+    g = None if gamma is None else np.ascontiguousarray(gamma, dtype=np.float64)
+    names = list(material_names or [])
+    cn = (C.c_char_p * max(len(names), 1))(*[str(m).encode() for m in names])
+    N.check(N.lib().a2c_snapshot_write_lattice(C.byref(desc), int(frame), float(time), C.byref(ls),
+                                               N.ptr(g) if g is not None else None, cn, len(names)),
+            "a2c_snapshot_write_lattice")
+
+
 def restart_write(path: str, nPd: int, nH: int, X, xH, gamma, full_H, step: int = 0, time: float = 0.0) -> None:
     """Restart file in the format the reference's readResults reads."""
     N.check(N.lib().a2c_restart_write(str(path).encode(), nPd, nH, N.ptr(_f64(X, 4 * (nPd + nH))),

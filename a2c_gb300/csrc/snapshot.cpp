@@ -4,6 +4,7 @@
 // displacement q - q0, site id, material id, tag, atomic frequency (the
 // Gaussian width sigma), one species column pair (molar fraction = the
 // occupancy, 1 for Pd; chemical potential = gamma, 0 for Pd).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -58,16 +59,52 @@ a2c_status a2c_snapshot_begin(const a2c_snapshot_desc *d) {
   return ok ? A2C_OK : A2C_ERR_INVALID;
 }
 
-a2c_status a2c_snapshot_write(const a2c_snapshot_desc *d, int frame, double time, int nPd, int nH, const double *X,
-                              const double *X0, const double *xH, const double *gamma, const signed char *siteid,
-                              const signed char *tag) {
-  if (!valid(d) || frame < 0 || nPd < 0 || nH < 0 || (nPd + nH > 0 && !X) || (nH > 0 && !xH)) return A2C_ERR_INVALID;
-  const long np = (long)nPd + nH;
-  auto q0 = [&](long i, int k) { return X0 ? X0[4 * i + k] : X[4 * i + k]; };
-  auto sid = [&](long i) { return siteid ? (int)siteid[i] : (i < nPd ? 0 : 1); };
-  auto tg = [&](long i) { return tag ? (int)tag[i] : 0; };
-  auto xv = [&](long i) { return i < nPd ? 1.0 : xH[i - nPd]; };
-  auto gv = [&](long i) { return (i < nPd || !gamma) ? 0.0 : gamma[i - nPd]; };
+}  // extern "C"
+
+namespace {
+
+// The sites of the evaluator's layout: X (4 per site, Pd sites then H
+// sites), occupancy and gamma on the H sites, material 0 "Pd" / 1 "H".
+struct EvalSites {
+  const double *X, *X0, *xH, *gamma;
+  const signed char *siteid, *tag;
+  long nPd;
+  double pos(long i, int k) const { return X[4 * i + k]; }
+  double ref(long i, int k) const { return X0 ? X0[4 * i + k] : X[4 * i + k]; }
+  int sid(long i) const { return siteid ? (int)siteid[i] : (i < nPd ? 0 : 1); }
+  int mid(long i) const { return i < nPd ? 0 : 1; }
+  const char *name(long i) const { return i < nPd ? "Pd" : "H"; }
+  int tag_of(long i) const { return tag ? (int)tag[i] : 0; }
+  double sigma(long i) const { return X[4 * i + 3]; }
+  double x(long i) const { return i < nPd ? 1.0 : xH[i - nPd]; }
+  double g(long i) const { return (i < nPd || !gamma) ? 0.0 : gamma[i - nPd]; }
+};
+
+// The sites of a set-up lattice (a2c_lattice_sites' fields), named by
+// their material (the names given, else M<id>).
+struct LatticeSitesView {
+  const a2c_lattice_sites *s;
+  const double *gamma;
+  const char *const *names;
+  int nnames;
+  std::vector<std::string> fallback;
+  double pos(long i, int k) const { return s->q[3 * i + k]; }
+  double ref(long i, int k) const { return s->q0[3 * i + k]; }
+  int sid(long i) const { return s->siteid[i]; }
+  int mid(long i) const { return s->matid[i]; }
+  const char *name(long i) const {
+    const int m = s->matid[i];
+    if (names && m >= 0 && m < nnames && names[m]) return names[m];
+    return (m >= 0 && m < (int)fallback.size()) ? fallback[(size_t)m].c_str() : "M";
+  }
+  int tag_of(long i) const { return s->tag[i]; }
+  double sigma(long i) const { return s->sigma[i]; }
+  double x(long i) const { return s->x[i]; }
+  double g(long i) const { return gamma ? gamma[i] : 0.0; }
+};
+
+template <class S>
+a2c_status write_frame(const a2c_snapshot_desc *d, int frame, double time, long np, const S &a) {
   const char *f = fmt1(d->precision);
   std::string sep = d->precision == 2 ? "  " : " ";
   if (d->format & 1) {
@@ -82,7 +119,7 @@ a2c_status a2c_snapshot_write(const a2c_snapshot_desc *d, int frame, double time
     std::fprintf(v, "      <Points>\n");
     std::fprintf(v, "        <DataArray type=\"Float32\" NumberOfComponents=\"3\" format=\"ascii\">\n");
     const std::string line = std::string("          ") + f + " " + f + " " + f + "\n";
-    for (long i = 0; i < np; ++i) std::fprintf(v, line.c_str(), X[4 * i], X[4 * i + 1], X[4 * i + 2]);
+    for (long i = 0; i < np; ++i) std::fprintf(v, line.c_str(), a.pos(i, 0), a.pos(i, 1), a.pos(i, 2));
     std::fprintf(v, "        </DataArray>\n");
     std::fprintf(v, "      </Points>\n");
     std::fprintf(v, "      <PointData Scalars=\"ScalarResults\" Vectors=\"VectorResults\">\n");
@@ -102,12 +139,12 @@ a2c_status a2c_snapshot_write(const a2c_snapshot_desc *d, int frame, double time
       std::fprintf(v, "\n");
       std::fprintf(v, "        </DataArray>\n");
     };
-    int_array("SiteID", sid);
-    int_array("MaterialID", [&](long i) { return i < nPd ? 0 : 1; });
-    int_array("Tag", tg);
-    real_array("AtomicFrequency", [&](long i) { return X[4 * i + 3]; });
-    real_array("MolarFraction", xv);
-    real_array("ChemicalPotential", gv);
+    int_array("SiteID", [&](long i) { return a.sid(i); });
+    int_array("MaterialID", [&](long i) { return a.mid(i); });
+    int_array("Tag", [&](long i) { return a.tag_of(i); });
+    real_array("AtomicFrequency", [&](long i) { return a.sigma(i); });
+    real_array("MolarFraction", [&](long i) { return a.x(i); });
+    real_array("ChemicalPotential", [&](long i) { return a.g(i); });
     std::fprintf(v, "      </PointData>\n");
     std::fprintf(v, "    </Piece>\n");
     std::fprintf(v, "  </PolyData>\n");
@@ -146,12 +183,12 @@ a2c_status a2c_snapshot_write(const a2c_snapshot_desc *d, int frame, double time
     const std::string head = d->precision == 2 ? "%16s  " : "%16s ";
     const std::string mid = d->precision == 2 ? std::string("%4d  ") + f + "  %4d  " : std::string("%4d ") + f + " %4d ";
     for (long i = 0; i < np; ++i) {
-      std::fprintf(x, head.c_str(), i < nPd ? "Pd" : "H");
-      std::fprintf(x, r3.c_str(), X[4 * i], X[4 * i + 1], X[4 * i + 2]);
-      std::fprintf(x, r3.c_str(), X[4 * i] - q0(i, 0), X[4 * i + 1] - q0(i, 1), X[4 * i + 2] - q0(i, 2));
-      std::fprintf(x, mid.c_str(), sid(i), X[4 * i + 3], tg(i));
-      std::fprintf(x, r.c_str(), xv(i));
-      std::fprintf(x, r.c_str(), gv(i));
+      std::fprintf(x, head.c_str(), a.name(i));
+      std::fprintf(x, r3.c_str(), a.pos(i, 0), a.pos(i, 1), a.pos(i, 2));
+      std::fprintf(x, r3.c_str(), a.pos(i, 0) - a.ref(i, 0), a.pos(i, 1) - a.ref(i, 1), a.pos(i, 2) - a.ref(i, 2));
+      std::fprintf(x, mid.c_str(), a.sid(i), a.sigma(i), a.tag_of(i));
+      std::fprintf(x, r.c_str(), a.x(i));
+      std::fprintf(x, r.c_str(), a.g(i));
       std::fprintf(x, "\n");
     }
     const bool ok = std::ferror(x) == 0;
@@ -159,6 +196,32 @@ a2c_status a2c_snapshot_write(const a2c_snapshot_desc *d, int frame, double time
     if (!ok) return A2C_ERR_INVALID;
   }
   return A2C_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+a2c_status a2c_snapshot_write(const a2c_snapshot_desc *d, int frame, double time, int nPd, int nH, const double *X,
+                              const double *X0, const double *xH, const double *gamma, const signed char *siteid,
+                              const signed char *tag) {
+  if (!valid(d) || frame < 0 || nPd < 0 || nH < 0 || (nPd + nH > 0 && !X) || (nH > 0 && !xH)) return A2C_ERR_INVALID;
+  const EvalSites a{X, X0, xH, gamma, siteid, tag, (long)nPd};
+  return write_frame(d, frame, time, (long)nPd + nH, a);
+}
+
+a2c_status a2c_snapshot_write_lattice(const a2c_snapshot_desc *d, int frame, double time,
+                                      const a2c_lattice_sites *sites, const double *gamma,
+                                      const char *const *material_names, int n_materials) {
+  if (!valid(d) || frame < 0 || !sites || sites->count < 0 || n_materials < 0 ||
+      (sites->count > 0 && (!sites->q || !sites->q0 || !sites->siteid || !sites->matid || !sites->tag ||
+                            !sites->sigma || !sites->x)))
+    return A2C_ERR_INVALID;
+  LatticeSitesView a{sites, gamma, material_names, n_materials, {}};
+  int maxm = -1;
+  for (int64_t i = 0; i < sites->count; ++i) maxm = std::max(maxm, sites->matid[i]);
+  for (int m = 0; m <= maxm; ++m) a.fallback.push_back("M" + std::to_string(m));
+  return write_frame(d, frame, time, (long)sites->count, a);
 }
 
 }  // extern "C"

@@ -512,6 +512,14 @@ typedef struct a2c_lattice_sites {
   double *sigma, *x;
 } a2c_lattice_sites;
 a2c_status a2c_lattice_build(const a2c_lattice_desc *desc, a2c_lattice_sites *out, char *errmsg, int errlen);
+/* Snapshot of a set-up lattice's sites (a2c_lattice_sites with count
+ * sites): the files of a2c_snapshot_write with each site's own site group,
+ * material id, tag, width and occupancy, and in the XYZ species column its
+ * material's name (material_names[matid], else "M<matid>"), as Output.cpp
+ * writes a lattice (:133-480).  gamma (count, may be NULL: 0). */
+a2c_status a2c_snapshot_write_lattice(const a2c_snapshot_desc *desc, int frame, double time,
+                                      const a2c_lattice_sites *sites, const double *gamma,
+                                      const char *const *material_names, int n_materials);
 /* SetupLatticeVariables' removal of sites closer than dmin to another
  * lattice's sites (SpaceInitializer.cpp:94-112, LatticeVariables.cpp:78-140):
  * keep[i] = 0 for every site i of q (n sites) with a site of q_other

@@ -97,3 +97,32 @@ def test_lattice_id_in_names(tmp_path):
     assert all(r.split()[0] == "H" for r in rows) and len(rows) == 8
     with pytest.raises(A.A2CError):
         A.snapshot_begin(A.snapshot_desc(str(tmp_path / "bad"), lattice_id=-1))
+
+
+def test_lattice_sites_writer_matches_evaluator_layout(tmp_path):
+    """A set-up lattice written with its own fields gives the evaluator
+    writer's bytes when it describes the same sites (material 0 "Pd" with
+    occupancy 1, material 1 "H")."""
+    X, xH, gam, X0 = state()
+    nPd, nH = 8, 8
+    n = nPd + nH
+    sid = (np.arange(n) % 4).astype(np.int8)
+    tag = (np.arange(n) % 3).astype(np.int8)
+    sites = {"q": X.reshape(-1, 4)[:, :3].copy(), "q0": X0.reshape(-1, 4)[:, :3].copy(),
+             "l": np.zeros((n, 3)), "siteid": sid.astype(np.int32), "matid": np.r_[np.zeros(nPd), np.ones(nH)].astype(np.int32),
+             "tag": tag.astype(np.int32), "sigma": X.reshape(-1, 4)[:, 3].copy(), "x": np.r_[np.ones(nPd), xH]}
+    g_all = np.r_[np.zeros(nPd), gam]
+    for prec in (0, 1, 2):
+        a = A.snapshot_desc(str(tmp_path / f"a{prec}"), precision=prec, box=(10.0, 11.0, 12.0))
+        b = A.snapshot_desc(str(tmp_path / f"b{prec}"), precision=prec, box=(10.0, 11.0, 12.0))
+        A.snapshot_begin(a)
+        A.snapshot_begin(b)
+        A.snapshot_write(a, 2, 0.5, nPd, nH, X, xH, X0=X0, gamma=gam, siteid=sid, tag=tag)
+        A.snapshot_write_lattice(b, 2, 0.5, sites, gamma=g_all, material_names=["Pd", "H"])
+        for ext in ("_L0_0002.vtp", "_L0_0002.xyz"):
+            assert open(tmp_path / f"a{prec}{ext}").read() == open(tmp_path / f"b{prec}{ext}").read()
+    # unnamed materials are labelled M<id>
+    c = A.snapshot_desc(str(tmp_path / "c"), fmt="xyz")
+    A.snapshot_write_lattice(c, 0, 0.0, sites)
+    rows = open(tmp_path / "c_L0_0000.xyz").read().splitlines()[2:]
+    assert [r.split()[0] for r in rows] == ["M0"] * nPd + ["M1"] * nH
