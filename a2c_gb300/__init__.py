@@ -578,6 +578,19 @@ def regions_from_input(path: str, max_regions: int = 64, max_geoms: int = 256) -
     return out
 
 
+def material_names_from_input(path: str, max_materials: int = 64) -> list:
+    """Material[m].MaterialName of an input file (a2c_input_material_names)."""
+    L = 256
+    buf = C.create_string_buffer(max_materials * L)
+    n = C.c_int(0)
+    msg = C.create_string_buffer(256)
+    st = N.lib().a2c_input_material_names(str(path).encode(), buf, max_materials, L, C.byref(n), msg, 256)
+    if st != N.A2C_OK:
+        raise A2CError(st, "a2c_input_material_names: " + msg.value.decode())
+    raw = buf.raw
+    return [raw[k * L:(k + 1) * L].split(b"\0", 1)[0].decode() for k in range(n.value)]
+
+
 def apply_region(sites: dict, region: dict) -> dict:
     """A regional initial condition (a2c_lattice_apply_region) applied to a
     copy of build_lattice's arrays."""

@@ -166,6 +166,7 @@ def lib() -> C.CDLL:
                                            C.POINTER(C.c_char_p), I]),
         "a2c_input_regions": (I, [C.c_char_p, C.POINTER(Region), I, C.POINTER(Geometry), I, C.POINTER(C.c_int),
                                   C.c_char_p, I]),
+        "a2c_input_material_names": (I, [C.c_char_p, P, I, I, C.POINTER(C.c_int), C.c_char_p, I]),
         "a2c_snapshot_write": (I, [C.POINTER(SnapshotDesc), I, D, I, I, P, P, P, P, P, P]),
         "a2c_gpp_snapshot_async": (I, [P, C.POINTER(SnapshotDesc), I, D, P, P, P, P]),
         "a2c_gpp_snapshot_wait": (I, [P]),
@@ -224,7 +225,7 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_get_occupancy", "a2c_gpp_set_state", "a2c_gpp_get_state", "a2c_gpp_build_neighbors",
             "a2c_gpp_neighbor_total", "a2c_gpp_set_neighbor_skin", "a2c_gpp_update_neighbors", "a2c_snapshot_begin", "a2c_input_read", "a2c_input_apply",
             "a2c_input_lattice", "a2c_lattice_build", "a2c_lattice_conflicts", "a2c_lattice_apply_region",
-            "a2c_input_regions", "a2c_snapshot_write_lattice",
+            "a2c_input_regions", "a2c_snapshot_write_lattice", "a2c_input_material_names",
             "a2c_snapshot_write", "a2c_gpp_snapshot_async", "a2c_gpp_snapshot_wait", "a2c_gpp_get_neighbors", "a2c_gpp_get_shell_counts", "a2c_gpp_eval",
             "a2c_gpp_eval_device", "a2c_gpp_profile_eval", "a2c_gpp_get_density", "a2c_gpp_eam_eval", "a2c_gpp_bounds", "a2c_gpp_minimize",
             "a2c_gpp_chem_potential", "a2c_gpp_minimize_stats", "a2c_gpp_apply_dirichlet", "a2c_gpp_diffuse", "a2c_gpp_macro_results",

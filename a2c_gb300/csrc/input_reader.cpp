@@ -596,6 +596,41 @@ extern "C" a2c_status a2c_input_lattice(const char *path, int lattice_id, a2c_la
   return A2C_OK;
 }
 
+// Material[m].MaterialName (MaterialData, IoData.cpp:538-560).
+extern "C" a2c_status a2c_input_material_names(const char *path, char *names, int max_materials, int name_len,
+                                               int *n_materials, char *errmsg, int errlen) {
+  if (!path || !n_materials || max_materials < 0 || name_len < 1 || (max_materials > 0 && !names))
+    return A2C_ERR_INVALID;
+  auto err = [&](const std::string &msg) {
+    if (errmsg && errlen > 0) std::snprintf(errmsg, (size_t)errlen, "%s", msg.c_str());
+    return A2C_ERR_INVALID;
+  };
+  std::ifstream f(path);
+  if (!f) return err(std::string("cannot open ") + path);
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string src = ss.str();  // the lexer reads it in place
+  try {
+    Parser p(src);
+    p.file();
+    const auto &m = p.values;
+    const std::vector<int> ids = block_ids(m, "", "Material");
+    int n = 0;
+    for (int k : ids) n = std::max(n, k + 1);
+    if (n > max_materials) throw Error{"more materials than the array holds"};
+    for (int k = 0; k < n; ++k) {
+      char *out = names + (size_t)k * (size_t)name_len;
+      out[0] = 0;
+      get_str(m, ("Material[" + std::to_string(k) + "].MaterialName").c_str(), out, (size_t)name_len);
+    }
+    *n_materials = n;
+  } catch (const Error &e) {
+    return err(e.msg);
+  }
+  if (errmsg && errlen > 0) errmsg[0] = 0;
+  return A2C_OK;
+}
+
 // RegionalInitialCondition[k] blocks (RegionalIcData, IoData.cpp:578-624).
 extern "C" a2c_status a2c_input_regions(const char *path, a2c_region *regions, int max_regions,
                                         a2c_geometry *geoms, int max_geoms, int *n_regions, char *errmsg,

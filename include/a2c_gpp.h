@@ -552,6 +552,11 @@ a2c_status a2c_lattice_apply_region(const a2c_region *region, a2c_lattice_sites 
  * (max_geoms in all); *n_regions receives n. */
 a2c_status a2c_input_regions(const char *path, a2c_region *regions, int max_regions, a2c_geometry *geoms,
                              int max_geoms, int *n_regions, char *errmsg, int errlen);
+/* Material[0 .. n-1].MaterialName of an input file (IoData.cpp:538-560;
+ * default ""): names[m] receives up to name_len bytes each (names holds
+ * max_materials * name_len); *n_materials receives n. */
+a2c_status a2c_input_material_names(const char *path, char *names, int max_materials, int name_len,
+                                    int *n_materials, char *errmsg, int errlen);
 /* Lattice[id] of an input file as a description: sites (capacity
  * max_sites) and geometries (max_geoms) are filled from the file's
  * Site[k] and Plane/Sphere/Parallelepiped/Spheroid/CylinderAndCone/

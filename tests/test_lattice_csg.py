@@ -348,3 +348,25 @@ def test_regions_from_input(tmp_path):
         ref = O.ref_apply_region(O.ref_apply_region(base, r0), r1)
         for k in A.LATTICE_SITE_FIELDS:
             assert np.array_equal(lat[k], ref[k]), k
+
+
+def test_material_names_and_lattice_snapshot(tmp_path):
+    f = tmp_path / "input.st"
+    f.write_text(textwrap.dedent("""
+        under Material[0] { MaterialName = "Pd"; }
+        under Material[1] { MaterialName = "PdH"; }
+        under Lattice[0] {
+          OAx = 3.89; OBy = 3.89; OCz = 3.89;
+          under Site[0] { La = 0.0; Lb = 0.0; Lc = 0.0; MaterialID = 0; AtomicFrequency = 0.1; }
+          under Site[1] { La = 0.5; Lb = 0.5; Lc = 0.5; MaterialID = 1; AtomicFrequency = 0.1; }
+          under Sphere[0] { Center_x = 4.0; Center_y = 4.0; Center_z = 4.0; Radius = 4.5;
+                            Side = Interior; Inclusion = Intersection; OperationOrder = 0; }
+        }
+    """))
+    names = A.material_names_from_input(str(f))
+    assert names == ["Pd", "PdH"]
+    lat = A.build_lattice(A.lattice_from_input(str(f), 0))
+    d = A.snapshot_desc(str(tmp_path / "sol"), fmt="xyz", lattice_id=0)
+    A.snapshot_write_lattice(d, 1, 0.0, lat, material_names=names)
+    rows = open(tmp_path / "sol_L0_0001.xyz").read().splitlines()[2:]
+    assert [r.split()[0] for r in rows] == [names[m] for m in lat["matid"]]
