@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <thread>
@@ -23,6 +24,31 @@ a2c_status cuda_status(cudaError_t e) {
     case cudaErrorInvalidDevice: return A2C_ERR_NO_DEVICE;
     default: return A2C_ERR_CUDA;
   }
+}
+
+int device_sms(int dev) {
+  static std::mutex m;
+  static int cache[kMaxDevices] = {};
+  if (dev < 0 || dev >= kMaxDevices) return 1;
+  std::lock_guard<std::mutex> lock(m);
+  if (!cache[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+      (void)cudaGetLastError();
+      return 1;  // not cached: asked again next time
+    }
+    cache[dev] = n;
+  }
+  return cache[dev];
+}
+
+int current_device_sms() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 1;
+  }
+  return device_sms(dev);
 }
 
 a2c_status eval_device_impl(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev) {

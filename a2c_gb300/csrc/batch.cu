@@ -765,15 +765,10 @@ BatchView view(a2c_gpp_batch *b, int which) {
   return v;
 }
 
+// The chunk kernels stride over chunks; each chunk's sum has a fixed
+// order, so results do not depend on this grid.
 int chunk_grid(int64_t nchunks) {
-  static int sms = 0;  // queried once, before any capture (the eager first tick)
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms < 1) sms = 1;
-  }
-  return (int)std::max<int64_t>(1, std::min<int64_t>(nchunks, 8 * (int64_t)sms));
+  return (int)std::max<int64_t>(1, std::min<int64_t>(nchunks, 8 * (int64_t)current_device_sms()));
 }
 
 a2c_status plan(a2c_gpp_batch *b, const Dev &D) {
@@ -784,7 +779,9 @@ a2c_status plan(a2c_gpp_batch *b, const Dev &D) {
   return A2C_OK;
 }
 
-int default_tps(a2c_gpp_batch *b) { return b->tps ? b->tps : (b->c->N < 152 * 2048 ? 4 : 1); }
+int default_tps(a2c_gpp_batch *b) {
+  return b->tps ? b->tps : default_threads_per_site(b->c->N, device_sms(b->c->device));
+}
 
 // Evaluation of every listed site at xn into gn (both forms; a form with
 // an empty list costs an empty launch).

@@ -120,6 +120,15 @@ a2c_status cuda_status(cudaError_t e);
 
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// Streaming multiprocessors of a device, queried once per device (api.cu).
+constexpr int kMaxDevices = 64;
+int device_sms(int dev);
+int current_device_sms();
+// Threads per site of the mixed pair kernels when none was chosen: a
+// system with fewer than 2048 sites per SM spreads each site over 4 lanes
+// so that every SM gets work; a larger one runs one lane per site.
+inline int default_threads_per_site(int64_t n_sites, int sms) { return n_sites < (int64_t)sms * 2048 ? 4 : 1; }
+
 // k_fp64.cu
 a2c_status launch_density64(a2c_gpp_ctx *c, const double *dX);
 a2c_status launch_gradient64(a2c_gpp_ctx *c, const double *dX, double *dG);

@@ -12,8 +12,10 @@
 // subtracting an exact zero leaves a value unchanged, so the component-wise
 // forms used below are bit-identical to it.
 #include <algorithm>
+#include <mutex>
 
 #include "eam64.cuh"
+
 #include "internal.cuh"
 
 namespace a2c {
@@ -392,7 +394,7 @@ SiteArgs site_args(a2c_gpp_ctx *c, const double *dX) {
 // pipe: a small system finishes sooner when its warps are spread over as
 // many SMs as possible (one-warp blocks); a large one fills the device
 // either way.  Results do not depend on the block size.
-unsigned block64(int64_t n) { return n < (int64_t)152 * kBlock * 4 ? 32u : (unsigned)kBlock; }
+unsigned block64(int64_t n) { return n < (int64_t)current_device_sms() * kBlock * 4 ? 32u : (unsigned)kBlock; }
 
 a2c_status launch_density64(a2c_gpp_ctx *c, const double *dX) {
   if (c->N == 0) return A2C_OK;
@@ -417,15 +419,26 @@ a2c_status launch_gradient64(a2c_gpp_ctx *c, const double *dX, double *dG) {
 // device, and a short list must still spread over all SMs.
 a2c_status launch_eval64_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv) {
   constexpr int kLB = 32;
-  static int cap[2] = {0, 0};
-  if (!cap[0]) {
-    int dev = 0, sms = 0, b0 = 0, b1 = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_density64_list, kLB, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_gradient64_list, kLB, 0);
-    cap[0] = std::max(1, sms * b0);
-    cap[1] = std::max(1, sms * b1);
+  // persistent grid sizes per device, computed once under a lock
+  static std::mutex m;
+  static int caps[kMaxDevices][2] = {};
+  int cap[2];
+  {
+    const int dev = (c->device >= 0 && c->device < kMaxDevices) ? c->device : 0;
+    std::lock_guard<std::mutex> lock(m);
+    if (!caps[dev][0]) {
+      const int sms = device_sms(c->device);
+      int b0 = 0, b1 = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_density64_list, kLB, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_gradient64_list, kLB, 0);
+      (void)cudaGetLastError();
+      if (b0 > 0 && b1 > 0) {
+        caps[dev][0] = sms * b0;
+        caps[dev][1] = sms * b1;
+      }
+    }
+    cap[0] = std::max(1, caps[dev][0]);
+    cap[1] = std::max(1, caps[dev][1]);
   }
   if (c->N == 0) return A2C_OK;
   SiteArgs a = site_args(c, dX);

@@ -783,12 +783,24 @@ const ExpTerms &exp_consts() {
 // a.rev, a.npre, a.recv set), else from both sides (k_grad_mixed).
 constexpr int kRecvTps = 8;  // lanes per site summing the received shares
 template <int TPS, bool LIST>
-void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, bool once = false) {
-  static int cap[4] = {0, 0, 0, 0};
-  if (!cap[0]) {
-    int dev = 0, sms = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+struct PairCaps {
+  int cap[4];
+};
+// Per device: the dynamic shared-memory limit of the pair kernels raised and
+// their persistent grid sizes (resident blocks x SMs) computed, once, under
+// a lock (the attribute is a per-device setting).
+template <int TPS, bool LIST>
+const PairCaps<TPS, LIST> &pair_caps() {
+  static std::mutex m;
+  static PairCaps<TPS, LIST> caps[kMaxDevices];
+  static bool ready[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+  std::lock_guard<std::mutex> lock(m);
+  PairCaps<TPS, LIST> &c = caps[dev];
+  if (!ready[dev]) {
+    const int sms = device_sms(dev);
+    int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
     cudaFuncSetAttribute(k_rho_mixed<TPS, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRhoSmem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_rho_mixed<TPS, LIST>, kBlock, kRhoSmem);
     cudaFuncSetAttribute(k_grad_mixed<TPS, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
@@ -796,11 +808,19 @@ void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, boo
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_grad_mixed<TPS, LIST>, kBlock, kGradSmem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_grad_once<TPS, LIST>, kBlock, kGradSmem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_grad_recv<kRecvTps, LIST>, kBlock, 0);
-    cap[0] = std::max(1, sms * b0);
-    cap[1] = std::max(1, sms * b1);
-    cap[2] = std::max(1, sms * b2);
-    cap[3] = std::max(1, sms * b3);
+    c.cap[0] = std::max(1, sms * b0);
+    c.cap[1] = std::max(1, sms * b1);
+    c.cap[2] = std::max(1, sms * b2);
+    c.cap[3] = std::max(1, sms * b3);
+    ready[dev] = b0 > 0 && b1 > 0 && b2 > 0 && b3 > 0;  // a failed query is retried on the next launch
+    (void)cudaGetLastError();
   }
+  return c;
+}
+
+template <int TPS, bool LIST>
+void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, bool once = false) {
+  const int *cap = pair_caps<TPS, LIST>().cap;
   const int64_t need = (a.N * TPS + kBlock - 1) / kBlock;
   k_rho_mixed<TPS, LIST>
       <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[0])), kBlock, kRhoSmem, st>>>(a);
@@ -907,9 +927,7 @@ a2c_status ensure_sym(a2c_gpp_ctx *c) {
     M->sym_sites = N + 1;
   }
   A2C_CUDA(cudaMemsetAsync(M->npre + N, 0, sizeof(int), st));
-  int dev = 0, sms = 0;
-  A2C_CUDA(cudaGetDevice(&dev));
-  A2C_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int sms = device_sms(c->device);
   k_sym_index<<<(unsigned)std::min<int64_t>(grid_for(N, 256), 8 * (int64_t)sms), 256, 0, st>>>(
       N, c->d_off, c->d_nbr, M->rev, M->npre, M->npre + N);
   A2C_CUDA(cudaGetLastError());
@@ -1019,7 +1037,7 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
       k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ);
     A2C_CUDA(cudaGetLastError());
     if (ev) cudaEventRecord(ev[1], c->stream);
-    int tps = M->tps ? M->tps : (N < 152 * 2048 ? 4 : 1);
+    const int tps = M->tps ? M->tps : default_threads_per_site(N, device_sms(c->device));
     switch (tps) {
       case 1: launch_pair_kernels<1, false>(a, c->stream, ev, once); break;
       case 2: launch_pair_kernels<2, false>(a, c->stream, ev, once); break;
@@ -1077,13 +1095,7 @@ a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const B
   a.npre = M->npre;
   a.recv = M->recv;
   a.Gown = M->Gown;
-  static int prep_cap = 0;
-  if (!prep_cap) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    prep_cap = 8 * sms;
-  }
+  const int prep_cap = 8 * device_sms(c->device);
   k_prep_list<<<(unsigned)std::min<int64_t>(grid_for(N, 256), prep_cap), 256, 0, c->stream>>>(dX, c->d_occ, bv, M->P,
                                                                                                M->occ);
   switch (tps) {
@@ -1132,20 +1144,46 @@ constexpr size_t kNaBytes = kNaTabEmb + 16 * 2 * (size_t)kEmbN;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
-// Host side: the device address of the array, looked up once per device.
-constexpr int kNaMaxDevices = 64;
-unsigned char *g_na_base[kNaMaxDevices] = {};
+// Host side, per device: the array's device address and the id of the
+// CUDA context it was resolved in.  A context id is never reused, so a
+// device reset (a new primary context, with the array's contents lost) is
+// seen on the next call, which then resolves the address and loads the
+// tables again.
+unsigned char *g_na_base[kMaxDevices] = {};
+unsigned long long g_na_ctx[kMaxDevices] = {};
 std::mutex g_na_mutex;
 float g_na_pair_host[12 * kTabN];
 float g_na_emb_host[2 * 4 * kEmbN];
 bool g_na_host_ready = false;
 
+// The current context's id through the driver entry point (no link-time
+// dependency on the driver library); 0 when it cannot be had.
+unsigned long long na_context_id() {
+  using CtxGetId = int (*)(void *, unsigned long long *);
+  static CtxGetId fn = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (CtxGetId)p;
+    (void)cudaGetLastError();
+    looked = true;
+  }
+  unsigned long long id = 0;
+  if (!fn || fn(nullptr, &id) != 0) return 0;
+  return id;
+}
+
 // Set-up on the current device: resolve the array's device address and
-// load the constant function tables into it.  Runs on a device's first call.
+// load the constant function tables into it.  Runs on a device's first
+// call, and again after the device's context was replaced.
 a2c_status na_setup(int dev, unsigned char **base) {
   std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (dev < 0 || dev >= kNaMaxDevices) return A2C_ERR_INVALID;
-  if (g_na_base[dev]) {
+  if (dev < 0 || dev >= kMaxDevices) return A2C_ERR_INVALID;
+  const unsigned long long ctx = na_context_id();
+  if (g_na_base[dev] && ctx != 0 && ctx == g_na_ctx[dev]) {
     *base = g_na_base[dev];
     return A2C_OK;
   }
@@ -1163,6 +1201,7 @@ a2c_status na_setup(int dev, unsigned char **base) {
   if (e == cudaSuccess) e = cudaMemcpy(b + kNaTabEmb, g_na_emb_host, sizeof(g_na_emb_host), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_status(e);
   g_na_base[dev] = b;
+  g_na_ctx[dev] = ctx;  // 0 (no context id available): set up again on every call
   *base = b;
   return A2C_OK;
 }
@@ -1253,7 +1292,8 @@ extern "C" a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *c, const double *d
   if (N > 0) {
     k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], (int4 *)(base + kNaP),
                                                      (float *)(base + kNaOcc));
-    const int tps = (c->mixed && c->mixed->tps) ? c->mixed->tps : (N < 152 * 2048 ? 4 : 1);
+    const int tps =
+        (c->mixed && c->mixed->tps) ? c->mixed->tps : default_threads_per_site(N, device_sms(c->device));
     switch (tps) {
       case 1: launch_pair_kernels<1, false>(a, c->stream, nullptr); break;
       case 2: launch_pair_kernels<2, false>(a, c->stream, nullptr); break;

@@ -94,8 +94,10 @@ struct LatticeSitesView {
   int mid(long i) const { return s->matid[i]; }
   const char *name(long i) const {
     const int m = s->matid[i];
-    if (names && m >= 0 && m < nnames && names[m]) return names[m];
-    return (m >= 0 && m < (int)fallback.size()) ? fallback[(size_t)m].c_str() : "M";
+    // Output.cpp:26-33: a material without a name (none given, or "") is
+    // labelled "Mat<id>"
+    if (names && m >= 0 && m < nnames && names[m] && names[m][0] != '\0') return names[m];
+    return (m >= 0 && m < (int)fallback.size()) ? fallback[(size_t)m].c_str() : "Mat";
   }
   int tag_of(long i) const { return s->tag[i]; }
   double sigma(long i) const { return s->sigma[i]; }
@@ -220,7 +222,7 @@ a2c_status a2c_snapshot_write_lattice(const a2c_snapshot_desc *d, int frame, dou
   LatticeSitesView a{sites, gamma, material_names, n_materials, {}};
   int maxm = -1;
   for (int64_t i = 0; i < sites->count; ++i) maxm = std::max(maxm, sites->matid[i]);
-  for (int m = 0; m <= maxm; ++m) a.fallback.push_back("M" + std::to_string(m));
+  for (int m = 0; m <= maxm; ++m) a.fallback.push_back("Mat" + std::to_string(m));
   return write_frame(d, frame, time, (long)sites->count, a);
 }
 

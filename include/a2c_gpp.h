@@ -229,6 +229,20 @@ a2c_status a2c_gpp_autotune(a2c_gpp_ctx *ctx, int reps, int *tps, float *ms);
  * loop instead (the FP64 plain form always uses it). */
 a2c_status a2c_gpp_set_minimizer(a2c_gpp_ctx *ctx, int host_loop);
 
+/* Allocation-free mixed-precision evaluation.  No counterpart in the
+ * reference: it is for callers that cannot allocate device memory while they
+ * evaluate -- a solver callback running inside another framework's memory
+ * pool, or work recorded under a driver that forbids allocation while it
+ * records.  Same arguments and results as a2c_gpp_eval_device in mixed
+ * precision (device pointers, stream-ordered on the context's stream), with
+ * the pass-2 pairs visited from both sides.  Its scratch is one fixed
+ * device array inside the library (about 5.8 MB, held by every GPU that
+ * loads the library until the process exits), so it serves at most 131,072
+ * sites and returns A2C_ERR_INVALID above that; it calls no allocator.  The
+ * first call on a device resolves the array and loads the function tables
+ * into it (make that call before any stream capture); a device reset is
+ * noticed on the next call, which loads them again.  Every call shares the
+ * array: calls that overlap on one GPU race. */
 a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG);
 /* Profiling aid: one stream-ordered evaluation on device pointers with CUDA
  * events between its launches; stage_ms[4] receives the durations of the

@@ -16,7 +16,10 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "liba2c_oracle.so"
 REF_SO = HERE / "_ref" / "liba2c_ref.so"
-REFERENCE_TREE = Path("/root/reference")
+# The reference tree: $A2C_REFERENCE_TREE when set, else a directory named
+# "reference" beside the repository (absent on machines that run only the
+# prebuilt libraries).
+REFERENCE_TREE = Path(os.environ.get("A2C_REFERENCE_TREE") or (HERE.parent.parent / "reference"))
 
 ID_MASK = (1 << 27) - 1
 EAM_FUNCS = ["F_Pd", "F_Pd_deriv", "F_H", "F_H_deriv", "f_Pd", "f_Pd_deriv", "f_H", "f_H_deriv", "phi_Pd",
@@ -32,8 +35,8 @@ def build(ref: bool | None = None) -> None:
     if ref is None:
         ref = REFERENCE_TREE.is_dir()
     if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
-        subprocess.run(["make", "-s", "-C", str(HERE), "geo"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_TREE}"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), "geo", f"REF={REFERENCE_TREE}"], check=True)
 
 
 class OrcParams(C.Structure):

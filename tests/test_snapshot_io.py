@@ -121,8 +121,14 @@ def test_lattice_sites_writer_matches_evaluator_layout(tmp_path):
         A.snapshot_write_lattice(b, 2, 0.5, sites, gamma=g_all, material_names=["Pd", "H"])
         for ext in ("_L0_0002.vtp", "_L0_0002.xyz"):
             assert open(tmp_path / f"a{prec}{ext}").read() == open(tmp_path / f"b{prec}{ext}").read()
-    # unnamed materials are labelled M<id>
+    # unnamed materials are labelled Mat<id>, as Output.cpp:26-33 does for
+    # no name and for an empty MaterialName alike
     c = A.snapshot_desc(str(tmp_path / "c"), fmt="xyz")
     A.snapshot_write_lattice(c, 0, 0.0, sites)
     rows = open(tmp_path / "c_L0_0000.xyz").read().splitlines()[2:]
-    assert [r.split()[0] for r in rows] == ["M0"] * nPd + ["M1"] * nH
+    assert [r.split()[0] for r in rows] == ["Mat0"] * nPd + ["Mat1"] * nH
+    d = A.snapshot_desc(str(tmp_path / "d"), fmt="xyz")
+    A.snapshot_write_lattice(d, 0, 0.0, sites, material_names=["", "H"])
+    rows = open(tmp_path / "d_L0_0000.xyz").read().splitlines()[2:]
+    assert [r.split()[0] for r in rows] == ["Mat0"] * nPd + ["H"] * nH
+    assert all(len(r.split()) == len(rows[0].split()) for r in rows)

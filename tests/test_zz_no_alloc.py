@@ -30,13 +30,20 @@ def noalloc_fn():
     return fn
 
 
-def test_noalloc_matches_context_path_twice(gpu):
+# (cells, periodic): a small slab, and the largest lattice the fixed array
+# holds (32 x 32 x 16 cells = 131,072 sites)
+SIZES = {"slab_8x8x6": ((8, 8, 6), (1, 1, 0)), "max_32x32x16": ((32, 32, 16), (1, 1, 1))}
+
+
+@pytest.mark.parametrize("size", list(SIZES))
+def test_noalloc_matches_context_path_twice(gpu, size):
     import torch
 
     fn = noalloc_fn()
-    X, xH, _, box, nPd, nH = A.lattice_fcc((8, 8, 6), periodic=(1, 1, 0), pos_std=0.03, sigma=(0.08, 0.14),
+    cells, per = SIZES[size]
+    X, xH, _, box, nPd, nH = A.lattice_fcc(cells, periodic=per, pos_std=0.03, sigma=(0.08, 0.14),
                                            x_center=0.15, x_half=0.15, seed=2)
-    with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 0), precision="mixed") as g:
+    with A.Gpp(nPd, nH, box=box, periodic=per, precision="mixed") as g:
         g.set_occupancy(xH)
         g.build_neighbors(X)
         dX = torch.tensor(X, device="cuda")
