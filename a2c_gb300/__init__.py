@@ -13,7 +13,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _native as N
-from ._native import A2CError, A2C_FP64, A2C_MIXED, A2C_PAIRS_BOTH_SIDES, A2C_PAIRS_ONCE  # noqa: F401
+from ._native import A2CError, A2C_ERR_LISTS_STALE, A2C_FP64, A2C_MIXED, A2C_PAIRS_BOTH_SIDES, A2C_PAIRS_ONCE  # noqa: F401
 from ._native import (CONVERGED_GATOL, CONVERGED_STALLED, DIVERGED_LS_FAILURE, DIVERGED_MAXFCN,  # noqa: F401
                       DIVERGED_MAXITS, DIVERGED_NAN)
 
@@ -241,9 +241,12 @@ class Gpp:
     def snapshot_wait(self) -> None:
         N.check(self._L.a2c_gpp_snapshot_wait(self._h), "a2c_gpp_snapshot_wait")
 
-    def set_minimizer(self, host_loop: bool) -> None:
-        """Mixed precision: device-driven graph ticks (default) or the host loop."""
-        N.check(self._L.a2c_gpp_set_minimizer(self._h, int(bool(host_loop))), "a2c_gpp_set_minimizer")
+    def set_minimizer(self, mode) -> None:
+        """L-BFGS driver (a2c_gpp_set_minimizer): "default" (mixed precision
+        device-driven, FP64 host-driven), "host" (True) or "device" (the
+        engine for both forms)."""
+        m = {"default": 0, False: 0, "host": 1, True: 1, "device": 2}[mode]
+        N.check(self._L.a2c_gpp_set_minimizer(self._h, m), "a2c_gpp_set_minimizer")
 
     def set_neighbor_skin(self, skin: float) -> None:
         N.check(self._L.a2c_gpp_set_neighbor_skin(self._h, float(skin)), "a2c_gpp_set_neighbor_skin")

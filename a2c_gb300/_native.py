@@ -21,6 +21,7 @@ A2C_ERR_NONFINITE = 5
 A2C_ERR_STATE = 6
 A2C_ERR_TIMEOUT = 7
 A2C_ERR_NO_DEVICE = 8
+A2C_ERR_LISTS_STALE = 9
 
 A2C_FP64 = 0
 A2C_MIXED = 1

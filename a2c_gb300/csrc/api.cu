@@ -42,6 +42,19 @@ int device_sms(int dev) {
   return cache[dev];
 }
 
+void span_limits(const a2c_gpp_ctx *c, double lim[3], const double **xlist) {
+  bool any = false;
+  for (int d = 0; d < 3; ++d) {
+    if (c->p.periodic[d]) {
+      lim[d] = HUGE_VAL;
+    } else {
+      any = true;
+      lim[d] = std::isfinite(c->list_reach[d]) ? 0.5 * (0.5 * kFreeSpan - c->list_reach[d]) : -HUGE_VAL;
+    }
+  }
+  *xlist = any ? c->d_xlist : nullptr;
+}
+
 int current_device_sms() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -207,6 +220,8 @@ const char *a2c_status_string(a2c_status s) {
     case A2C_ERR_STATE: return "call order violated (build neighbors / set state first)";
     case A2C_ERR_TIMEOUT: return "bounded device wait gave up";
     case A2C_ERR_NO_DEVICE: return "no usable CUDA device";
+    case A2C_ERR_LISTS_STALE:
+      return "mixed form: a site moved too far in a free direction since the neighbor lists were built; rebuild them";
     default: return "unknown status";
   }
 }
@@ -240,6 +255,8 @@ a2c_status a2c_gpp_create(const a2c_gpp_params *p, a2c_gpp_ctx **out) {
   if (!s) s = dalloc(&c->d_npd, N);
   if (!s) s = dalloc(&c->d_shell, 3 * (int64_t)p->nPd);
   if (!s) s = dalloc(&c->d_hh1_off, (int64_t)p->nH + 1);
+  for (int d = 0; d < 3; ++d) c->list_reach[d] = HUGE_VAL;  // no lists yet
+  if (!s && (!p->periodic[0] || !p->periodic[1] || !p->periodic[2])) s = dalloc(&c->d_xlist, 4 * N);
   if (!s && cudaMallocHost((void **)&c->h_small, 64) != cudaSuccess) s = A2C_ERR_NOMEM;
   if (!s) {
     if (N > 0) {
@@ -270,7 +287,7 @@ a2c_status a2c_gpp_destroy(a2c_gpp_ctx *c) {
   for (void *p : {(void *)c->d_X, (void *)c->d_G, (void *)c->d_occ, (void *)c->d_rho, (void *)c->d_Fp,
                   (void *)c->d_Vs, (void *)c->d_Ss, (void *)c->d_red, (void *)c->d_status, (void *)c->d_off,
                   (void *)c->d_nbr, (void *)c->d_npd, (void *)c->d_shell, (void *)c->d_hh1_off, (void *)c->d_hh1,
-                  (void *)c->d_ext_off, (void *)c->d_ext_nbr, (void *)c->d_xref})
+                  (void *)c->d_ext_off, (void *)c->d_ext_nbr, (void *)c->d_xref, (void *)c->d_xlist})
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->h_small) cudaFreeHost(c->h_small);
@@ -342,9 +359,9 @@ a2c_status a2c_gpp_autotune(a2c_gpp_ctx *c, int reps, int *tps_out, float *ms) {
   return s;
 }
 
-a2c_status a2c_gpp_set_minimizer(a2c_gpp_ctx *c, int host_loop) {
-  if (!c) return A2C_ERR_INVALID;
-  c->host_loop = host_loop ? 1 : 0;
+a2c_status a2c_gpp_set_minimizer(a2c_gpp_ctx *c, int mode) {
+  if (!c || mode < A2C_MINIMIZER_DEFAULT || mode > A2C_MINIMIZER_DEVICE) return A2C_ERR_INVALID;
+  c->host_loop = mode;
   return A2C_OK;
 }
 
@@ -602,10 +619,22 @@ a2c_status a2c_gpp_set_neighbor_lists(a2c_gpp_ctx *c, const double *X, const int
   c->max_neighbors = maxn;
   ++c->nbr_version;
   c->has_neighbors = true;
+  // the span guard: how far apart a listed pair is in each free direction
+  // (unknown without positions)
+  for (int d = 0; d < 3; ++d) {
+    c->list_reach[d] = (c->p.periodic[d] || (X && N > 0)) ? 0.0 : HUGE_VAL;
+    if (c->p.periodic[d] || !X) continue;
+    double r = 0.0;
+    for (int64_t i = 0; i < N; ++i)
+      for (int64_t t = off[(size_t)i]; t < off[(size_t)i + 1]; ++t)
+        r = std::max(r, std::fabs(X[4 * i + d] - X[4 * (int64_t)(nbr[(size_t)t] & kIdMask) + d]));
+    c->list_reach[d] = r;
+  }
   A2C_TRY(mixed_lists_changed(c));
   c->has_density = false;
   if (X && N > 0) {
     A2C_TRY(copy_in(c, c->d_X, X, 4 * N));
+    if (c->d_xlist) A2C_TRY(copy_in(c, c->d_xlist, X, 4 * N));
     c->has_state = true;
   }
   return finish(c);
@@ -737,6 +766,7 @@ a2c_status a2c_gpp_eval(a2c_gpp_ctx *c, const double *X, double *f, double *G) {
     if (st & kStatusOverflow) return A2C_ERR_NEIGHBOR_OVERFLOW;
     if (st & kStatusTimeout) return A2C_ERR_TIMEOUT;
     if (st & kStatusNonfinite) return A2C_ERR_NONFINITE;
+    if (st & kStatusSpan) return A2C_ERR_LISTS_STALE;
     return A2C_OK;
   }
   A2C_TRY(copy_in(c, c->d_X, X, 4 * c->N));

@@ -28,6 +28,7 @@
 // the batch, and the oracle reproduces them (its "batch" reduction order).
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -860,6 +861,18 @@ struct DeviceGuard2 {
   explicit DeviceGuard2(int d) { cudaSetDevice(d); }
 };
 
+// The span-guard limits of instance k (InstGeo::lim): a batch builds its
+// lists at each instance's cutoff; a context's one-instance engine takes
+// the reach of the context's lists (which the caller may have supplied).
+void set_limits(const a2c_gpp_batch *b, int k, InstGeo &G) {
+  const a2c_gpp_params &p = b->P[(size_t)k];
+  for (int d = 0; d < 3; ++d) {
+    const double reach = b->borrowed ? b->c->list_reach[d] : p.rc;
+    G.lim[d] = p.periodic[d] ? HUGE_VALF
+                             : (std::isfinite(reach) ? (float)(0.5 * (0.5 * kFreeSpan - reach)) : -HUGE_VALF);
+  }
+}
+
 // Instance, chunk and list tables of a batch whose system b->c exists;
 // set_occ: Pd occupancy 1, H 0 (a fresh union system).
 a2c_status init_tables(a2c_gpp_batch *b, const a2c_gpp_params *params, int n, bool set_occ) {
@@ -879,9 +892,10 @@ a2c_status init_tables(a2c_gpp_batch *b, const a2c_gpp_params *params, int n, bo
     b->start[k + 1] = s0 + nk;
     InstGeo &G = geo[k];
     for (int d = 0; d < 3; ++d) {
-      G.S[d] = p.periodic[d] ? p.box[d] : 64.0;
+      G.S[d] = p.periodic[d] ? p.box[d] : kFreeSpan;
       G.sc[d] = (float)(G.S[d] / 4294967296.0);
     }
+    set_limits(b, k, G);
     G.T = p.T;
     G.start = (int)s0;
     G.nPd = p.nPd;
@@ -1101,6 +1115,12 @@ a2c_status a2c_gpp_batch_create(const a2c_gpp_params *params, int n, a2c_gpp_bat
     return s;
   }
   s = init_tables(b, params, n, true);
+  bool any_free = false;
+  for (int k = 0; k < n; ++k)
+    for (int d = 0; d < 3; ++d) any_free = any_free || !params[k].periodic[d];
+  if (!s && any_free && !b->c->d_xlist &&
+      cudaMalloc(&b->c->d_xlist, sizeof(double) * 4 * (size_t)std::max<int64_t>(N, 1)) != cudaSuccess)
+    s = A2C_ERR_NOMEM;
   if (s) {
     a2c_gpp_batch_destroy(b);
     return s;
@@ -1194,6 +1214,8 @@ a2c_status a2c_gpp_batch_build_neighbors(a2c_gpp_batch *b, const double *X, int 
     maxn = std::max(maxn, mk);
   }
   k_set_i64<<<1, 1, 0, c->stream>>>(c->d_off + N, base);
+  if (c->d_xlist && N > 0)  // span guard: the positions the lists were built at
+    A2C_CUDA(cudaMemcpyAsync(c->d_xlist, X, sizeof(double) * 4 * N, cudaMemcpyHostToDevice, c->stream));
   A2C_CUDA(cudaStreamSynchronize(c->stream));
   c->nbr_total = base;
   c->max_neighbors = maxn;
@@ -1352,6 +1374,11 @@ a2c_status engine_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *l
   }
   b->precision = c->p.precision;
   b->tps = mixed_threads_per_site(c);
+  {  // the context's lists may have changed since the tables were made
+    InstGeo G{};
+    set_limits(b, 0, G);
+    A2C_CUDA(cudaMemcpy((char *)b->geo + offsetof(InstGeo, lim), G.lim, sizeof(G.lim), cudaMemcpyHostToDevice));
+  }
   std::vector<Inst> last;
   int it = 0, fev = 0, why = 0;
   double f = 0.0, gn = 0.0;

@@ -19,11 +19,12 @@ constexpr double kB = 8.6173324e-5;  // minimizer.cpp:92
 // of instance b are [start, start + nPd + nH), Pd first, in the caller's
 // concatenated layout; neighbor lists never cross instances.
 struct InstGeo {
-  double S[3];   // periodic box length, or 64 A in a free direction
+  double S[3];   // periodic box length, or kFreeSpan in a free direction
   double T;      // temperature [K]
   float sc[3];   // S / 2^32 (one fixed-point unit of the mixed form)
   int start;     // first site
   int nPd, nH;
+  float lim[3];  // free direction: how far a site may move from its list position (span guard); else +inf
 };
 
 // What a list-driven evaluator launch reads: the instance of every site,
@@ -55,7 +56,15 @@ struct SiteArgs {
 };
 
 // Device status bits (a2c never traps; kernels record and return).
-enum : int { kStatusNonfinite = 1, kStatusOverflow = 2, kStatusTimeout = 4, kStatusBadIndex = 8 };
+// kStatusSpan: the mixed form's fixed-point span cannot represent a listed
+// pair any more (a site moved too far in a free direction since the lists
+// were built).
+enum : int { kStatusNonfinite = 1, kStatusOverflow = 2, kStatusTimeout = 4, kStatusBadIndex = 8, kStatusSpan = 16 };
+
+// The mixed form encodes free-direction coordinates modulo this span [A]:
+// the difference of two encoded coordinates is exact while the pair is
+// less than half of it apart.
+constexpr double kFreeSpan = 64.0;
 
 struct Mixed;   // mixed-precision buffers (k_mixed.cu)
 struct Lbfgs;   // L-BFGS buffers (lbfgs.cu)
@@ -90,6 +99,11 @@ struct a2c_gpp_ctx {
   uint32_t *d_ext_nbr;
   int64_t ext_cap, ext_total;
   double *d_xref;      // 4N
+  // The mixed form's free-direction guard: positions the current lists were
+  // built from (4N, allocated when a direction is free) and, per direction,
+  // how far apart a listed pair was at most then (infinite when unknown).
+  double *d_xlist;
+  double list_reach[3];
   // host staging
   double *h_pinned;
   int64_t h_pinned_n;
@@ -97,7 +111,7 @@ struct a2c_gpp_ctx {
   a2c::Lbfgs *lbfgs;
   void *snap;  // the snapshot in flight (api.cu)
   void *engine;     // the device-driven minimizer (batch.cu), created on first use
-  int host_loop;    // 1: mixed-precision minimization by the host loop (lbfgs.cu)
+  int host_loop;    // L-BFGS driver, A2C_MINIMIZER_* (a2c_gpp_set_minimizer)
   double *h_small;  // pinned: f and the status word of a host-pointer call
   int last_mixed_iters, last_fp64_iters;
   double last_mixed_gnorm;
@@ -154,6 +168,13 @@ a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X);
 // skin path (positions in c->d_X; h_X may be null): rebuild the extended
 // lists if needed, then re-filter at rc
 a2c_status update_neighbors_device(a2c_gpp_ctx *c, const double *h_X, int *rebuilt);
+
+// The span guard of the mixed form: per direction, how far a site may move
+// from the position the lists were built at before a listed pair could
+// reach half the free span (+inf where periodic; negative when the lists'
+// reach is unknown or too long), and the list positions to compare with
+// (null when every direction is periodic).
+void span_limits(const a2c_gpp_ctx *c, double lim[3], const double **xlist);
 
 // k_mixed.cu
 // ev: optional 5 events recorded before the first launch and after each

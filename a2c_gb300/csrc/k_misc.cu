@@ -232,6 +232,7 @@ a2c_status check_status_word(a2c_gpp_ctx *c) {
   if (st & kStatusOverflow) return A2C_ERR_NEIGHBOR_OVERFLOW;
   if (st & kStatusTimeout) return A2C_ERR_TIMEOUT;
   if (st & kStatusNonfinite) return A2C_ERR_NONFINITE;
+  if (st & kStatusSpan) return A2C_ERR_LISTS_STALE;
   return A2C_OK;
 }
 

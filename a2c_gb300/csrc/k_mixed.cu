@@ -6,10 +6,14 @@
 //
 // Layout per evaluation (k_prep): every site becomes one int4 -- its
 // position as three 32-bit fixed-point coordinates (unit S/2^32 with S the
-// periodic box length, or 64 A in a free direction) and sigma as FP32 bits.
-// The integer difference of two coordinates, taken modulo 2^32, is the
-// minimum-image difference exactly, so no FP64 arithmetic and no image
-// decoding happen per neighbor; converting it to FP32 costs one rounding.
+// periodic box length, or kFreeSpan = 64 A in a free direction) and sigma
+// as FP32 bits.  The integer difference of two coordinates, taken modulo
+// 2^32, is the minimum-image difference exactly, so no FP64 arithmetic and
+// no image decoding happen per neighbor; converting it to FP32 costs one
+// rounding.  In a free direction it is exact while the pair is less than
+// 32 A apart: the prep kernels flag any site that moved far enough from
+// its position at the list build for a listed pair to get there
+// (span_check), and the call returns A2C_ERR_LISTS_STALE.
 //
 // Quadrature in closed form: point k moves coordinate m = k/2 mod 3 of atom i
 // (k < 6) or of atom j (k >= 6) by u = sqrt(6) sigma, so with the pair
@@ -700,27 +704,29 @@ __global__ void k_sym_index(int64_t N, const int64_t *off, const uint32_t *nbr, 
   }
 }
 
-__global__ void k_prep(const double *X, const double *occ, int64_t N, double k0, double k1, double k2, int4 *P,
-                       float *occf) {
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= N) return;
-  const long long u0 = __double2ll_rn(X[4 * s] * k0);
-  const long long u1 = __double2ll_rn(X[4 * s + 1] * k1);
-  const long long u2 = __double2ll_rn(X[4 * s + 2] * k2);
-  P[s] = make_int4((int)(unsigned)u0, (int)(unsigned)u1, (int)(unsigned)u2, __float_as_int((float)X[4 * s + 3]));
-  occf[s] = (float)occ[s];
+// Span guard (free directions only; xl null when every direction is
+// periodic): a site more than lim from the position its lists were built at
+// could make a listed pair leave the fixed-point span, where the encoded
+// difference would wrap.  Flag it; the caller gets A2C_ERR_LISTS_STALE.
+__device__ __forceinline__ void span_check(const double4 &x, const double *xl, int64_t s, double l0, double l1,
+                                           double l2, int *status) {
+  if (!xl) return;
+  const double4 r = *reinterpret_cast<const double4 *>(xl + 4 * s);
+  if (fabs(x.x - r.x) > l0 || fabs(x.y - r.y) > l1 || fabs(x.z - r.z) > l2) atomicOr(status, kStatusSpan);
 }
 
-// The same, reading X from the caller's pinned host memory over the
-// coherent host link: also keeps the context's device copy of the state and
-// flags non-finite inputs (what a separate copy and check would do).
-__global__ void k_prep_copy(const double *X, const double *occ, int64_t N, double k0, double k1, double k2, int4 *P,
-                            float *occf, double *Xcopy, int *status) {
+struct SpanArgs {
+  const double *xl;  // list positions (4N), null when all directions are periodic
+  double lim[3];
+  int *status;
+};
+
+__global__ void k_prep(const double *X, const double *occ, int64_t N, double k0, double k1, double k2, int4 *P,
+                       float *occf, SpanArgs sg) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= N) return;
-  const double4 x = *reinterpret_cast<const double4 *>(X + 4 * s);
-  *reinterpret_cast<double4 *>(Xcopy + 4 * s) = x;
-  if (!isfinite(x.x) || !isfinite(x.y) || !isfinite(x.z) || !isfinite(x.w)) atomicOr(status, kStatusNonfinite);
+  const double4 x = make_double4(X[4 * s], X[4 * s + 1], X[4 * s + 2], X[4 * s + 3]);
+  span_check(x, sg.xl, s, sg.lim[0], sg.lim[1], sg.lim[2], sg.status);
   const long long u0 = __double2ll_rn(x.x * k0);
   const long long u1 = __double2ll_rn(x.y * k1);
   const long long u2 = __double2ll_rn(x.z * k2);
@@ -728,18 +734,47 @@ __global__ void k_prep_copy(const double *X, const double *occ, int64_t N, doubl
   occf[s] = (float)occ[s];
 }
 
-// Batched: positions of the listed sites with their instance's scale.
-__global__ void k_prep_list(const double *X, const double *occ, BatchView bv, int4 *P, float *occf) {
+// The same, reading X from the caller's pinned host memory over the
+// coherent host link: also keeps the context's device copy of the state and
+// flags non-finite inputs (what a separate copy and check would do).
+__global__ void k_prep_copy(const double *X, const double *occ, int64_t N, double k0, double k1, double k2, int4 *P,
+                            float *occf, double *Xcopy, SpanArgs sg) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  const double4 x = *reinterpret_cast<const double4 *>(X + 4 * s);
+  *reinterpret_cast<double4 *>(Xcopy + 4 * s) = x;
+  if (!isfinite(x.x) || !isfinite(x.y) || !isfinite(x.z) || !isfinite(x.w)) atomicOr(sg.status, kStatusNonfinite);
+  span_check(x, sg.xl, s, sg.lim[0], sg.lim[1], sg.lim[2], sg.status);
+  const long long u0 = __double2ll_rn(x.x * k0);
+  const long long u1 = __double2ll_rn(x.y * k1);
+  const long long u2 = __double2ll_rn(x.z * k2);
+  P[s] = make_int4((int)(unsigned)u0, (int)(unsigned)u1, (int)(unsigned)u2, __float_as_int((float)x.w));
+  occf[s] = (float)occ[s];
+}
+
+// Batched: positions of the listed sites with their instance's scale (and
+// its span-guard limits; xl null when no instance has a free direction).
+__global__ void k_prep_list(const double *X, const double *occ, BatchView bv, int4 *P, float *occf, const double *xl,
+                            int *status) {
   const int n = *bv.count;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int64_t s = bv.list[k];
     const InstGeo &g = bv.geo[bv.inst[s]];
-    const long long u0 = __double2ll_rn(X[4 * s] * (4294967296.0 / g.S[0]));
-    const long long u1 = __double2ll_rn(X[4 * s + 1] * (4294967296.0 / g.S[1]));
-    const long long u2 = __double2ll_rn(X[4 * s + 2] * (4294967296.0 / g.S[2]));
-    P[s] = make_int4((int)(unsigned)u0, (int)(unsigned)u1, (int)(unsigned)u2, __float_as_int((float)X[4 * s + 3]));
+    const double4 x = make_double4(X[4 * s], X[4 * s + 1], X[4 * s + 2], X[4 * s + 3]);
+    span_check(x, xl, s, g.lim[0], g.lim[1], g.lim[2], status);
+    const long long u0 = __double2ll_rn(x.x * (4294967296.0 / g.S[0]));
+    const long long u1 = __double2ll_rn(x.y * (4294967296.0 / g.S[1]));
+    const long long u2 = __double2ll_rn(x.z * (4294967296.0 / g.S[2]));
+    P[s] = make_int4((int)(unsigned)u0, (int)(unsigned)u1, (int)(unsigned)u2, __float_as_int((float)x.w));
     occf[s] = (float)occ[s];
   }
+}
+
+SpanArgs span_args(const a2c_gpp_ctx *c) {
+  SpanArgs sg;
+  span_limits(c, sg.lim, &sg.xl);
+  sg.status = c->d_status;
+  return sg;
 }
 
 // Persistent grids: as many blocks as fit on the device at once (occupancy
@@ -1005,7 +1040,7 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   a.W = (float)c->p.QWp;
   double k[3];
   for (int d = 0; d < 3; ++d) {
-    const double S = c->p.periodic[d] ? c->p.box[d] : 64.0;  // free direction: any span > 2 x neighbor reach
+    const double S = c->p.periodic[d] ? c->p.box[d] : kFreeSpan;  // free direction: guarded span (span_check)
     k[d] = 4294967296.0 / S;
     a.sc[d] = (float)(S / 4294967296.0);
   }
@@ -1030,11 +1065,12 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   a.Gown = M->Gown;
   if (ev) cudaEventRecord(ev[0], c->stream);
   if (N > 0) {
+    const SpanArgs sg = span_args(c);
     if (Xcopy)
       k_prep_copy<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ, Xcopy,
-                                                           c->d_status);
+                                                           sg);
     else
-      k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ);
+      k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ, sg);
     A2C_CUDA(cudaGetLastError());
     if (ev) cudaEventRecord(ev[1], c->stream);
     const int tps = M->tps ? M->tps : default_threads_per_site(N, device_sms(c->device));
@@ -1096,8 +1132,8 @@ a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const B
   a.recv = M->recv;
   a.Gown = M->Gown;
   const int prep_cap = 8 * device_sms(c->device);
-  k_prep_list<<<(unsigned)std::min<int64_t>(grid_for(N, 256), prep_cap), 256, 0, c->stream>>>(dX, c->d_occ, bv, M->P,
-                                                                                               M->occ);
+  k_prep_list<<<(unsigned)std::min<int64_t>(grid_for(N, 256), prep_cap), 256, 0, c->stream>>>(
+      dX, c->d_occ, bv, M->P, M->occ, c->d_xlist, c->d_status);
   switch (tps) {
     case 1: launch_pair_kernels<1, true>(a, c->stream, nullptr, once); break;
     case 2: launch_pair_kernels<2, true>(a, c->stream, nullptr, once); break;
@@ -1269,7 +1305,7 @@ extern "C" a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *c, const double *d
   a.W = (float)c->p.QWp;
   double k[3];
   for (int d = 0; d < 3; ++d) {
-    const double S = c->p.periodic[d] ? c->p.box[d] : 64.0;
+    const double S = c->p.periodic[d] ? c->p.box[d] : kFreeSpan;
     k[d] = 4294967296.0 / S;
     a.sc[d] = (float)(S / 4294967296.0);
   }
@@ -1291,7 +1327,7 @@ extern "C" a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *c, const double *d
   // in this call (P, occupancy, F/F', energy partials, block partials).
   if (N > 0) {
     k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], (int4 *)(base + kNaP),
-                                                     (float *)(base + kNaOcc));
+                                                     (float *)(base + kNaOcc), span_args(c));
     const int tps =
         (c->mixed && c->mixed->tps) ? c->mixed->tps : default_threads_per_site(N, device_sms(c->device));
     switch (tps) {

@@ -393,7 +393,13 @@ a2c_status make_lists(a2c_gpp_ctx *c, const GridArgs &g, Src src, bool ext) {
   A2C_CUDA(cudaMemcpyAsync(&stat, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
   A2C_CUDA(cudaStreamSynchronize(st));
   if (stat & kStatusBadIndex) return A2C_ERR_STATE;
-  if (!ext) ++c->nbr_version;
+  if (!ext) {
+    ++c->nbr_version;
+    // span guard: lists at the cutoff, built from the positions in d_X
+    for (int d = 0; d < 3; ++d) c->list_reach[d] = p.periodic[d] ? 0.0 : g.rc;
+    if (c->d_xlist && N > 0)
+      A2C_CUDA(cudaMemcpyAsync(c->d_xlist, c->d_X, sizeof(double) * 4 * N, cudaMemcpyDeviceToDevice, st));
+  }
   return A2C_OK;
 }
 

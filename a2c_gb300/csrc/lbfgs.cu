@@ -270,8 +270,9 @@ a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp
   // Mixed precision: the same algorithm driven on the device (batch.cu, one
   // instance; its global sums in the per-instance chunk order) unless the
   // host loop below is asked for.  The FP64 plain form keeps the host loop,
-  // whose reductions the oracle replays bit for bit.
-  if (c->p.precision == A2C_MIXED && !c->host_loop)
+  // whose reductions the oracle replays bit for bit, unless the device
+  // engine is asked for.
+  if ((c->p.precision == A2C_MIXED && c->host_loop == A2C_MINIMIZER_DEFAULT) || c->host_loop == A2C_MINIMIZER_DEVICE)
     return engine_minimize(c, dX, lp, fmin, iters, nfev, gnorm_out, reason);
   A2C_TRY(lbfgs_alloc(c, lp->m));
   Lbfgs *L = c->lbfgs;

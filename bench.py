@@ -23,8 +23,8 @@ data-path collective); `value` is the sum over ranks of atom-evals divided
 by the slowest rank's device time.
 
 --impl reference times the reference's CPU algorithm (the oracle port with
-the reference's redundant finite-difference calls, all host threads) on a
-bounded 12x12x12-cell sample of the same workload.
+the reference's redundant finite-difference calls, all host threads) on the
+same 262,144-site workload, without loading this repository's library.
 """
 from __future__ import annotations
 
@@ -147,23 +147,31 @@ def measured_peaks():
         return {}
 
 
-def cpu_sample(threads: int, seconds: float = 10.0, max_evals: int = 50):
-    """The oracle (reference arithmetic, the reference's redundant FD calls)
-    on a 12x12x12-cell sample drawn like the workload; returns (atom-evals/s,
-    evals, sites)."""
-    import a2c_gb300 as A
+def workload_lattice(ncell=None):
+    """The evaluator-throughput lattice from the oracle's generator (the
+    same values as the library's a2c_lattice_fcc, without loading the
+    library): (X, xH, surface, box, nPd, nH)."""
     from oracle import oracle as O
 
-    w = dict(WORKLOAD, ncell=12)
-    X, xH, _, box, nPd, nH = A.lattice_fcc(w["ncell"], periodic=w["periodic"], pos_std=w["pos_std"],
-                                           sigma=w["sigma"], x_center=w["x_center"], x_half=w["x_half"],
-                                           seed=w["seed"])
-    pb = O.Problem(nPd, nH, box=box, periodic=w["periodic"])
+    w = dict(WORKLOAD)
+    if ncell:
+        w["ncell"] = ncell
+    return O.lattice_fcc(w["ncell"], periodic=w["periodic"], pos_std=w["pos_std"], sigma=w["sigma"],
+                         x_center=w["x_center"], x_half=w["x_half"], seed=w["seed"])
+
+
+def cpu_sample(threads: int, max_evals: int = 4, seconds: float = 20.0):
+    """The oracle (reference arithmetic, the reference's redundant FD calls)
+    on the full 262,144-site workload: `max_evals` evaluations, fewer when
+    they would exceed `seconds`; returns (atom-evals/s, evals, sites)."""
+    from oracle import oracle as O
+
+    X, xH, _, box, nPd, nH = workload_lattice()
+    pb = O.Problem(nPd, nH, box=box, periodic=WORKLOAD["periodic"])
     off, nbr, *_ = O.neighbors(pb, X)
-    O.evaluate(pb, X, xH, off, nbr, mode=1, threads=threads)  # warm-up
     t0 = time.perf_counter()
     n = 0
-    while n < max_evals and (time.perf_counter() - t0) < seconds:
+    while n < max_evals and (n == 0 or (time.perf_counter() - t0) * (n + 1) / n < seconds):
         O.evaluate(pb, X, xH, off, nbr, mode=1, threads=threads)
         n += 1
     dt = time.perf_counter() - t0
@@ -182,16 +190,23 @@ def nucleus_lattice(cells: int, seed: int = 3):
                          seed=seed)
 
 
-def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0, polish_cap: int = 0):
-    """Wall time of a2c_gpp_minimize to gatol in FP64 and in mixed precision
-    -- the mixed form alone and the mixed form followed by the FP64 polish --
-    and the mixed results' distance from the FP64 minimum.  With fp64_cap >
-    0 the FP64 run stops after fp64_cap iterations (the full run is too long
-    for one GPU session); its time to minimum is then extrapolated as its
-    measured seconds per iteration times the iterations of the mixed phase
-    (a low estimate of what FP64 needs), and labelled so.  With polish_cap > 0 the FP64 polish
-    gets at most polish_cap iterations (the mixed phase is the same
-    deterministic trajectory as the run without polish)."""
+def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0, polish_cap: int = 0,
+                    gatol_mixed: float = 1e-6):
+    """Wall time of a2c_gpp_minimize to `gatol` in FP64 and in mixed
+    precision on the hydride-nucleus lattice, and how far the mixed results
+    are from the FP64 minimum.
+
+    FP64 runs twice: host-driven (its sums in the single-system order) and
+    device-driven by the batched engine (sums in chunks of 2048 terms).  The
+    two are the same algorithm on the same objective; their distance
+    (`fp64_vs_fp64_spread`) is how well `gatol` determines the minimum at
+    all, and every mixed error is reported beside it.  The mixed form runs
+    alone (gatol on its own gradient) and followed by the FP64 polish
+    (gatol on the FP64 gradient), both to the same `gatol`, and alone to
+    `gatol_mixed` (the configuration's 1e-6, below the FP64 form's
+    finite-difference floor at this size).  With fp64_cap > 0 the FP64 runs
+    stop after fp64_cap iterations and the FP64 time is extrapolated
+    (labelled); polish_cap > 0 caps the polish iterations."""
     import numpy as np
 
     import a2c_gb300 as A
@@ -199,6 +214,11 @@ def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0, po
     X, xH, _, box, nPd, nH = nucleus_lattice(cells)
     out = {"cells": cells, "sites": nPd + nH, "gatol": gatol}
     kw = dict(gatol=gatol, max_it=20000, max_fev=40000)
+
+    def state_err(Xa, Xb):
+        a, b = Xa.reshape(-1, 4), Xb.reshape(-1, 4)
+        return float(np.abs(a[:, :3] - b[:, :3]).max()), float(np.abs(a[:, 3] - b[:, 3]).max())
+
     with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1), device=device) as g:
         g.set_occupancy(xH)
         g.build_neighbors(X)
@@ -207,13 +227,18 @@ def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0, po
         g.eval(X)
         out["autotune_tps"] = g.autotune()[0]
         g.set_precision("fp64")
-        t0 = time.perf_counter()
-        r64 = g.minimize(X, **(dict(kw, max_it=fp64_cap) if fp64_cap else kw))
-        t64 = time.perf_counter() - t0
+        fp64 = {}
+        for name, drv in (("fp64", "default"), ("fp64_device_engine", "device")):
+            g.set_minimizer(drv)
+            t0 = time.perf_counter()
+            r = g.minimize(X, **(dict(kw, max_it=fp64_cap) if fp64_cap else kw))
+            fp64[name] = (r, time.perf_counter() - t0)
+        g.set_minimizer("default")
         g.set_precision("mixed")
         runs = {}
-        for name, polish in (("mixed_no_polish", 0), ("mixed", 1)):
-            kwr = dict(kw)
+        for name, polish, gt in (("mixed_no_polish", 0, gatol), ("mixed", 1, gatol),
+                                 ("mixed_no_polish_gatol_mixed", 0, gatol_mixed)):
+            kwr = dict(kw, gatol=gt)
             if polish and polish_cap:
                 kwr["max_it"] = runs["mixed_no_polish"][0].iters + polish_cap
             t0 = time.perf_counter()
@@ -225,26 +250,36 @@ def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0, po
             fv, gv = g.eval(r.X)
             f64_at[name] = fv
             g64_at[name] = float(np.linalg.norm(gv))
-    out["fp64"] = {"seconds": t64, "iters": r64.iters, "nfev": r64.nfev, "reason": r64.reason, "gnorm": r64.gnorm,
-                   "sigma_range_A": [float(r64.X[3::4].min()), float(r64.X[3::4].max())],
-                   "f": r64.fmin, "seconds_per_iter": t64 / max(r64.iters, 1)}
+    r64, t64 = fp64["fp64"]
+    for name, (r, t) in fp64.items():
+        out[name] = {"seconds": t, "iters": r.iters, "nfev": r.nfev, "reason": r.reason, "gnorm": r.gnorm,
+                     "sigma_range_A": [float(r.X[3::4].min()), float(r.X[3::4].max())], "f": r.fmin,
+                     "seconds_per_iter": t / max(r.iters, 1)}
+    r64e = fp64["fp64_device_engine"][0]
+    dq, ds = state_err(r64.X, r64e.X)
+    out["fp64_vs_fp64_spread"] = {"free_entropy_rel": abs(r64.fmin - r64e.fmin) / abs(r64.fmin),
+                                  "max_position_A": dq, "max_sigma_A": ds,
+                                  "what": "FP64 host-driven vs FP64 device-engine minimum (two summation orders)"}
     if fp64_cap:
         need = runs["mixed_no_polish"][0].iters
         out["fp64"].update(capped_at_iters=fp64_cap, extrapolated_seconds=t64 / max(r64.iters, 1) * need,
                            extrapolation="FP64 seconds per iteration x iterations of the mixed phase (a low "
-                                         "estimate: at 12^3 cells the FP64 run needed 1.7x the mixed phase's "
-                                         "iterations)")
+                                         "estimate)")
     t64_ref = out["fp64"].get("extrapolated_seconds", t64)
+    t64_best = min(t64_ref, fp64["fp64_device_engine"][1]) if not fp64_cap else t64_ref
     for name, (r, t) in runs.items():
-        dq = float(np.abs(r.X.reshape(-1, 4)[:, :3] - r64.X.reshape(-1, 4)[:, :3]).max())
-        ds = float(np.abs(r.X.reshape(-1, 4)[:, 3] - r64.X.reshape(-1, 4)[:, 3]).max())
-        out[name] = {"seconds": t, "iters": r.iters, "mixed_iters": r.mixed_iters, "fp64_polish_iters": r.fp64_iters,
+        out[name] = {"seconds": t, "gatol": kw["gatol"] if name != "mixed_no_polish_gatol_mixed" else gatol_mixed,
+                     "iters": r.iters, "mixed_iters": r.mixed_iters, "fp64_polish_iters": r.fp64_iters,
                      "sigma_range_A": [float(r.X[3::4].min()), float(r.X[3::4].max())],
                      "mixed_phase_gnorm": r.mixed_gnorm, "nfev": r.nfev, "reason": r.reason, "gnorm": r.gnorm,
-                     "fp64_gnorm_at_result": g64_at[name], "speedup_vs_fp64": t64_ref / t}
+                     "fp64_gnorm_at_result": g64_at[name], "speedup_vs_fp64": t64_ref / t,
+                     "speedup_vs_fastest_fp64": t64_best / t}
         if not fp64_cap:
+            dq, ds = state_err(r.X, r64.X)
             out[name]["vs_fp64_minimum"] = {"free_entropy_rel": abs(f64_at[name] - r64.fmin) / abs(r64.fmin),
-                                            "max_position_A": dq, "max_sigma_A": ds}
+                                            "max_position_A": dq, "max_sigma_A": ds,
+                                            "fp64_vs_fp64_spread_position_A": out["fp64_vs_fp64_spread"][
+                                                "max_position_A"]}
         else:
             out[name]["free_entropy_fp64_at_result"] = f64_at[name]
     return out
@@ -467,6 +502,12 @@ def run_batch_case(args):
 
 
 def run_reference(args):
+    """The reference's CPU path on this host's cores: the oracle restatement
+    (pinned bit for bit to the reference's own hot-path sources) with the
+    reference's redundant finite-difference calls, OpenMP over sites, on the
+    full 262,144-site workload; one objective+gradient evaluation per step.
+    Loads no library of this repository: the lattice comes from the
+    oracle's own generator."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
@@ -474,14 +515,11 @@ def run_reference(args):
 
     O.build(ref=False)
     threads = os.cpu_count() or 1
-    w = dict(WORKLOAD, ncell=12)
-    import a2c_gb300 as A
-
-    X, xH, _, box, nPd, nH = A.lattice_fcc(w["ncell"], periodic=w["periodic"], pos_std=w["pos_std"],
-                                           sigma=w["sigma"], x_center=w["x_center"], x_half=w["x_half"],
-                                           seed=w["seed"])
-    pb = O.Problem(nPd, nH, box=box, periodic=w["periodic"])
+    X, xH, _, box, nPd, nH = workload_lattice()
+    pb = O.Problem(nPd, nH, box=box, periodic=WORKLOAD["periodic"])
+    t0 = time.perf_counter()
     off, nbr, *_ = O.neighbors(pb, X)
+    nbr_s = time.perf_counter() - t0
     for _ in range(args.warmup):
         O.evaluate(pb, X, xH, off, nbr, mode=1, threads=threads)
     times = []
@@ -491,16 +529,18 @@ def run_reference(args):
         times.append(time.perf_counter() - t0)
     tot = sum(times)
     value = (nPd + nH) * args.steps / tot
-    sample = (f"{w['ncell']}x{w['ncell']}x{w['ncell']}-cell sample ({nPd + nH} sites) of the workload, "
-              f"one objective+gradient evaluation per step")
+    sample = (f"the full workload ({nPd + nH} sites), one objective+gradient evaluation per step, "
+              f"{threads} OpenMP threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict({"sample_sites": nPd + nH}),
+            "config": config_dict({"parallelism": "host cores", "same_workload": True}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "neighbor_build_s": nbr_s,
             "note": "the reference's CPU path: the oracle restatement (bit-exact with the reference's own "
-                    "sources where those compile) with its redundant FD calls, OpenMP over sites"}
+                    "sources where those compile) with its redundant FD calls, OpenMP over sites; the "
+                    "reference itself needs PETSc and MPI, absent here"}
     print(json.dumps(line))
     return 0
 
@@ -707,13 +747,13 @@ def run_ours(args):
         threads = os.cpu_count() or 1
         v, n, sites = cpu_sample(threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"12x12x12-cell sample ({sites} sites) of the workload, {n} evaluations, "
-                         f"oracle with the reference's arithmetic and redundant FD calls, OpenMP"}
+               "sample": f"{n} evaluations of the full workload ({sites} sites), oracle with the reference's "
+                         f"arithmetic and redundant FD calls, OpenMP"}
 
     g.close()
     ttm = None
     if world == 1 and args.ttm_cells > 0:
-        ttm = time_to_minimum(args.ttm_cells, 1e-6, dev)
+        ttm = time_to_minimum(args.ttm_cells, args.ttm_gatol, dev)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_time_mixed * 1e3 / args.steps, "higher_is_better": True,
@@ -780,8 +820,11 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
-    ap.add_argument("--ttm-cells", type=int, default=12,
+    ap.add_argument("--ttm-cells", type=int, default=32,
                     help="time-to-minimum leg on a cells^3 nucleus lattice (0 = skip; 64 = the full 2,097,152 sites)")
+    ap.add_argument("--ttm-gatol", type=float, default=1e-5,
+                    help="gradient-norm tolerance both forms run to in the time-to-minimum leg (the FP64 form's "
+                         "finite-difference gradient cannot go much below 5e-6 at 262,144 sites)")
     ap.add_argument("--case", choices=["bench", "profile", "ttm", "dmd", "batch"], default="bench",
                     help="profile: the small untimed case used for ncu captures")
     ap.add_argument("--case-cells", type=int, default=40)
@@ -809,7 +852,7 @@ def main():
     if args.case == "batch":
         return run_batch_case(args)
     if args.case == "ttm":
-        print(json.dumps({"time_to_minimum": time_to_minimum(args.ttm_cells, 1e-6, dist_env()[2],
+        print(json.dumps({"time_to_minimum": time_to_minimum(args.ttm_cells, args.ttm_gatol, dist_env()[2],
                                                              args.ttm_fp64_cap, args.ttm_polish_cap)}))
         return 0
     if args.warmup < 3:

@@ -37,7 +37,13 @@ enum {
   A2C_ERR_NONFINITE = 5,          /* NaN/Inf in an input or a result */
   A2C_ERR_STATE = 6,              /* call order violated (e.g. no neighbors) */
   A2C_ERR_TIMEOUT = 7,            /* a bounded device wait gave up */
-  A2C_ERR_NO_DEVICE = 8           /* no usable CUDA device */
+  A2C_ERR_NO_DEVICE = 8,          /* no usable CUDA device */
+  A2C_ERR_LISTS_STALE = 9         /* mixed form: since the neighbor lists were
+                                     built a site moved so far in a free
+                                     (non-periodic) direction that a listed
+                                     pair could leave the form's fixed-point
+                                     span (more than (32 A - reach) / 2, reach
+                                     = the lists' cutoff); rebuild the lists */
 };
 
 /* Arithmetic forms of the evaluator. */
@@ -222,12 +228,17 @@ a2c_status a2c_mixed_table_eval(int which, const double *x, int64_t n, double *v
  * evaluation of each candidate in milliseconds. */
 a2c_status a2c_gpp_autotune(a2c_gpp_ctx *ctx, int reps, int *tps, float *ms);
 
-/* Mixed-precision minimization (a2c_gpp_minimize, a2c_gpp_dmd_run) runs
- * device-driven by default: each L-BFGS iteration is one CUDA-graph replay
- * of the batched engine with this context as its only instance (global sums
- * in the per-instance chunk order).  host_loop = 1 selects the host-driven
- * loop instead (the FP64 plain form always uses it). */
-a2c_status a2c_gpp_set_minimizer(a2c_gpp_ctx *ctx, int host_loop);
+/* Which L-BFGS driver a2c_gpp_minimize and a2c_gpp_dmd_run use.
+ * A2C_MINIMIZER_DEFAULT: mixed precision device-driven -- each L-BFGS
+ * iteration is one CUDA-graph replay of the batched engine with this
+ * context as its only instance (global sums in the per-instance chunk
+ * order) -- and the FP64 plain form host-driven (its reductions replayed
+ * bit for bit by the oracle).  A2C_MINIMIZER_HOST: the host-driven loop for
+ * both forms.  A2C_MINIMIZER_DEVICE: the device-driven engine for both
+ * forms (for FP64, the same minimization in the engine's summation order).
+ * The value 1 keeps its earlier meaning (host_loop = 1). */
+enum { A2C_MINIMIZER_DEFAULT = 0, A2C_MINIMIZER_HOST = 1, A2C_MINIMIZER_DEVICE = 2 };
+a2c_status a2c_gpp_set_minimizer(a2c_gpp_ctx *ctx, int mode);
 
 /* Allocation-free mixed-precision evaluation.  No counterpart in the
  * reference: it is for callers that cannot allocate device memory while they

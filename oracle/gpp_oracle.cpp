@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <random>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -1029,6 +1030,69 @@ int orc_minimize(const orc_params *p, double *X, const double *xH, const int64_t
   *nfev_out = nfev;
   *gnorm_out = gnorm;
   *reason = why;
+  return 0;
+}
+
+int orc_lattice_fcc(const int ncell[3], double a, double pos_std, double sigma_lo, double sigma_hi, int x_mode,
+                    double x_center, double x_half, double x_matrix, double x_nucleus, double nucleus_radius,
+                    double interface_width, double xLb, double xUb, uint64_t seed, double *X, double *xH,
+                    int *surface) {
+  if (!ncell || !X || ncell[0] < 1 || ncell[1] < 1 || ncell[2] < 1 || !(a > 0.0) || pos_std < 0.0) return -1;
+  const int64_t nx = ncell[0], ny = ncell[1], nz = ncell[2];
+  const int64_t half = 4 * nx * ny * nz, N = 2 * half;
+  // lattice point of site s: species s / half, cell (s % half) / 4 in
+  // z-major order, basis vector (s % half) % 4
+  static const double basis[2][4][3] = {{{0.0, 0.0, 0.0}, {0.0, 0.5, 0.5}, {0.5, 0.0, 0.5}, {0.5, 0.5, 0.0}},
+                                        {{0.5, 0.0, 0.0}, {0.0, 0.5, 0.0}, {0.0, 0.0, 0.5}, {0.5, 0.5, 0.5}}};
+  auto lattice_point = [&](int64_t s, double q[3]) {
+    const int sp = s >= half ? 1 : 0;
+    const int64_t r = s - sp * half, cell = r / 4;
+    const int b = (int)(r % 4);
+    const int64_t cx = cell % nx, cy = (cell / nx) % ny, cz = cell / (nx * ny);
+    q[0] = a * ((double)cx + basis[sp][b][0]);
+    q[1] = a * ((double)cy + basis[sp][b][1]);
+    q[2] = a * ((double)cz + basis[sp][b][2]);
+  };
+  std::mt19937_64 rng(seed);
+  auto uniform = [&]() { return (double)(rng() >> 11) * (1.0 / 9007199254740992.0); };
+  double pending = 0.0;
+  bool have_pending = false;
+  auto normal = [&]() {
+    if (have_pending) {
+      have_pending = false;
+      return pending;
+    }
+    const double u1 = 1.0 - uniform(), u2 = uniform();
+    const double rad = std::sqrt(-2.0 * std::log(u1)), ang = 6.283185307179586 * u2;
+    pending = rad * std::sin(ang);
+    have_pending = true;
+    return rad * std::cos(ang);
+  };
+  for (int64_t s = 0; s < N; ++s) {
+    double q[3];
+    lattice_point(s, q);
+    for (int d = 0; d < 3; ++d) X[4 * s + d] = q[d] + pos_std * normal();
+  }
+  for (int64_t s = 0; s < N; ++s)
+    X[4 * s + 3] = sigma_hi > sigma_lo ? sigma_lo + (sigma_hi - sigma_lo) * uniform() : sigma_lo;
+  const double centre[3] = {0.5 * a * (double)nx, 0.5 * a * (double)ny, 0.5 * a * (double)nz};
+  for (int64_t h = 0; h < half; ++h) {
+    double q[3];
+    lattice_point(half + h, q);
+    if (xH) {
+      double x;
+      if (x_mode == 1) {
+        const double dx = q[0] - centre[0], dy = q[1] - centre[1], dz = q[2] - centre[2];
+        const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+        x = x_matrix + (x_nucleus - x_matrix) * 0.5 * (1.0 - std::tanh((r - nucleus_radius) / interface_width));
+        x += x_half * (2.0 * uniform() - 1.0);
+      } else {
+        x = x_center + x_half * (2.0 * uniform() - 1.0);
+      }
+      xH[h] = std::min(std::max(x, xLb), xUb);
+    }
+    if (surface) surface[h] = q[2] < 1e-6 ? 1 : 0;
+  }
   return 0;
 }
 

@@ -118,6 +118,24 @@ int orc_minimize(const orc_params *p, double *X, const double *xH,
                  int nthreads, double *fmin, int *iters, int *nfev,
                  double *gnorm, int *reason);
 
+/* The seeded synthetic lattices of the benchmark configurations, written
+ * independently of the library's generator so that CPU baselines need not
+ * load the library: fcc cells of edge a visited z, y, x (slowest to
+ * fastest), Pd basis (0,0,0) (0,1/2,1/2) (1/2,0,1/2) (1/2,1/2,0) then the
+ * octahedral H basis (1/2,0,0) (0,1/2,0) (0,0,1/2) (1/2,1/2,1/2), all Pd
+ * sites first; one std::mt19937_64(seed) stream drawn in this order: three
+ * Box-Muller normals per site for the positions (pairs from u1 = 1 - U,
+ * u2 = U with U = (draw >> 11) / 2^53, cosine first), then one uniform per
+ * site for sigma when sigma_hi > sigma_lo, then one uniform per H site for
+ * the occupancy jitter.  x_mode 0: x = x_center + x_half (2U - 1);
+ * x_mode 1: a tanh nucleus profile about the box centre plus the jitter;
+ * clamped to [xLb, xUb].  surface[h] = 1 for H sites of the z = 0 layer.
+ * Returns 0, or -1 for invalid arguments. */
+int orc_lattice_fcc(const int ncell[3], double a, double pos_std, double sigma_lo, double sigma_hi, int x_mode,
+                    double x_center, double x_half, double x_matrix, double x_nucleus, double nucleus_radius,
+                    double interface_width, double xLb, double xUb, uint64_t seed, double *X, double *xH,
+                    int *surface);
+
 #ifdef __cplusplus
 }
 #endif

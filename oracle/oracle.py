@@ -81,6 +81,7 @@ def olib() -> C.CDLL:
         L.orc_macro_results.restype = None
         L.orc_minimize.argtypes = [C.POINTER(OrcParams), P, P, P, P, C.POINTER(OrcLbfgs), I, C.POINTER(D),
                                    C.POINTER(I), C.POINTER(I), C.POINTER(D), C.POINTER(I)]
+        L.orc_lattice_fcc.argtypes = [P, D, D, D, D, I, D, D, D, D, D, D, D, D, C.c_uint64, P, P, P]
         _olib = L
     return _olib
 
@@ -169,6 +170,29 @@ class Problem:
     @property
     def coe(self) -> np.ndarray:
         return np.array(list(self.p.coe_Pd) + list(self.p.coe_H), dtype=np.float64)
+
+
+def lattice_fcc(ncell, *, a: float = 3.89, periodic=(1, 1, 1), pos_std: float = 0.0, sigma=(0.1, 0.1),
+                x_mode: int = 0, x_center: float = 0.05, x_half: float = 0.0, x_matrix: float = 0.02,
+                x_nucleus: float = 0.6, nucleus_radius: float = 80.0, interface_width: float = 5.0,
+                xLb: float = 1e-3, xUb: float = 1.0 - 1e-16, seed: int = 1):
+    """The seeded benchmark lattice from the oracle's own generator
+    (orc_lattice_fcc; the library's a2c_lattice_fcc draws the same values):
+    (X, xH, surface, box, nPd, nH)."""
+    if isinstance(ncell, int):
+        ncell = (ncell, ncell, ncell)
+    nc = np.array([int(c) for c in ncell], dtype=np.int32)
+    nPd = nH = 4 * int(nc[0]) * int(nc[1]) * int(nc[2])
+    X = np.empty(4 * (nPd + nH))
+    xH = np.empty(nH)
+    surf = np.empty(nH, dtype=np.int32)
+    rc = olib().orc_lattice_fcc(_p(nc), a, pos_std, float(sigma[0]), float(sigma[1]), int(x_mode), x_center, x_half,
+                                x_matrix, x_nucleus, nucleus_radius, interface_width, xLb, xUb, int(seed), _p(X),
+                                _p(xH), _p(surf))
+    if rc != 0:
+        raise ValueError("orc_lattice_fcc: invalid arguments")
+    box = tuple(float(ncell[d]) * a for d in range(3))
+    return X, xH, surf, box, nPd, nH
 
 
 def nthreads() -> int:

@@ -24,19 +24,24 @@ TOL_F = 1e-11
 TOL_G = 1e-11
 
 CASES = {
-    # name: (ncell, periodic, pos_std, sigma range, x_center, x_half, seed)
+    # name: (ncell, periodic, pos_std, sigma range, x_center, x_half, seed[, T])
     "free3": ((3, 3, 3), (0, 0, 0), 0.02, (0.10, 0.10), 0.05, 0.01, 1),
     "config1_6cube": ((6, 6, 6), (1, 1, 1), 0.02, (0.10, 0.10), 0.05, 0.01, 1),
     "slab_4x5x6": ((4, 5, 6), (1, 1, 0), 0.03, (0.08, 0.14), 0.15, 0.15, 7),
     "config2_16cube": ((16, 16, 16), (1, 1, 1), 0.03, (0.08, 0.14), 0.15, 0.15, 2),
+    # the evaluator-throughput state at full size: 32^3 cells, 262,144 sites
+    "config2_32cube": ((32, 32, 32), (1, 1, 1), 0.03, (0.08, 0.14), 0.15, 0.15, 2),
+    # the coupled-DMD geometry at a reduced edge: periodic x, y, free
+    # surfaces in z, x = 0.01, T = 400 K (24,576 sites)
+    "config5_slab_16x16x12": ((16, 16, 12), (1, 1, 0), 0.02, (0.10, 0.10), 0.01, 0.0, 5, 400.0),
 }
 
 
 def make(case):
-    ncell, per, ps, sg, xc, xh, seed = CASES[case]
+    ncell, per, ps, sg, xc, xh, seed, *T = CASES[case]
     X, xH, surf, box, nPd, nH = A.lattice_fcc(ncell, periodic=per, pos_std=ps, sigma=sg, x_center=xc, x_half=xh,
                                              seed=seed)
-    pb = O.Problem(nPd, nH, box=box, periodic=per)
+    pb = O.Problem(nPd, nH, box=box, periodic=per, T=T[0] if T else 300.0)
     return X, xH, surf, box, per, nPd, nH, pb
 
 
@@ -84,7 +89,7 @@ def test_objective_gradient_fp64(gpu, case):
     f_ref, G_ref, rho_ref, _ = O.evaluate(pb, X, xH, off, nbr, mode=1)
     with O.arithmetic("device"):
         f_dev, G_dev, rho_dev, _ = O.evaluate(pb, X, xH, off, nbr, mode=1)
-    with gpp(nPd, nH, box, per) as g:
+    with gpp(nPd, nH, box, per, T=pb.p.T) as g:
         g.set_occupancy(xH)
         g.build_neighbors(X)
         f, G = g.eval(X)
@@ -187,6 +192,29 @@ def test_diffusion_conserves_h(gpu):
         x = g.diffuse(1e-14, 1e13, 0.23, 1e-6, 1 - 1e-16, gamma, np.zeros(nH, np.int32), xH)
     assert abs(x.sum() - xH.sum()) < 1e-10 * xH.sum()
     assert np.abs(x - xH).max() > 1e-6
+
+
+@pytest.mark.parametrize("case", ["free3", "config1_6cube"])
+def test_minimize_fp64_device_engine_matches_oracle(gpu, case):
+    """The FP64 plain form minimized by the device-driven engine
+    (A2C_MINIMIZER_DEVICE, one-instance batch) reproduces the oracle's
+    minimization in the engine's summation order (chunks of 2048 terms)
+    bit for bit: iterations, evaluations, reason, f and X."""
+    X, xH, surf, box, per, nPd, nH, pb = make(case)
+    off, nbr, *_ = O.neighbors(pb, X)
+    kw = dict(m=5, max_it=400, gatol=1e-6)
+    with O.arithmetic("device"), O.reduction("batch"):
+        r_ref = O.minimize(pb, X, xH, off, nbr, **kw)
+    with gpp(nPd, nH, box, per) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        g.set_minimizer("device")
+        r = g.minimize(X, **kw)
+    print(f"oracle: it={r_ref['iters']} fev={r_ref['nfev']} reason={r_ref['reason']}; "
+          f"engine: it={r.iters} fev={r.nfev} reason={r.reason}")
+    assert r_ref["reason"] == r.reason and r_ref["iters"] == r.iters and r_ref["nfev"] == r.nfev
+    assert r.fmin == r_ref["fmin"]
+    assert np.array_equal(r.X, r_ref["X"])
 
 
 @pytest.mark.parametrize("case", ["free3", "config1_6cube"])
