@@ -227,6 +227,24 @@ class Gpp:
         N.check(self._L.a2c_gpp_autotune(self._h, int(reps), C.byref(t), ms), "a2c_gpp_autotune")
         return t.value, {k: float(v) for k, v in zip((1, 2, 4, 8), ms)}
 
+    def set_tile(self, tps: int = 0, rho_block: int = 0, grad_block: int = 0) -> None:
+        """Tile of the mixed pair kernels (a2c_gpp_set_tile; 0 = the library's choice)."""
+        N.check(self._L.a2c_gpp_set_tile(self._h, int(tps), int(rho_block), int(grad_block)), "a2c_gpp_set_tile")
+
+    def tile(self) -> tuple[int, int, int]:
+        """(threads per site, pass-1 block, pass-2 block) in use (a2c_gpp_get_tile)."""
+        t = (C.c_int * 3)()
+        N.check(self._L.a2c_gpp_get_tile(self._h, t), "a2c_gpp_get_tile")
+        return tuple(int(v) for v in t)
+
+    def autotune_tile(self, reps: int = 3) -> tuple[tuple[int, int, int], list]:
+        """Tile chosen by the library's tuner at the current state (set on
+        the context) and the candidates as (tile, ms) in the order timed."""
+        t = (C.c_int * 3)()
+        ms = (C.c_float * 10)()
+        N.check(self._L.a2c_gpp_autotune_tile(self._h, int(reps), t, ms), "a2c_gpp_autotune_tile")
+        return tuple(int(v) for v in t), _tile_candidates(ms)
+
     def snapshot_async(self, desc, frame: int, time: float, X0=None, gamma=None, siteid=None, tag=None) -> None:
         """Writes the context's current state (a2c_gpp_snapshot_async)."""
         X0, gamma = _opt(X0, np.float64, 4 * self.N), _opt(gamma, np.float64, self.nH)
@@ -298,14 +316,16 @@ class Gpp:
 
     def dmd_run(self, X, xH, gamma, full_H, bd_sites, surf_sites, nsteps: int, *, dt: float, nu: float, Qm: float,
                 x_bd: float, gamma_bd: float, xLb: float = 1e-3, xUb: float = 1.0 - 1e-16,
-                neighbor_update: bool = False, **lbfgs) -> dict:
-        """nsteps DMD outer steps on the device (a2c_gpp_dmd_run)."""
+                neighbor_update: bool = False, host_steps: bool = False, **lbfgs) -> dict:
+        """nsteps DMD outer steps on the device (a2c_gpp_dmd_run); host_steps
+        sequences every step from the host instead of one CUDA graph."""
         dp = N.DmdParams()
         self._L.a2c_lbfgs_default_params(C.byref(dp.lbfgs))
         for k, v in lbfgs.items():
             setattr(dp.lbfgs, k, v)
         dp.dt, dp.nu, dp.Qm, dp.xLb, dp.xUb, dp.x_bd, dp.gamma_bd = dt, nu, Qm, xLb, xUb, x_bd, gamma_bd
         dp.neighbor_update = int(bool(neighbor_update))
+        dp.host_steps = int(bool(host_steps))
         X = _f64(X, 4 * self.N).copy()
         xH = _f64(xH, self.nH).copy()
         g = _f64(gamma, self.nH).copy()
@@ -443,6 +463,24 @@ class Batch:
         N.check(self._L.a2c_gpp_batch_autotune(self._h, N.ptr(_f64(X, 4 * self.N)), int(reps), C.byref(t), ms),
                 "a2c_gpp_batch_autotune")
         return t.value, {k: float(v) for k, v in zip((1, 2, 4, 8), ms)}
+
+    def set_tile(self, tps: int = 0, rho_block: int = 0, grad_block: int = 0) -> None:
+        N.check(self._L.a2c_gpp_batch_set_tile(self._h, int(tps), int(rho_block), int(grad_block)),
+                "a2c_gpp_batch_set_tile")
+
+    def tile(self) -> tuple[int, int, int]:
+        t = (C.c_int * 3)()
+        N.check(self._L.a2c_gpp_batch_get_tile(self._h, t), "a2c_gpp_batch_get_tile")
+        return tuple(int(v) for v in t)
+
+    def autotune_tile(self, X, reps: int = 3) -> tuple[tuple[int, int, int], list]:
+        """Tile chosen by the library's tuner on the whole batch at X, and the
+        candidates as (tile, ms) in the order timed."""
+        t = (C.c_int * 3)()
+        ms = (C.c_float * 10)()
+        N.check(self._L.a2c_gpp_batch_autotune_tile(self._h, N.ptr(_f64(X, 4 * self.N)), int(reps), t, ms),
+                "a2c_gpp_batch_autotune_tile")
+        return tuple(int(v) for v in t), _tile_candidates(ms)
 
     def split(self, X) -> list[np.ndarray]:
         """Per-instance views of a concatenated 4N array."""
@@ -781,6 +819,26 @@ def lattice_fcc(ncell, *, a: float = 3.89, periodic=(1, 1, 1), pos_std: float = 
     N.check(N.lib().a2c_lattice_fcc(C.byref(sp), N.ptr(X), N.ptr(xH), N.ptr(surf)), "a2c_lattice_fcc")
     box = tuple(float(ncell[d]) * a for d in range(3))
     return X, xH, surf, box, nPd, nH
+
+
+def _tile_candidates(ms) -> list:
+    """The tuner's ten candidates in the order it times them (threads per
+    site at 256-thread blocks, then the pass-1 block, then the pass-2 block;
+    the later stages at the earlier stages' winners) with their ms."""
+    ms = [float(v) for v in ms]
+    tps = (1, 2, 4, 8)
+    t1 = tps[int(np.argmin(ms[0:4]))]
+    best = min(range(4), key=lambda k: ms[k])
+    cands = [(q, 256, 256) for q in tps]
+    rb = (256, 512, 768)
+    cands += [(t1, q, 256) for q in rb]
+    b_ms = ms[best]
+    r1 = 256
+    for k, q in enumerate(rb):
+        if ms[4 + k] < b_ms:
+            b_ms, r1 = ms[4 + k], q
+    cands += [(t1, r1, q) for q in (128, 256, 512)]
+    return list(zip(cands, ms))
 
 
 def batch_workload(n: int = 256, edge=(4, 16), T=(200.0, 600.0), x_mean=(0.01, 0.70), x_jitter: float = 0.02,

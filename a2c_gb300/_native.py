@@ -116,7 +116,7 @@ class LatticeSites(C.Structure):
 class DmdParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("nu", C.c_double), ("Qm", C.c_double), ("xLb", C.c_double),
                 ("xUb", C.c_double), ("x_bd", C.c_double), ("gamma_bd", C.c_double), ("lbfgs", LbfgsParams),
-                ("neighbor_update", C.c_int)]
+                ("neighbor_update", C.c_int), ("host_steps", C.c_int)]
 
 
 _lib = None
@@ -205,6 +205,12 @@ def lib() -> C.CDLL:
         "a2c_gpp_batch_stats": (I, [P, C.POINTER(I), C.POINTER(D)]),
         "a2c_gpp_batch_autotune": (I, [P, P, I, C.POINTER(I), P]),
         "a2c_gpp_autotune": (I, [P, I, C.POINTER(I), P]),
+        "a2c_gpp_set_tile": (I, [P, I, I, I]),
+        "a2c_gpp_get_tile": (I, [P, P]),
+        "a2c_gpp_autotune_tile": (I, [P, I, P, P]),
+        "a2c_gpp_batch_set_tile": (I, [P, I, I, I]),
+        "a2c_gpp_batch_get_tile": (I, [P, P]),
+        "a2c_gpp_batch_autotune_tile": (I, [P, P, I, P, P]),
         "a2c_gpp_set_minimizer": (I, [P, I]),
         "a2c_eam_analytic": (I, [I, P, C.c_int64, P, P]),
         "a2c_mixed_table_eval": (I, [I, P, C.c_int64, P, P]),
@@ -235,7 +241,8 @@ def exported_symbols() -> list[str]:
             "a2c_gpp_batch_build_neighbors", "a2c_gpp_batch_set_threads_per_site", "a2c_gpp_batch_set_graphs",
             "a2c_gpp_batch_eval", "a2c_gpp_batch_minimize", "a2c_gpp_batch_stats", "a2c_gpp_batch_autotune",
             "a2c_gpp_autotune", "a2c_gpp_set_minimizer", "a2c_eam_analytic", "a2c_mixed_table_eval",
-            "a2c_lattice_fcc_device"]
+            "a2c_lattice_fcc_device", "a2c_gpp_set_tile", "a2c_gpp_get_tile", "a2c_gpp_autotune_tile",
+            "a2c_gpp_batch_set_tile", "a2c_gpp_batch_get_tile", "a2c_gpp_batch_autotune_tile"]
 
 
 class A2CError(RuntimeError):

@@ -82,6 +82,57 @@ a2c_status eval_device_impl(a2c_gpp_ctx *c, const double *dX, double *d_f, doubl
   return A2C_OK;
 }
 
+// Mean milliseconds of `reps` mixed evaluations of the context's current
+// state at tile t (after one untimed evaluation).
+a2c_status time_context_tile(a2c_gpp_ctx *c, int reps, const Tile &t, float *ms) {
+  double *d_f = c->d_red + 2 * 1024 + 8;
+  A2C_TRY(mixed_set_tile(c, t));
+  A2C_TRY(eval_device_impl(c, c->d_X, d_f, c->d_G));
+  cudaEvent_t e0, e1;
+  A2C_CUDA(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return A2C_ERR_CUDA;
+  }
+  a2c_status s = cudaEventRecord(e0, c->stream) == cudaSuccess ? A2C_OK : A2C_ERR_CUDA;
+  for (int r = 0; r < reps && !s; ++r) s = eval_device_impl(c, c->d_X, d_f, c->d_G);
+  if (!s && cudaEventRecord(e1, c->stream) != cudaSuccess) s = A2C_ERR_CUDA;
+  float t_ms = 0.0f;
+  if (!s && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&t_ms, e0, e1) != cudaSuccess))
+    s = A2C_ERR_CUDA;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t_ms / (float)reps;
+  return s;
+}
+
+a2c_status tune_tile(const std::function<a2c_status(const Tile &, float *)> &time_tile, Tile *best, float *ms) {
+  static const int tps_c[4] = {1, 2, 4, 8}, rho_c[3] = {256, 512, 768}, grad_c[3] = {128, 256, 512};
+  Tile b;
+  b.rho_block = 256;
+  b.grad_block = 256;
+  float best_ms = 0.0f;
+  int k = 0;
+  auto trial = [&](const Tile &t) -> a2c_status {
+    float v = 0.0f;
+    A2C_TRY(time_tile(t, &v));
+    if (ms) ms[k] = v;
+    ++k;
+    if (b.tps == 0 || v < best_ms) {
+      best_ms = v;
+      b = t;
+    }
+    return A2C_OK;
+  };
+  for (int q : tps_c) A2C_TRY(trial(Tile{q, 256, 256}));
+  const Tile after_tps = b;
+  for (int q : rho_c) A2C_TRY(trial(Tile{after_tps.tps, q, after_tps.grad_block}));
+  const Tile after_rho = b;
+  for (int q : grad_c) A2C_TRY(trial(Tile{after_rho.tps, after_rho.rho_block, q}));
+  *best = b;
+  return A2C_OK;
+}
+
 }  // namespace a2c
 
 using namespace a2c;
@@ -325,38 +376,61 @@ a2c_status a2c_gpp_autotune(a2c_gpp_ctx *c, int reps, int *tps_out, float *ms) {
   DeviceGuard g(c->device);
   const int saved = c->p.precision;
   c->p.precision = A2C_MIXED;
-  double *d_f = c->d_red + 2 * 1024 + 8;
-  cudaEvent_t e0, e1;
-  A2C_CUDA(cudaEventCreate(&e0));
-  A2C_CUDA(cudaEventCreate(&e1));
+  const Tile keep = mixed_tile(c);
   const int choice[4] = {1, 2, 4, 8};
   float best_ms = 0.0f;
   int best = 0;
   a2c_status s = A2C_OK;
   for (int k = 0; k < 4 && !s; ++k) {
-    s = mixed_set_threads_per_site(c, choice[k]);
-    if (!s) s = eval_device_impl(c, c->d_X, d_f, c->d_G);
-    if (!s && cudaEventRecord(e0, c->stream) != cudaSuccess) s = A2C_ERR_CUDA;
-    for (int r = 0; r < reps && !s; ++r) s = eval_device_impl(c, c->d_X, d_f, c->d_G);
-    if (!s && cudaEventRecord(e1, c->stream) != cudaSuccess) s = A2C_ERR_CUDA;
     float t = 0.0f;
-    if (!s && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
-      s = A2C_ERR_CUDA;
-    t /= (float)reps;
+    s = time_context_tile(c, reps, Tile{choice[k], keep.rho_block, keep.grad_block}, &t);
     if (ms) ms[k] = t;
     if (!s && (best == 0 || t < best_ms)) {
       best_ms = t;
       best = choice[k];
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   c->p.precision = saved;
   c->has_density = false;
-  if (!s) s = mixed_set_threads_per_site(c, best);
+  if (!s) s = mixed_set_tile(c, Tile{best, keep.rho_block, keep.grad_block});
   if (!s && tps_out) *tps_out = best;
   if (!s) s = check_status_word(c);
   return s;
+}
+
+a2c_status a2c_gpp_autotune_tile(a2c_gpp_ctx *c, int reps, int *tile, float *ms) {
+  if (!c || reps < 1 || reps > 1000) return A2C_ERR_INVALID;
+  if (!c->has_neighbors || !c->has_state) return A2C_ERR_STATE;
+  DeviceGuard g(c->device);
+  const int saved = c->p.precision;
+  c->p.precision = A2C_MIXED;
+  Tile best;
+  a2c_status s = tune_tile([&](const Tile &t, float *v) { return time_context_tile(c, reps, t, v); }, &best, ms);
+  c->p.precision = saved;
+  c->has_density = false;
+  if (!s) s = mixed_set_tile(c, best);
+  if (!s && tile) {
+    tile[0] = best.tps;
+    tile[1] = best.rho_block;
+    tile[2] = best.grad_block;
+  }
+  if (!s) s = check_status_word(c);
+  return s;
+}
+
+a2c_status a2c_gpp_set_tile(a2c_gpp_ctx *c, int tps, int rho_block, int grad_block) {
+  if (!c || !valid_tile(tps, rho_block, grad_block)) return A2C_ERR_INVALID;
+  DeviceGuard g(c->device);
+  return mixed_set_tile(c, Tile{tps, rho_block, grad_block});
+}
+
+a2c_status a2c_gpp_get_tile(a2c_gpp_ctx *c, int *tile) {
+  if (!c || !tile) return A2C_ERR_INVALID;
+  const Tile t = effective_tile(mixed_tile(c), c->N, device_sms(c->device));
+  tile[0] = t.tps;
+  tile[1] = t.rho_block;
+  tile[2] = t.grad_block;
+  return A2C_OK;
 }
 
 a2c_status a2c_gpp_set_minimizer(a2c_gpp_ctx *c, int mode) {
@@ -995,12 +1069,14 @@ a2c_status a2c_gpp_dmd_run(a2c_gpp_ctx *c, double *X, double *xH, double *gamma,
   std::vector<int> flags((size_t)nH, 0);
   for (int t = 0; t < n_surf; ++t)
     if (surf_sites[t] >= 0 && surf_sites[t] < nH) flags[(size_t)surf_sites[t]] = 1;
-  double *dg = nullptr, *dsend = nullptr, *dx = nullptr;
-  int *dfull = nullptr, *dbd = nullptr, *dsurf = nullptr;
+  double *dg = nullptr, *dsend = nullptr, *dx = nullptr, *drec = nullptr;
+  int *dfull = nullptr, *dbd = nullptr, *dsurf = nullptr, *dcnt = nullptr;
   A2C_TRY(ensure_hscratch(c, &dg, &dsend, &dx, &dfull));
   a2c_status s = A2C_OK;
   if (cudaMallocAsync((void **)&dbd, sizeof(int) * std::max(n_bd, 1), st) ||
-      cudaMallocAsync((void **)&dsurf, sizeof(int) * nH, st))
+      cudaMallocAsync((void **)&dsurf, sizeof(int) * nH, st) ||
+      cudaMallocAsync((void **)&drec, sizeof(double) * (4 * (size_t)std::max(nsteps, 1) + 2), st) ||
+      cudaMallocAsync((void **)&dcnt, sizeof(int) * 2, st))
     s = A2C_ERR_NOMEM;
   if (!s && (cudaMemcpyAsync(c->d_X, X, sizeof(double) * 4 * c->N, cudaMemcpyHostToDevice, st) ||
              cudaMemcpyAsync(c->d_occ + c->p.nPd, xH, sizeof(double) * nH, cudaMemcpyHostToDevice, st) ||
@@ -1011,7 +1087,13 @@ a2c_status a2c_gpp_dmd_run(a2c_gpp_ctx *c, double *X, double *xH, double *gamma,
     s = A2C_ERR_CUDA;
   c->has_state = true;
   std::vector<double> hX;
-  for (int k = 0; k < nsteps && !s; ++k) {
+  // After an eager first step (one-time set-up, the engine), the remaining
+  // steps can run as one CUDA graph (engine_dmd_graph).
+  const bool graph = !dp->host_steps && nsteps >= 2 && !dp->neighbor_update &&
+                     ((c->p.precision == A2C_MIXED && c->host_loop == A2C_MINIMIZER_DEFAULT) ||
+                      c->host_loop == A2C_MINIMIZER_DEVICE);
+  const int eager_steps = graph ? 1 : nsteps;
+  for (int k = 0; k < eager_steps && !s; ++k) {
     double f = 0.0, gn = 0.0;
     int it = 0, fev = 0, why = 0;
     if (k > 0 && dp->neighbor_update) {  // findNeighbors + findLocalNeighbors at the current positions
@@ -1044,6 +1126,25 @@ a2c_status a2c_gpp_dmd_run(a2c_gpp_ctx *c, double *X, double *xH, double *gamma,
     if (fmin) fmin[k] = f;
     if (iters) iters[k] = it;
   }
+  if (!s && graph && engine_dmd_graph_usable(c, dp)) {
+    DmdDev dd{dg, dsend, dx, drec, drec + 4 * (size_t)nsteps, dfull, dbd, dsurf, dcnt, n_bd, n_surf};
+    s = engine_dmd_graph(c, dp, dd, eager_steps, nsteps);
+    std::vector<double> rec(4 * (size_t)nsteps);
+    int done[2] = {0, 0};
+    if (!s && (cudaMemcpyAsync(rec.data(), drec, sizeof(double) * rec.size(), cudaMemcpyDeviceToHost, st) ||
+               cudaMemcpyAsync(done, dcnt, sizeof(done), cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st)))
+      s = A2C_ERR_CUDA;
+    if (!s) s = check_status_word(c);
+    if (!s && done[0] != nsteps) s = A2C_ERR_STATE;
+    for (int k = eager_steps; k < nsteps && !s; ++k) {
+      if (xH_mean) xH_mean[k] = rec[4 * (size_t)k];
+      if (xH_interior) xH_interior[k] = rec[4 * (size_t)k + 1];
+      if (fmin) fmin[k] = rec[4 * (size_t)k + 2];
+      if (iters) iters[k] = (int)rec[4 * (size_t)k + 3];
+    }
+  } else if (!s && graph) {
+    s = A2C_ERR_STATE;
+  }
   if (!s && (cudaMemcpyAsync(X, c->d_X, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToHost, st) ||
              cudaMemcpyAsync(xH, c->d_occ + c->p.nPd, sizeof(double) * nH, cudaMemcpyDeviceToHost, st) ||
              cudaMemcpyAsync(gamma, dg, sizeof(double) * nH, cudaMemcpyDeviceToHost, st) ||
@@ -1052,6 +1153,8 @@ a2c_status a2c_gpp_dmd_run(a2c_gpp_ctx *c, double *X, double *xH, double *gamma,
   free_hscratch(c, dg, dsend, dx, dfull);
   if (dbd) cudaFreeAsync(dbd, st);
   if (dsurf) cudaFreeAsync(dsurf, st);
+  if (drec) cudaFreeAsync(drec, st);
+  if (dcnt) cudaFreeAsync(dcnt, st);
   c->has_density = false;
   if (s) return s;
   return finish(c);

@@ -678,7 +678,7 @@ struct a2c_gpp_batch {
   int B = 0;
   int device = 0;
   int precision = A2C_FP64;
-  int tps = 0;
+  Tile tile;  // the mixed pair kernels' tile (zeros: the library's choice)
   bool graphs = true;
   a2c_gpp_ctx *c = nullptr;  // the union system (evaluator buffers, lists, stream)
   std::vector<a2c_gpp_params> P;
@@ -703,7 +703,7 @@ struct a2c_gpp_batch {
   // rebuild may reallocate it)
   cudaGraphExec_t exec = nullptr;
   Cfg exec_cfg{};
-  int exec_tps = -1;
+  Tile exec_tile{-1, -1, -1};
   const void *exec_nbr = nullptr;
   const void *exec_pass2[5] = {};  // the captured pass 2: mode and its index buffers
   bool borrowed = false;  // c belongs to a context (the one-instance engine)
@@ -780,20 +780,18 @@ a2c_status plan(a2c_gpp_batch *b, const Dev &D) {
   return A2C_OK;
 }
 
-int default_tps(a2c_gpp_batch *b) {
-  return b->tps ? b->tps : default_threads_per_site(b->c->N, device_sms(b->c->device));
-}
+Tile batch_tile(a2c_gpp_batch *b) { return effective_tile(b->tile, b->c->N, device_sms(b->c->device)); }
 
 // Evaluation of every listed site at xn into gn (both forms; a form with
 // an empty list costs an empty launch).
-a2c_status eval_lists(a2c_gpp_batch *b, const double *X, double *G, int tps) {
-  A2C_TRY(mixed_eval_list(b->c, X, G, view(b, 0), tps));
+a2c_status eval_lists(a2c_gpp_batch *b, const double *X, double *G, const Tile &tile) {
+  A2C_TRY(mixed_eval_list(b->c, X, G, view(b, 0), tile));
   A2C_TRY(launch_eval64_list(b->c, X, G, view(b, 1)));
   return A2C_OK;
 }
 
 // One tick (see the file comment); the same launches whether captured or not.
-a2c_status tick(a2c_gpp_batch *b, const Dev &D, const Cfg &cf, int tps) {
+a2c_status tick(a2c_gpp_batch *b, const Dev &D, const Cfg &cf, const Tile &tps) {
   cudaStream_t s = b->c->stream;
   const int ge = chunk_grid(cf.nec), gs = chunk_grid(cf.nsc), B = cf.B;
   k_projgrad<<<ge, kBlk, 0, s>>>(D, cf);
@@ -943,26 +941,17 @@ a2c_status init_tables(a2c_gpp_batch *b, const a2c_gpp_params *params, int n, bo
   return s;
 }
 
-// The minimization of every instance; X in/out on the host or (dev) on
-// the device.  Per-instance results into the host arrays (any may be null)
-// and, when `last` is given, the per-instance records.
-a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_params *lp, double *fmin, int *iters,
-                         int *nfev, double *gnorm, int *reason, int *mixed_iters, int *fp64_iters,
-                         std::vector<Inst> *last) {
-  if (!b || !X || !lp) return A2C_ERR_INVALID;
+// Set-up of a minimization: argument checks, L-BFGS buffers, constants,
+// threads per site and the mixed form's tables (all outside any capture).
+a2c_status setup_min(a2c_gpp_batch *b, const a2c_lbfgs_params *lp, Cfg &cf, Tile &tps) {
   if (lp->m < 1 || lp->m > kMaxM || lp->max_ls < 1 || !(lp->sigma_lb > 0.0) || !(lp->init_step > 0.0) ||
       lp->stall_window < 0 || lp->stall_window > 4096 || lp->max_fev < 1)
     return A2C_ERR_INVALID;
   a2c_gpp_ctx *c = b->c;
   if (!c->has_neighbors) return A2C_ERR_STATE;
-  DeviceGuard2 dg(b->device);
-  const int64_t N = c->N;
-  if (!dev)
-    for (int64_t t = 0; t < 4 * N; ++t)
-      if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
   A2C_TRY(ensure_lbfgs(b, lp->m, lp->stall_window));
-  cudaStream_t s = c->stream;
-  Cfg cf{};
+  const int64_t N = c->N;
+  cf = Cfg{};
   cf.B = b->B;
   cf.m = lp->m;
   cf.ring = lp->m + 1;
@@ -983,8 +972,43 @@ a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_
   cf.fn_fp64 = lp->f_noise > 0.0 ? lp->f_noise : 1.0e-14;
   cf.st_mixed = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-10;
   cf.st_fp64 = lp->stall_rtol > 0.0 ? lp->stall_rtol : 1.0e-14;
-  const int tps = default_tps(b);
+  tps = batch_tile(b);
   if (b->precision == A2C_MIXED) A2C_TRY(mixed_prepare(c));
+  return A2C_OK;
+}
+
+// The launches that start a minimization from X (device or host memory):
+// iterate, projection onto the bounds, per-instance records, site lists.
+a2c_status start_min(a2c_gpp_batch *b, const Dev &D, const Cfg &cf, const double *X, bool dev) {
+  cudaStream_t s = b->c->stream;
+  A2C_CUDA(cudaMemcpyAsync(b->x, X, sizeof(double) * cf.n, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  k_project_all<<<chunk_grid((cf.n + 255) / 256), 256, 0, s>>>(b->x, cf.n, cf.lb);
+  k_init_state<<<(b->B + 127) / 128, 128, 0, s>>>(D, cf, b->precision == A2C_MIXED ? kPhaseMixed : kPhaseFp64);
+  A2C_CUDA(cudaMemsetAsync(b->listed, 0xff, sizeof(int) * b->B, s));  // -1: force a plan
+  return plan(b, D);
+}
+
+// Ticks a minimization may take at most (each tick is at least one
+// evaluation of every live instance; line searches and the polish add some).
+int64_t max_ticks_for(const a2c_lbfgs_params *lp) { return 2 * ((int64_t)lp->max_fev + 2) + 16; }
+
+// The minimization of every instance; X in/out on the host or (dev) on
+// the device.  Per-instance results into the host arrays (any may be null)
+// and, when `last` is given, the per-instance records.
+a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_params *lp, double *fmin, int *iters,
+                         int *nfev, double *gnorm, int *reason, int *mixed_iters, int *fp64_iters,
+                         std::vector<Inst> *last) {
+  if (!b || !X || !lp) return A2C_ERR_INVALID;
+  a2c_gpp_ctx *c = b->c;
+  DeviceGuard2 dg(b->device);
+  const int64_t N = c->N;
+  if (!dev)
+    for (int64_t t = 0; t < 4 * N; ++t)
+      if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
+  Cfg cf{};
+  Tile tps;
+  A2C_TRY(setup_min(b, lp, cf, tps));
+  cudaStream_t s = c->stream;
   Dev D = dev_view(b);
   cudaEvent_t e0, e1;
   A2C_CUDA(cudaEventCreate(&e0));
@@ -993,21 +1017,15 @@ a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_
   auto fail = [&](a2c_status v) {
     if (!st) st = v;
   };
-  if (cudaMemcpyAsync(b->x, X, sizeof(double) * 4 * N, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s) !=
-      cudaSuccess)
-    fail(A2C_ERR_CUDA);
   cudaEventRecord(e0, s);
-  k_project_all<<<chunk_grid((4 * N + 255) / 256), 256, 0, s>>>(b->x, 4 * N, cf.lb);
-  k_init_state<<<(b->B + 127) / 128, 128, 0, s>>>(D, cf, b->precision == A2C_MIXED ? kPhaseMixed : kPhaseFp64);
-  if (cudaMemsetAsync(b->listed, 0xff, sizeof(int) * b->B, s) != cudaSuccess) fail(A2C_ERR_CUDA);
-  if (!st) fail(plan(b, D));
+  fail(start_min(b, D, cf, X, dev));
   // the first tick (every instance's first evaluation) runs eagerly: it also
   // performs the launchers' one-time occupancy queries outside any capture
   if (!st) fail(tick(b, D, cf, tps));
   // the captured tick, reused while the configuration is unchanged
   const void *pass2[5];
   mixed_graph_key(c, pass2);
-  const bool same = b->exec && b->exec_tps == tps && b->exec_nbr == (const void *)c->d_nbr &&
+  const bool same = b->exec && b->exec_tile == tps && b->exec_nbr == (const void *)c->d_nbr &&
                     !std::memcmp(b->exec_pass2, pass2, sizeof(pass2)) && !std::memcmp(&b->exec_cfg, &cf, sizeof(Cfg));
   if (!st && b->graphs && !same) {
     if (b->exec) {
@@ -1022,13 +1040,13 @@ a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_
     if (!st && cudaGraphInstantiate(&b->exec, gr, 0) != cudaSuccess) fail(A2C_ERR_CUDA);
     if (gr) cudaGraphDestroy(gr);
     b->exec_cfg = cf;
-    b->exec_tps = tps;
+    b->exec_tile = tps;
     b->exec_nbr = c->d_nbr;
     std::memcpy(b->exec_pass2, pass2, sizeof(pass2));
   }
   // replay: K ticks, then read how many instances are left
   const int K = 8;
-  const int64_t max_ticks = 2 * ((int64_t)lp->max_fev + 2) + 2 * K;
+  const int64_t max_ticks = max_ticks_for(lp);
   int64_t ticks = 1;
   while (!st) {
     for (int k = 0; k < K; ++k) {
@@ -1039,9 +1057,12 @@ a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_
       }
     }
     ticks += K;
-    if (cudaMemcpyAsync(b->h_cnt, b->cnt, 8 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+    if (cudaMemcpyAsync(b->h_cnt, b->cnt, 7 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(b->h_cnt + 7, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
       fail(A2C_ERR_CUDA);
+    // a span-guard flag ends the minimization: its gradients could be wrong
+    if (!st && (b->h_cnt[7] & kStatusSpan)) fail(A2C_ERR_LISTS_STALE);
     if (st || b->h_cnt[kCntLeft] == 0) break;
     if (ticks >= max_ticks) {
       fail(A2C_ERR_STATE);
@@ -1055,7 +1076,10 @@ a2c_status minimize_core(a2c_gpp_batch *b, double *X, bool dev, const a2c_lbfgs_
   std::vector<Inst> hs((size_t)b->B);
   if (!st && cudaMemcpyAsync(hs.data(), b->st, sizeof(Inst) * b->B, cudaMemcpyDeviceToHost, s) != cudaSuccess)
     fail(A2C_ERR_CUDA);
+  if (cudaMemcpyAsync(b->h_cnt + 7, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    fail(A2C_ERR_CUDA);
   if (cudaStreamSynchronize(s) != cudaSuccess) fail(A2C_ERR_CUDA);
+  if (!st && (b->h_cnt[7] & kStatusSpan)) fail(A2C_ERR_LISTS_STALE);
   float ms = 0.0f;
   if (!st && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) b->seconds = 1e-3 * ms;
   cudaEventDestroy(e0);
@@ -1227,7 +1251,7 @@ a2c_status a2c_gpp_batch_build_neighbors(a2c_gpp_batch *b, const double *X, int 
 
 a2c_status a2c_gpp_batch_set_threads_per_site(a2c_gpp_batch *b, int tps) {
   if (!b || (tps != 0 && tps != 1 && tps != 2 && tps != 4 && tps != 8)) return A2C_ERR_INVALID;
-  b->tps = tps;
+  b->tile.tps = tps;
   return A2C_OK;
 }
 
@@ -1263,7 +1287,7 @@ a2c_status a2c_gpp_batch_eval(a2c_gpp_batch *b, const double *X, double *f, doub
   if (!st) st = plan(b, D);
   if (!st && cudaMemcpyAsync(c->d_X, X, sizeof(double) * 4 * N, cudaMemcpyHostToDevice, s) != cudaSuccess)
     st = A2C_ERR_CUDA;
-  if (!st) st = eval_lists(b, c->d_X, c->d_G, default_tps(b));
+  if (!st) st = eval_lists(b, c->d_X, c->d_G, batch_tile(b));
   if (!st) {
     k_objpart<<<chunk_grid(b->nsc), kBlk, 0, s>>>(D, cf, 1);
     k_objective<<<b->B, kBlk, 0, s>>>(D, cf, df);
@@ -1294,11 +1318,35 @@ a2c_status a2c_gpp_batch_minimize(a2c_gpp_batch *b, double *X, const a2c_lbfgs_p
 // Autotuner of the mixed form's threads per site over the whole batch at X
 // (every instance listed): each choice evaluates once untimed, then `reps`
 // times between two events; the fastest choice is kept for the batch.
-a2c_status a2c_gpp_batch_autotune(a2c_gpp_batch *b, const double *X, int reps, int *tps_out, float *ms) {
-  if (!b || !X || reps < 1 || reps > 1000) return A2C_ERR_INVALID;
+namespace {
+// Mean milliseconds of `reps` mixed evaluations of every instance at tile t
+// (the state in c->d_X, every instance listed; one untimed evaluation first).
+a2c_status time_batch_tile(a2c_gpp_batch *b, int reps, const Tile &t, float *ms) {
+  a2c_gpp_ctx *c = b->c;
+  cudaStream_t s = c->stream;
+  A2C_TRY(mixed_eval_list(c, c->d_X, c->d_G, view(b, 0), t));
+  cudaEvent_t e0, e1;
+  A2C_CUDA(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return A2C_ERR_CUDA;
+  }
+  a2c_status st = cudaEventRecord(e0, s) == cudaSuccess ? A2C_OK : A2C_ERR_CUDA;
+  for (int r = 0; r < reps && !st; ++r) st = mixed_eval_list(c, c->d_X, c->d_G, view(b, 0), t);
+  if (!st && cudaEventRecord(e1, s) != cudaSuccess) st = A2C_ERR_CUDA;
+  float v = 0.0f;
+  if (!st && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&v, e0, e1) != cudaSuccess))
+    st = A2C_ERR_CUDA;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = v / (float)reps;
+  return st;
+}
+
+// Every instance listed, X on the device: the state the tuners time.
+a2c_status tune_setup(a2c_gpp_batch *b, const double *X) {
   a2c_gpp_ctx *c = b->c;
   if (!c->has_neighbors) return A2C_ERR_STATE;
-  DeviceGuard dg(b->device);
   cudaStream_t s = c->stream;
   A2C_TRY(mixed_prepare(c));
   Dev D = dev_view(b);
@@ -1308,34 +1356,59 @@ a2c_status a2c_gpp_batch_autotune(a2c_gpp_batch *b, const double *X, int reps, i
   A2C_CUDA(cudaMemsetAsync(b->listed, 0xff, sizeof(int) * b->B, s));
   A2C_TRY(plan(b, D));
   A2C_CUDA(cudaMemcpyAsync(c->d_X, X, sizeof(double) * 4 * c->N, cudaMemcpyHostToDevice, s));
-  cudaEvent_t e0, e1;
-  A2C_CUDA(cudaEventCreate(&e0));
-  A2C_CUDA(cudaEventCreate(&e1));
+  return A2C_OK;
+}
+}  // namespace
+
+a2c_status a2c_gpp_batch_autotune(a2c_gpp_batch *b, const double *X, int reps, int *tps_out, float *ms) {
+  if (!b || !X || reps < 1 || reps > 1000) return A2C_ERR_INVALID;
+  DeviceGuard dg(b->device);
+  A2C_TRY(tune_setup(b, X));
   const int choice[4] = {1, 2, 4, 8};
   float best_ms = 0.0f;
   int best = 0;
-  a2c_status st = A2C_OK;
-  for (int k = 0; k < 4 && !st; ++k) {
-    st = mixed_eval_list(c, c->d_X, c->d_G, view(b, 0), choice[k]);
-    if (!st && cudaEventRecord(e0, s) != cudaSuccess) st = A2C_ERR_CUDA;
-    for (int r = 0; r < reps && !st; ++r) st = mixed_eval_list(c, c->d_X, c->d_G, view(b, 0), choice[k]);
-    if (!st && cudaEventRecord(e1, s) != cudaSuccess) st = A2C_ERR_CUDA;
+  for (int k = 0; k < 4; ++k) {
     float t = 0.0f;
-    if (!st && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
-      st = A2C_ERR_CUDA;
-    t /= (float)reps;
+    A2C_TRY(time_batch_tile(b, reps, Tile{choice[k], b->tile.rho_block, b->tile.grad_block}, &t));
     if (ms) ms[k] = t;
-    if (!st && (best == 0 || t < best_ms)) {
+    if (best == 0 || t < best_ms) {
       best_ms = t;
       best = choice[k];
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (st) return st;
-  b->tps = best;
+  b->tile.tps = best;
   if (tps_out) *tps_out = best;
-  return check_status_word(c);
+  return check_status_word(b->c);
+}
+
+a2c_status a2c_gpp_batch_autotune_tile(a2c_gpp_batch *b, const double *X, int reps, int *tile, float *ms) {
+  if (!b || !X || reps < 1 || reps > 1000) return A2C_ERR_INVALID;
+  DeviceGuard dg(b->device);
+  A2C_TRY(tune_setup(b, X));
+  Tile best;
+  A2C_TRY(tune_tile([&](const Tile &t, float *v) { return time_batch_tile(b, reps, t, v); }, &best, ms));
+  b->tile = best;
+  if (tile) {
+    tile[0] = best.tps;
+    tile[1] = best.rho_block;
+    tile[2] = best.grad_block;
+  }
+  return check_status_word(b->c);
+}
+
+a2c_status a2c_gpp_batch_set_tile(a2c_gpp_batch *b, int tps, int rho_block, int grad_block) {
+  if (!b || !valid_tile(tps, rho_block, grad_block)) return A2C_ERR_INVALID;
+  b->tile = Tile{tps, rho_block, grad_block};
+  return A2C_OK;
+}
+
+a2c_status a2c_gpp_batch_get_tile(a2c_gpp_batch *b, int *tile) {
+  if (!b || !tile) return A2C_ERR_INVALID;
+  const Tile t = batch_tile(b);
+  tile[0] = t.tps;
+  tile[1] = t.rho_block;
+  tile[2] = t.grad_block;
+  return A2C_OK;
 }
 
 // Ticks replayed and device seconds of the last a2c_gpp_batch_minimize.
@@ -1373,7 +1446,7 @@ a2c_status engine_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *l
     c->engine = b;
   }
   b->precision = c->p.precision;
-  b->tps = mixed_threads_per_site(c);
+  b->tile = mixed_tile(c);
   {  // the context's lists may have changed since the tables were made
     InstGeo G{};
     set_limits(b, 0, G);
@@ -1398,6 +1471,167 @@ a2c_status engine_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *l
 void engine_free(a2c_gpp_ctx *c) {
   if (c->engine) a2c_gpp_batch_destroy((a2c_gpp_batch *)c->engine);
   c->engine = nullptr;
+}
+
+// ------------------------------------------------- DMD run as one graph
+namespace {
+
+// The L-BFGS tick loop's condition: continue while an instance is live,
+// for at most max_ticks ticks (counters[1]); running out sets the timeout
+// bit instead of looping on.
+__global__ void k_tick_cond(cudaGraphConditionalHandle h, const int *cnt, int *counters, int max_ticks, int *status) {
+  const int t = counters[1] + 1;
+  counters[1] = t;
+  const bool more = cnt[kCntLeft] > 0;
+  if (more && t >= max_ticks) atomicOr(status, kStatusTimeout);
+  cudaGraphSetConditional(h, (more && t < max_ticks) ? 1u : 0u);
+}
+
+__global__ void k_set_cond(cudaGraphConditionalHandle h, unsigned v) { cudaGraphSetConditional(h, v); }
+
+// After a minimization: a trial point the line search rejected for a
+// non-finite objective is not an error (the eager engine clears the word
+// likewise); every other bit stays.
+__global__ void k_status_keep(int *status, int keep) { *status &= keep; }
+
+// End of an outer step: its records, the next step index, and the outer
+// loop's condition (more steps, and no error bit set).
+__global__ void k_dmd_record(const Inst *st, const double *macro, int *counters, double *rec, int nsteps,
+                             const int *status, int fatal, cudaGraphConditionalHandle h) {
+  const int k = counters[0];
+  rec[4 * k] = macro[0];
+  rec[4 * k + 1] = macro[1];
+  rec[4 * k + 2] = st[0].f;
+  rec[4 * k + 3] = (double)st[0].it;
+  counters[0] = k + 1;
+  counters[1] = 0;
+  cudaGraphSetConditional(h, (k + 1 < nsteps && !(*status & fatal)) ? 1u : 0u);
+}
+
+// The launches of one outer step after its minimization (minimizer.cpp:588
+// -> boundaryconditions.cpp:30 -> integrate.cpp:9 -> calculateresults.cpp:8),
+// as the host-sequenced loop issues them.
+a2c_status dmd_post(a2c_gpp_ctx *c, const a2c_dmd_params *dp, const DmdDev &dd) {
+  cudaStream_t s = c->stream;
+  const int nH = c->p.nH;
+  A2C_TRY(launch_density64(c, c->d_X));
+  A2C_TRY(launch_chem64(c, c->d_X, dp->gamma_bd, dd.send, dd.full));
+  A2C_TRY(launch_gamma_update(c, dd.send, dp->gamma_bd, dd.gamma, dd.full));
+  A2C_TRY(launch_dirichlet(c, dd.bd, dd.n_bd, dp->gamma_bd, dp->x_bd, dd.gamma, dd.full));
+  A2C_CUDA(cudaMemcpyAsync(dd.x, c->d_occ + c->p.nPd, sizeof(double) * nH, cudaMemcpyDeviceToDevice, s));
+  A2C_TRY(launch_diffuse(c, dd.gamma, dd.full, dp->dt, dp->nu, dp->Qm, dp->xLb, dp->xUb, dd.x));
+  A2C_CUDA(cudaMemcpyAsync(c->d_occ + c->p.nPd, dd.x, sizeof(double) * nH, cudaMemcpyDeviceToDevice, s));
+  return launch_macro_device(c, dd.x, dd.surf, dd.n_surf, dd.macro);
+}
+
+}  // namespace
+
+bool engine_dmd_graph_usable(const a2c_gpp_ctx *c, const a2c_dmd_params *dp) {
+  if (!c->engine || dp->neighbor_update) return false;
+  return (c->p.precision == A2C_MIXED && c->host_loop == A2C_MINIMIZER_DEFAULT) ||
+         c->host_loop == A2C_MINIMIZER_DEVICE;
+}
+
+a2c_status engine_dmd_graph(a2c_gpp_ctx *c, const a2c_dmd_params *dp, const DmdDev &dd, int first, int nsteps) {
+  a2c_gpp_batch *b = (a2c_gpp_batch *)c->engine;
+  if (!b || first >= nsteps) return b ? A2C_OK : A2C_ERR_STATE;
+  const a2c_lbfgs_params *lp = &dp->lbfgs;
+  b->precision = c->p.precision;
+  b->tile = mixed_tile(c);
+  {
+    InstGeo G{};
+    set_limits(b, 0, G);
+    A2C_CUDA(cudaMemcpy((char *)b->geo + offsetof(InstGeo, lim), G.lim, sizeof(G.lim), cudaMemcpyHostToDevice));
+  }
+  Cfg cf{};
+  Tile tps;
+  A2C_TRY(setup_min(b, lp, cf, tps));
+  const Dev D = dev_view(b);
+  cudaStream_t s = c->stream;
+  const int init[2] = {first, 0};
+  A2C_CUDA(cudaMemcpyAsync(dd.counters, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  A2C_CUDA(cudaStreamSynchronize(s));
+  const int max_ticks = (int)std::min<int64_t>(max_ticks_for(lp), 1 << 30);
+  const int fatal = kStatusBadIndex | kStatusOverflow | kStatusTimeout | kStatusNonfinite | kStatusSpan;
+
+  a2c_status st = A2C_OK;
+  auto fail = [&](a2c_status v) {
+    if (!st) st = v;
+  };
+  auto cuda = [&](cudaError_t e) {
+    if (e != cudaSuccess) fail(cuda_status(e));
+  };
+  cudaGraph_t G = nullptr;
+  cudaGraphExec_t E = nullptr;
+  cuda(cudaGraphCreate(&G, 0));
+  // the loop over outer steps
+  cudaGraphConditionalHandle hStep = 0, hTick = 0;
+  cudaGraph_t bodyStep = nullptr, bodyTick = nullptr;
+  if (!st) cuda(cudaGraphConditionalHandleCreate(&hStep, G, 1, cudaGraphCondAssignDefault));
+  if (!st) {
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = hStep;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t n = nullptr;
+    cuda(cudaGraphAddNode(&n, G, nullptr, nullptr, 0, &np));
+    if (!st) bodyStep = np.conditional.phGraph_out[0];
+  }
+  if (!st) cuda(cudaGraphConditionalHandleCreate(&hTick, bodyStep, 1, cudaGraphCondAssignDefault));
+  // one outer step: start the minimization, the tick loop, the rest
+  if (!st && cudaStreamBeginCaptureToGraph(s, bodyStep, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                 cudaSuccess) {
+    fail(start_min(b, D, cf, c->d_X, true));
+    k_set_cond<<<1, 1, 0, s>>>(hTick, 1u);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    if (!st) cuda(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd));
+    if (!st) {
+      cudaGraphNodeParams tp{};
+      tp.type = cudaGraphNodeTypeConditional;
+      tp.conditional.handle = hTick;
+      tp.conditional.type = cudaGraphCondTypeWhile;
+      tp.conditional.size = 1;
+      cudaGraphNode_t n = nullptr;
+      cuda(cudaGraphAddNode(&n, cg, deps, nullptr, nd, &tp));
+      if (!st) {
+        bodyTick = tp.conditional.phGraph_out[0];
+        cuda(cudaStreamUpdateCaptureDependencies(s, &n, nullptr, 1, cudaStreamSetCaptureDependencies));
+      }
+    }
+    if (!st) {
+      k_status_keep<<<1, 1, 0, s>>>(c->d_status, ~(int)kStatusNonfinite);
+      cuda(cudaMemcpyAsync(c->d_X, b->x, sizeof(double) * cf.n, cudaMemcpyDeviceToDevice, s));
+      fail(dmd_post(c, dp, dd));
+      k_dmd_record<<<1, 1, 0, s>>>(D.st, dd.macro, dd.counters, dd.rec, nsteps, c->d_status, fatal, hStep);
+      cuda(cudaGetLastError());
+    }
+    cudaGraph_t out = nullptr;
+    cuda(cudaStreamEndCapture(s, &out));
+  } else if (!st) {
+    fail(A2C_ERR_CUDA);
+  }
+  // the tick loop's body: one L-BFGS tick and the loop condition
+  if (!st && cudaStreamBeginCaptureToGraph(s, bodyTick, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                 cudaSuccess) {
+    fail(tick(b, D, cf, tps));
+    k_tick_cond<<<1, 1, 0, s>>>(hTick, b->cnt, dd.counters, max_ticks, c->d_status);
+    cuda(cudaGetLastError());
+    cudaGraph_t out = nullptr;
+    cuda(cudaStreamEndCapture(s, &out));
+  } else if (!st) {
+    fail(A2C_ERR_CUDA);
+  }
+  if (!st) cuda(cudaGraphInstantiate(&E, G, 0));
+  if (!st) cuda(cudaGraphLaunch(E, s));
+  cuda(cudaStreamSynchronize(s));
+  if (E) cudaGraphExecDestroy(E);
+  if (G) cudaGraphDestroy(G);
+  (void)cudaGetLastError();
+  return st;
 }
 
 }  // namespace a2c

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
+
 #include "a2c_gpp.h"
 
 namespace a2c {
@@ -138,6 +140,24 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 constexpr int kMaxDevices = 64;
 int device_sms(int dev);
 int current_device_sms();
+// Tile shape of the mixed pair kernels: threads per site (1, 2, 4, 8) and
+// threads per block of pass 1 (256, 512, 768) and pass 2 (128, 256, 512);
+// 0 = the library's choice.
+struct Tile {
+  int tps = 0, rho_block = 0, grad_block = 0;
+  bool operator==(const Tile &o) const { return tps == o.tps && rho_block == o.rho_block && grad_block == o.grad_block; }
+};
+inline bool valid_tile(int tps, int rho_block, int grad_block) {
+  return (tps == 0 || tps == 1 || tps == 2 || tps == 4 || tps == 8) &&
+         (rho_block == 0 || rho_block == 256 || rho_block == 512 || rho_block == 768) &&
+         (grad_block == 0 || grad_block == 128 || grad_block == 256 || grad_block == 512);
+}
+// The tile tuner (api.cu): threads per site at the default block sizes,
+// then the pass-1 block size, then the pass-2 block size, each stage keeping
+// the fastest; time_tile(tile, &ms) measures one candidate.  ms[10]
+// receives the candidates' times in that order (may be null).
+constexpr int kTileCandidates = 10;
+a2c_status tune_tile(const std::function<a2c_status(const Tile &, float *)> &time_tile, Tile *best, float *ms);
 // Threads per site of the mixed pair kernels when none was chosen: a
 // system with fewer than 2048 sites per SM spreads each site over 4 lanes
 // so that every SM gets work; a larger one runs one lane per site.
@@ -161,6 +181,8 @@ a2c_status launch_dirichlet(a2c_gpp_ctx *c, const int *d_sites, int n, double ga
                             int *d_full);
 a2c_status launch_macro(a2c_gpp_ctx *c, const double *d_x, const int *d_surf_flags, int nSurf, double *h_xH,
                         double *h_xHint);
+// the same reduction into d_out[2] on the device (stream-ordered, capturable)
+a2c_status launch_macro_device(a2c_gpp_ctx *c, const double *d_x, const int *d_surf_flags, int nSurf, double *d_out);
 a2c_status check_status_word(a2c_gpp_ctx *c);
 
 // k_neighbors.cu
@@ -186,8 +208,12 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
 void mixed_free(a2c_gpp_ctx *c);
 a2c_status mixed_set_threads_per_site(a2c_gpp_ctx *c, int tps);
 int mixed_threads_per_site(a2c_gpp_ctx *c);
+// the context's tile as chosen (zeros: the library's choice) and as used
+a2c_status mixed_set_tile(a2c_gpp_ctx *c, const Tile &t);
+Tile mixed_tile(a2c_gpp_ctx *c);
+Tile effective_tile(const Tile &t, int64_t n_sites, int sms);
 // batched: prep + both passes over the listed sites (G, Vs, Ss; no objective)
-a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, int tps);
+a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, const Tile &tile);
 a2c_status mixed_prepare(a2c_gpp_ctx *c);  // tables and buffers, before any graph capture
 // pass 2 pair visiting (A2C_PAIRS_*); the pairs-once index is rebuilt when
 // the lists change (mixed_lists_changed, called after every list build)
@@ -201,6 +227,22 @@ void mixed_graph_key(a2c_gpp_ctx *c, const void *key[5]);
 // batch.cu: the one-instance device-driven minimizer of a context
 a2c_status engine_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp, double *fmin, int *iters,
                            int *nfev, double *gnorm, int *reason);
+// Device buffers of a DMD run (a2c_gpp_dmd_run): chemical potential, its
+// pair sums, the diffused occupancy, full flags, boundary sites, surface
+// flags; per step 4 records (xH mean, xH interior, f, iterations); two ints
+// of loop counters.
+struct DmdDev {
+  double *gamma, *send, *x, *rec, *macro;
+  int *full, *bd, *surf, *counters;
+  int n_bd, n_surf;
+};
+// Outer steps first..nsteps-1 of a DMD run as one CUDA graph: a loop over
+// steps, each the device-driven minimization (a loop over L-BFGS ticks)
+// followed by the chemical potential, the Dirichlet condition, the
+// diffusion step and the macro results.  Needs the context's engine (a
+// step run eagerly before).  Waits for completion.
+a2c_status engine_dmd_graph(a2c_gpp_ctx *c, const a2c_dmd_params *dp, const DmdDev &dd, int first, int nsteps);
+bool engine_dmd_graph_usable(const a2c_gpp_ctx *c, const a2c_dmd_params *dp);
 void engine_free(a2c_gpp_ctx *c);
 
 // lbfgs.cu

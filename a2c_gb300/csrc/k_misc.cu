@@ -206,15 +206,21 @@ a2c_status launch_diffuse(a2c_gpp_ctx *c, const double *d_gamma, const int *d_fu
   return A2C_OK;
 }
 
-a2c_status launch_macro(a2c_gpp_ctx *c, const double *d_x, const int *d_surf_flags, int nSurf, double *h_xH,
-                        double *h_xHint) {
+a2c_status launch_macro_device(a2c_gpp_ctx *c, const double *d_x, const int *d_surf_flags, int nSurf, double *d_out) {
   const int nH = c->p.nH;
-  double *pa = c->d_red, *pb = c->d_red + kRedGrid, *out = c->d_red + 2 * kRedGrid + 4;
+  double *pa = c->d_red, *pb = c->d_red + kRedGrid;
   const int grid = std::max(1, std::min(kRedGrid, (nH + kRedBlock - 1) / kRedBlock));
   k_macro_partial<<<grid, kRedBlock, 0, c->stream>>>(d_x, d_surf_flags, nH, pa, pb);
   A2C_CUDA(cudaGetLastError());
-  k_macro_final<<<1, kRedBlock, 0, c->stream>>>(pa, pb, grid, nH, nSurf, out);
+  k_macro_final<<<1, kRedBlock, 0, c->stream>>>(pa, pb, grid, nH, nSurf, d_out);
   A2C_CUDA(cudaGetLastError());
+  return A2C_OK;
+}
+
+a2c_status launch_macro(a2c_gpp_ctx *c, const double *d_x, const int *d_surf_flags, int nSurf, double *h_xH,
+                        double *h_xHint) {
+  double *out = c->d_red + 2 * kRedGrid + 4;
+  A2C_TRY(launch_macro_device(c, d_x, d_surf_flags, nSurf, out));
   double h[2];
   A2C_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   A2C_CUDA(cudaStreamSynchronize(c->stream));

@@ -56,6 +56,7 @@ struct Mixed {
   int grid_cap[9] = {};       // persistent grid size per threads-per-site
   float4 *tabEmb = nullptr;   // per rho interval: F_Pd cubics, then F_H cubics
   int tps = 0;                // threads per site (0 = choose)
+  int rho_block = 0, grad_block = 0;  // threads per block of pass 1 and pass 2 (0 = 256)
   // Pass 2 with every pair evaluated once (sorted, symmetric lists): per
   // list entry of a pair the site owns (neighbor id below its own) the slot
   // of the reverse entry; per site the count of such entries, with the
@@ -73,16 +74,27 @@ struct Mixed {
 
 namespace {
 
-constexpr int kBlock = 256;
-// Pass 2 resident blocks per SM the register allocation must allow (4
-// blocks of 256 threads = 64 registers per thread).
+constexpr int kBlock = 256;  // threads per block of the other kernels (and the tiles' default)
+// Pass 2 resident threads per SM the register allocation must allow: 1024
+// (64 registers per thread), whatever the block size.
 #ifndef A2C_GRAD_MIN_BLOCKS
 #define A2C_GRAD_MIN_BLOCKS 4
 #endif
-// Pass 1 likewise (5 blocks = 48 registers per thread).
+// Pass 1 at 256 threads per block: 5 blocks = 48 registers per thread.
+// Its 98 KB of table copies allow two blocks per SM, so larger blocks are
+// how it gets more warps: 512 threads (2 blocks, 64 registers) or 768
+// (2 blocks, 42 registers).
 #ifndef A2C_RHO_MIN_BLOCKS
 #define A2C_RHO_MIN_BLOCKS 5
 #endif
+template <int BLOCK>
+constexpr int grad_min_blocks() {
+  return A2C_GRAD_MIN_BLOCKS * 256 / BLOCK;
+}
+template <int BLOCK>
+constexpr int rho_min_blocks() {
+  return BLOCK == 256 ? A2C_RHO_MIN_BLOCKS : 2;
+}
 
 // Folded exponential constants of f_H, phi_PdH, phi_H (see fH, morse below).
 struct MorseExp {
@@ -278,9 +290,9 @@ constexpr int kGradCopies = A2C_GRAD_COPIES;
 constexpr int kGradTabN = kGradCopies > 1 ? kRhoTabN : kTabN;
 constexpr size_t kGradSmem = 2 * sizeof(float4) * kGradTabN * kGradCopies;
 
-template <int TPS, bool LIST>
-__global__ void __launch_bounds__(kBlock, A2C_RHO_MIN_BLOCKS) k_rho_mixed(MixArgs a) {
-  constexpr int kSitesPerBlock = kBlock / TPS;
+template <int TPS, bool LIST, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, rho_min_blocks<BLOCK>()) k_rho_mixed(MixArgs a) {
+  constexpr int kSitesPerBlock = BLOCK / TPS;
   const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
   extern __shared__ float4 sF8[];
@@ -443,9 +455,9 @@ __device__ __forceinline__ void add_pair(SiteAcc &A, const PairAcc &p, float3 D,
   kahan(A.s[4], A.c[4], vx * p.v);
 }
 
-template <int TPS, bool LIST>
-__global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_mixed(MixArgs a) {
-  constexpr int kSitesPerBlock = kBlock / TPS;
+template <int TPS, bool LIST, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, grad_min_blocks<BLOCK>()) k_grad_mixed(MixArgs a) {
+  constexpr int kSitesPerBlock = BLOCK / TPS;
   const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
   extern __shared__ float4 sTab[];  // f_Pd' quadratics, then phi_Pd cubics, kGradCopies-way interleaved
@@ -540,9 +552,9 @@ __device__ __forceinline__ void send_share(const MixArgs &a, int64_t t, const Pa
                              -w * fmaf(D.z, p.csum, p.e[2]), w * p.sigj);
 }
 
-template <int TPS, bool LIST>
-__global__ void __launch_bounds__(kBlock, A2C_GRAD_MIN_BLOCKS) k_grad_once(MixArgs a) {
-  constexpr int kSitesPerBlock = kBlock / TPS;
+template <int TPS, bool LIST, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, grad_min_blocks<BLOCK>()) k_grad_once(MixArgs a) {
+  constexpr int kSitesPerBlock = BLOCK / TPS;
   const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
   extern __shared__ float4 sTab[];  // f_Pd' quadratics, then phi_Pd cubics, kGradCopies-way interleaved
@@ -817,60 +829,87 @@ const ExpTerms &exp_consts() {
 // once = true: pass 2 evaluates every pair once (k_grad_once + k_grad_recv;
 // a.rev, a.npre, a.recv set), else from both sides (k_grad_mixed).
 constexpr int kRecvTps = 8;  // lanes per site summing the received shares
-template <int TPS, bool LIST>
-struct PairCaps {
-  int cap[4];
-};
-// Per device: the dynamic shared-memory limit of the pair kernels raised and
-// their persistent grid sizes (resident blocks x SMs) computed, once, under
-// a lock (the attribute is a per-device setting).
-template <int TPS, bool LIST>
-const PairCaps<TPS, LIST> &pair_caps() {
+// Persistent grid size of a kernel at a block size on the current device
+// (resident blocks x SMs), computed once per (kernel, block, device) under
+// a lock, with the dynamic shared-memory limit raised on that device first.
+int grid_cap(const void *fn, int block, size_t smem) {
+  struct Entry {
+    const void *fn;
+    int dev, block, cap;
+  };
   static std::mutex m;
-  static PairCaps<TPS, LIST> caps[kMaxDevices];
-  static bool ready[kMaxDevices] = {};
+  static std::vector<Entry> cache;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
   std::lock_guard<std::mutex> lock(m);
-  PairCaps<TPS, LIST> &c = caps[dev];
-  if (!ready[dev]) {
-    const int sms = device_sms(dev);
-    int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-    cudaFuncSetAttribute(k_rho_mixed<TPS, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRhoSmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_rho_mixed<TPS, LIST>, kBlock, kRhoSmem);
-    cudaFuncSetAttribute(k_grad_mixed<TPS, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
-    cudaFuncSetAttribute(k_grad_once<TPS, LIST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_grad_mixed<TPS, LIST>, kBlock, kGradSmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_grad_once<TPS, LIST>, kBlock, kGradSmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_grad_recv<kRecvTps, LIST>, kBlock, 0);
-    c.cap[0] = std::max(1, sms * b0);
-    c.cap[1] = std::max(1, sms * b1);
-    c.cap[2] = std::max(1, sms * b2);
-    c.cap[3] = std::max(1, sms * b3);
-    ready[dev] = b0 > 0 && b1 > 0 && b2 > 0 && b3 > 0;  // a failed query is retried on the next launch
-    (void)cudaGetLastError();
+  for (const Entry &e : cache)
+    if (e.fn == fn && e.dev == dev && e.block == block) return e.cap;
+  int nb = 0;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, smem);
+  (void)cudaGetLastError();
+  if (nb < 1) return 1;  // not cached: asked again next time
+  cache.push_back({fn, dev, block, nb * device_sms(dev)});
+  return cache.back().cap;
+}
+
+inline unsigned persistent_grid(int64_t n_items, int per_block, int cap) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n_items + per_block - 1) / per_block, cap));
+}
+
+template <int TPS, bool LIST, int B>
+void launch_rho(const MixArgs &a, cudaStream_t st) {
+  const void *fn = (const void *)k_rho_mixed<TPS, LIST, B>;
+  k_rho_mixed<TPS, LIST, B><<<persistent_grid(a.N, B / TPS, grid_cap(fn, B, kRhoSmem)), B, kRhoSmem, st>>>(a);
+}
+template <int TPS, bool LIST, int B>
+void launch_grad(const MixArgs &a, cudaStream_t st, bool once) {
+  if (once) {
+    const void *fn = (const void *)k_grad_once<TPS, LIST, B>;
+    k_grad_once<TPS, LIST, B><<<persistent_grid(a.N, B / TPS, grid_cap(fn, B, kGradSmem)), B, kGradSmem, st>>>(a);
+  } else {
+    const void *fn = (const void *)k_grad_mixed<TPS, LIST, B>;
+    k_grad_mixed<TPS, LIST, B><<<persistent_grid(a.N, B / TPS, grid_cap(fn, B, kGradSmem)), B, kGradSmem, st>>>(a);
   }
-  return c;
 }
 
 template <int TPS, bool LIST>
-void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, bool once = false) {
-  const int *cap = pair_caps<TPS, LIST>().cap;
-  const int64_t need = (a.N * TPS + kBlock - 1) / kBlock;
-  k_rho_mixed<TPS, LIST>
-      <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[0])), kBlock, kRhoSmem, st>>>(a);
+void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, bool once, const Tile &t) {
+  switch (t.rho_block) {
+    case 512: launch_rho<TPS, LIST, 512>(a, st); break;
+    case 768: launch_rho<TPS, LIST, 768>(a, st); break;
+    default: launch_rho<TPS, LIST, 256>(a, st); break;
+  }
   if (ev) cudaEventRecord(ev[2], st);
+  switch (t.grad_block) {
+    case 128: launch_grad<TPS, LIST, 128>(a, st, once); break;
+    case 512: launch_grad<TPS, LIST, 512>(a, st, once); break;
+    default: launch_grad<TPS, LIST, 256>(a, st, once); break;
+  }
   if (once) {
-    k_grad_once<TPS, LIST>
-        <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[2])), kBlock, kGradSmem, st>>>(a);
-    const int64_t need_r = (a.N * kRecvTps + kBlock - 1) / kBlock;
-    k_grad_recv<kRecvTps, LIST>
-        <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need_r, cap[3])), kBlock, 0, st>>>(a);
-  } else {
-    k_grad_mixed<TPS, LIST>
-        <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(need, cap[1])), kBlock, kGradSmem, st>>>(a);
+    const void *fn = (const void *)k_grad_recv<kRecvTps, LIST>;
+    k_grad_recv<kRecvTps, LIST><<<persistent_grid(a.N, kBlock / kRecvTps, grid_cap(fn, kBlock, 0)), kBlock, 0, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[3], st);
+}
+
+// Dispatch on threads per site.
+void launch_tile(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, bool once, const Tile &t, bool list) {
+  if (list) {
+    switch (t.tps) {
+      case 1: launch_pair_kernels<1, true>(a, st, ev, once, t); break;
+      case 2: launch_pair_kernels<2, true>(a, st, ev, once, t); break;
+      case 4: launch_pair_kernels<4, true>(a, st, ev, once, t); break;
+      default: launch_pair_kernels<8, true>(a, st, ev, once, t); break;
+    }
+  } else {
+    switch (t.tps) {
+      case 1: launch_pair_kernels<1, false>(a, st, ev, once, t); break;
+      case 2: launch_pair_kernels<2, false>(a, st, ev, once, t); break;
+      case 4: launch_pair_kernels<4, false>(a, st, ev, once, t); break;
+      default: launch_pair_kernels<8, false>(a, st, ev, once, t); break;
+    }
+  }
 }
 
 // The pair tables as the kernels read them (3 kTabN float4): the f_Pd
@@ -1023,6 +1062,33 @@ void mixed_free(a2c_gpp_ctx *c) {
 
 int mixed_threads_per_site(a2c_gpp_ctx *c) { return (c->mixed && c->mixed->tps) ? c->mixed->tps : 0; }
 
+Tile effective_tile(const Tile &t, int64_t n_sites, int sms) {
+  Tile e;
+  e.tps = t.tps ? t.tps : default_threads_per_site(n_sites, sms);
+  e.rho_block = t.rho_block ? t.rho_block : kBlock;
+  e.grad_block = t.grad_block ? t.grad_block : kBlock;
+  return e;
+}
+
+Tile mixed_tile(a2c_gpp_ctx *c) {
+  Tile t;
+  if (c->mixed) {
+    t.tps = c->mixed->tps;
+    t.rho_block = c->mixed->rho_block;
+    t.grad_block = c->mixed->grad_block;
+  }
+  return t;
+}
+
+a2c_status mixed_set_tile(a2c_gpp_ctx *c, const Tile &t) {
+  if (!valid_tile(t.tps, t.rho_block, t.grad_block)) return A2C_ERR_INVALID;
+  A2C_TRY(ensure_mixed(c));
+  c->mixed->tps = t.tps;
+  c->mixed->rho_block = t.rho_block;
+  c->mixed->grad_block = t.grad_block;
+  return A2C_OK;
+}
+
 a2c_status mixed_set_threads_per_site(a2c_gpp_ctx *c, int tps) {
   if (tps != 0 && tps != 1 && tps != 2 && tps != 4 && tps != 8) return A2C_ERR_INVALID;
   A2C_TRY(ensure_mixed(c));
@@ -1073,13 +1139,7 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
       k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ, sg);
     A2C_CUDA(cudaGetLastError());
     if (ev) cudaEventRecord(ev[1], c->stream);
-    const int tps = M->tps ? M->tps : default_threads_per_site(N, device_sms(c->device));
-    switch (tps) {
-      case 1: launch_pair_kernels<1, false>(a, c->stream, ev, once); break;
-      case 2: launch_pair_kernels<2, false>(a, c->stream, ev, once); break;
-      case 4: launch_pair_kernels<4, false>(a, c->stream, ev, once); break;
-      default: launch_pair_kernels<8, false>(a, c->stream, ev, once); break;
-    }
+    launch_tile(a, c->stream, ev, once, effective_tile(mixed_tile(c), N, device_sms(c->device)), false);
     A2C_CUDA(cudaGetLastError());
   } else if (ev) {
     for (int k2 = 1; k2 < 4; ++k2) cudaEventRecord(ev[k2], c->stream);
@@ -1104,7 +1164,7 @@ void mixed_graph_key(a2c_gpp_ctx *c, const void *key[5]) {
   key[4] = M ? (const void *)M->Gown : nullptr;
 }
 
-a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, int tps) {
+a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, const Tile &tile) {
   A2C_TRY(ensure_mixed(c));
   Mixed *M = c->mixed;
   const int64_t N = c->N;
@@ -1134,12 +1194,7 @@ a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const B
   const int prep_cap = 8 * device_sms(c->device);
   k_prep_list<<<(unsigned)std::min<int64_t>(grid_for(N, 256), prep_cap), 256, 0, c->stream>>>(
       dX, c->d_occ, bv, M->P, M->occ, c->d_xlist, c->d_status);
-  switch (tps) {
-    case 1: launch_pair_kernels<1, true>(a, c->stream, nullptr, once); break;
-    case 2: launch_pair_kernels<2, true>(a, c->stream, nullptr, once); break;
-    case 4: launch_pair_kernels<4, true>(a, c->stream, nullptr, once); break;
-    default: launch_pair_kernels<8, true>(a, c->stream, nullptr, once); break;
-  }
+  launch_tile(a, c->stream, nullptr, once, effective_tile(tile, N, device_sms(c->device)), true);
   A2C_CUDA(cudaGetLastError());
   return A2C_OK;
 }
@@ -1328,14 +1383,7 @@ extern "C" a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *c, const double *d
   if (N > 0) {
     k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], (int4 *)(base + kNaP),
                                                      (float *)(base + kNaOcc), span_args(c));
-    const int tps =
-        (c->mixed && c->mixed->tps) ? c->mixed->tps : default_threads_per_site(N, device_sms(c->device));
-    switch (tps) {
-      case 1: launch_pair_kernels<1, false>(a, c->stream, nullptr); break;
-      case 2: launch_pair_kernels<2, false>(a, c->stream, nullptr); break;
-      case 4: launch_pair_kernels<4, false>(a, c->stream, nullptr); break;
-      default: launch_pair_kernels<8, false>(a, c->stream, nullptr); break;
-    }
+    launch_tile(a, c->stream, nullptr, false, effective_tile(mixed_tile(c), N, device_sms(c->device)), false);
   }
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(kNaRedGrid, (N + kNaRedBlock - 1) / kNaRedBlock));
   k_na_partial<<<grid, kNaRedBlock, 0, c->stream>>>(a.Vs, a.Ss, N, pa, pb);

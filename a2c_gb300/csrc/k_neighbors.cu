@@ -41,6 +41,11 @@ struct GridArgs {
   int nPd;
   int64_t N;
   const double *X;
+  // FP32 prefilter (see prefilter below): positions as float, the largest
+  // |coordinate| (as float bits, set by k_positions_f32), the box as float
+  const float4 *Xf = nullptr;
+  const unsigned *qmax_bits = nullptr;
+  float boxf[3] = {0.f, 0.f, 0.f}, invboxf[3] = {0.f, 0.f, 0.f}, Lmaxf = 0.f, rcf = 0.f;
 };
 
 __device__ __forceinline__ int cell_coord(const GridArgs &g, double x, int d) {
@@ -58,21 +63,17 @@ __device__ __forceinline__ int64_t cell_of(const GridArgs &g, int64_t s) {
 }
 
 // The reference's acceptance test (KDTree.h:250-254 Chebyshev prefilter,
-// neighbors.cpp:77-82 self and squared distance), with the image shift.
-__device__ __forceinline__ bool pair_test(const GridArgs &g, int64_t i, int64_t j, uint32_t &entry, double &d2) {
+// neighbors.cpp:77-82 self and squared distance) in FP64, with the image
+// shift m (fixed by the FP32 prefilter, or decoded from an entry).
+__device__ __forceinline__ bool exact_test(const GridArgs &g, int64_t i, int64_t j, const int m[3], uint32_t &entry,
+                                           double &d2) {
   if (i == j) return false;
   double dd[3];
-  int m[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const double qi = g.X[4 * i + d];
     double qj = g.X[4 * j + d];
-    m[d] = 0;
-    if (g.periodic[d]) {
-      const double n = rint((qj - qi) / g.box[d]);
-      m[d] = -(int)n;
-      if (m[d] != 0) qj = qj + m[d] * g.box[d];
-    }
+    if (m[d] != 0) qj = qj + m[d] * g.box[d];
     dd[d] = qj - qi;
     if (fabs(dd[d]) > g.rc) return false;
   }
@@ -81,6 +82,70 @@ __device__ __forceinline__ bool pair_test(const GridArgs &g, int64_t i, int64_t 
   if (m[0] < -1 || m[0] > 1 || m[1] < -1 || m[1] > 1 || m[2] < -1 || m[2] > 1) return false;
   entry = (uint32_t)j | ((uint32_t)((m[0] + 1) + 3 * (m[1] + 1) + 9 * (m[2] + 1)) << kIdBits);
   return true;
+}
+
+// FP32 prefilter: rejects candidates farther than rc + guard in any
+// coordinate or in distance, and picks the image m of the rest.  guard
+// bounds the FP32 error of a coordinate difference (coordinates rounded to
+// float, one subtraction, the image shift) four times over, so a pair the
+// FP64 test accepts is never rejected here; a pair within rc + guard has a
+// unique nearest image because the box exceeds 2 (rc + guard) (checked on
+// the host before the prefilter is used), so m is the image the FP64
+// division rint((qj - qi) / L) would pick.
+__device__ __forceinline__ float prefilter_guard(const GridArgs &g) {
+  const float qmax = __uint_as_float(*g.qmax_bits);
+  return 1e-4f + 1.9073486328125e-6f * (qmax + g.Lmaxf + g.rcf);  // 2^-19 (qmax + L + rc)
+}
+__device__ __forceinline__ bool prefilter(const GridArgs &g, float4 fi, int64_t j, float lim, int m[3]) {
+  const float4 fj = g.Xf[j];
+  float dd[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    m[d] = 0;
+    if (g.periodic[d]) {
+      const float n = rintf(dd[d] * g.invboxf[d]);
+      dd[d] = dd[d] - n * g.boxf[d];
+      m[d] = -(int)n;
+    }
+    if (fabsf(dd[d]) > lim) return false;
+  }
+  return dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2] <= lim * lim;
+}
+
+// Candidate j of site i: the prefilter, then the FP64 test.  lim <= 0
+// (the prefilter cannot be used: a periodic box of at most 2 (rc + guard))
+// takes the image from the FP64 division instead.
+__device__ __forceinline__ bool pair_test(const GridArgs &g, int64_t i, float4 fi, float lim, int64_t j,
+                                          uint32_t &entry, double &d2) {
+  int m[3];
+  if (i == j) return false;
+  if (lim > 0.0f) {
+    if (!prefilter(g, fi, j, lim, m)) return false;
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      m[d] = g.periodic[d] ? -(int)rint((g.X[4 * j + d] - g.X[4 * i + d]) / g.box[d]) : 0;
+  }
+  return exact_test(g, i, j, m, entry, d2);
+}
+
+// The prefilter's cutoff for this build, or 0 when it cannot be used.
+__device__ __forceinline__ float prefilter_lim(const GridArgs &g) {
+  const float lim = g.rcf + prefilter_guard(g);
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (g.periodic[d] && !(0.5f * g.boxf[d] > lim * 1.0001f)) return 0.0f;
+  return lim;
+}
+
+// Positions as float for the prefilter and the largest |coordinate|.
+__global__ void k_positions_f32(const double *X, int64_t N, float4 *Xf, unsigned *qmax_bits) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  const float4 f = make_float4((float)X[4 * s], (float)X[4 * s + 1], (float)X[4 * s + 2], 0.0f);
+  Xf[s] = f;
+  const float q = fmaxf(fabsf(f.x), fmaxf(fabsf(f.y), fabsf(f.z)));
+  atomicMax(qmax_bits, __float_as_uint(q) + 1u);  // one ulp up: the float rounding of |q| may round down
 }
 
 template <class Fn>
@@ -165,10 +230,12 @@ __global__ void __launch_bounds__(kBlock) k_nbr_count(GridArgs g, Src src, int64
   int64_t n = 0, nP = 0, n1 = 0;
   int sh[3] = {0, 0, 0};
   const bool iPd = i < g.nPd;
+  const float4 fi = g.Xf[i];
+  const float lim = prefilter_lim(g);
   src.each(g, i, [&](int64_t j) {
     uint32_t e;
     double d2;
-    if (!pair_test(g, i, j, e, d2)) return;
+    if (!pair_test(g, i, fi, lim, j, e, d2)) return;
     ++n;
     const bool jPd = j < g.nPd;
     if (jPd) {
@@ -204,10 +271,12 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, Src src, const 
   if (i >= g.N) return;
   const int64_t b = off[i], e = off[i + 1];
   int64_t w = b;
+  const float4 fi = g.Xf[i];
+  const float lim = prefilter_lim(g);
   src.each(g, i, [&](int64_t j) {
     uint32_t en;
     double d2;
-    if (!pair_test(g, i, j, en, d2)) return;
+    if (!pair_test(g, i, fi, lim, j, en, d2)) return;
     if (w < e) nbr[w] = en;
     ++w;
   });
@@ -230,11 +299,14 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, Src src, const 
     const int64_t h = i - g.nPd;
     int64_t w1 = hh1_off[h];
     for (int64_t t = b; t < e; ++t) {
-      const int64_t j = nbr[t] & kIdMask;
+      const uint32_t ent = nbr[t];
+      const int64_t j = ent & kIdMask;
       if (j < g.nPd) continue;
+      const int code = (int)(ent >> kIdBits);  // the entry's image: (mx+1) + 3(my+1) + 9(mz+1)
+      const int m[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
       uint32_t en;
       double d2;
-      if (pair_test(g, i, j, en, d2) && d2 < g.A75) {
+      if (exact_test(g, i, j, m, en, d2) && d2 < g.A75) {
         if (w1 < hh1_off[h + 1]) hh1[w1] = (int)(j - g.nPd);
         ++w1;
       }
@@ -291,6 +363,13 @@ int64_t make_grid(const a2c_gpp_ctx *c, const double *h_X, double cut, GridArgs 
   g.rc2 = cut * cut;
   g.A75 = p.a_Pd * p.a_Pd * 0.75;
   g.A125 = p.a_Pd * p.a_Pd * 1.25;
+  g.rcf = (float)cut;
+  for (int d = 0; d < 3; ++d)
+    if (p.periodic[d]) {
+      g.boxf[d] = (float)p.box[d];
+      g.invboxf[d] = (float)(1.0 / p.box[d]);
+      g.Lmaxf = std::max(g.Lmaxf, (float)p.box[d]);
+    }
   int64_t ncell = 1;
   for (int d = 0; d < 3; ++d) {
     g.periodic[d] = p.periodic[d] ? 1 : 0;
@@ -345,11 +424,21 @@ a2c_status grow(int **p, int64_t *cap, int64_t need) {
 // Count, scan, allocate and fill from one candidate source.  ext = true:
 // the extended lists (no Pd head counts, shells or HH1).
 template <class Src>
-a2c_status make_lists(a2c_gpp_ctx *c, const GridArgs &g, Src src, bool ext) {
+a2c_status make_lists(a2c_gpp_ctx *c, const GridArgs &g0, Src src, bool ext) {
   const int64_t N = c->N;
   const a2c_gpp_params &p = c->p;
   cudaStream_t st = c->stream;
-  DevBuf counts(st), hh1c(st), maxc(st);
+  DevBuf counts(st), hh1c(st), maxc(st), xf(st), qmax(st);
+  GridArgs g = g0;  // with the prefilter's positions
+  A2C_CUDA(cudaMallocAsync(&xf.p, sizeof(float4) * std::max<int64_t>(N, 1), st));
+  A2C_CUDA(cudaMallocAsync(&qmax.p, sizeof(unsigned), st));
+  A2C_CUDA(cudaMemsetAsync(qmax.p, 0, sizeof(unsigned), st));
+  if (N > 0) {
+    k_positions_f32<<<grid_for(N, 256), 256, 0, st>>>(c->d_X, N, (float4 *)xf.p, (unsigned *)qmax.p);
+    A2C_CUDA(cudaGetLastError());
+  }
+  g.Xf = (const float4 *)xf.p;
+  g.qmax_bits = (const unsigned *)qmax.p;
   A2C_CUDA(cudaMallocAsync(&counts.p, sizeof(int64_t) * (N + 1), st));
   A2C_CUDA(cudaMallocAsync(&hh1c.p, sizeof(int64_t) * (p.nH + 1), st));
   A2C_CUDA(cudaMallocAsync(&maxc.p, sizeof(int), st));

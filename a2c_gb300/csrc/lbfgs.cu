@@ -434,7 +434,13 @@ a2c_status lbfgs_minimize(a2c_gpp_ctx *c, double *dX, const a2c_lbfgs_params *lp
   c->p.precision = saved_precision;
   A2C_TRY(st_run);
   A2C_CUDA(cudaMemcpyAsync(dX, L->x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  int word = 0;  // the mixed form's span guard (a rejected non-finite trial is not an error here)
+  A2C_CUDA(cudaMemcpyAsync(&word, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
   A2C_CUDA(cudaStreamSynchronize(st));
+  if (word & kStatusSpan) {
+    A2C_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
+    return A2C_ERR_LISTS_STALE;
+  }
   *fmin = f;
   *iters = it;
   *nfev = fev;

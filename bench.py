@@ -139,6 +139,79 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+# The sources that decide what the mixed kernels read and write: a traffic
+# figure captured for other sources is stale.
+KERNEL_SOURCES = ("k_mixed.cu", "internal.cuh", "tables.h", "tables.cpp")
+TRAFFIC_FILE = ROOT / "profiles" / "traffic.json"
+
+
+def kernel_source_sha() -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        h.update((ROOT / "a2c_gb300" / "csrc" / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def traffic_from_ncu(csv_path: str, sites: int, bench_sites: int = 262144) -> dict:
+    """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum)
+    of every captured kernel in an ncu CSV (--csv --log-file), averaged over
+    its launches and scaled from the captured case's `sites` to one
+    `bench_sites` launch; keyed by the kernel's base name."""
+    import csv
+
+    per = {}
+    with open(csv_path, newline="") as fh:
+        rows = [r for r in csv.reader(fh) if r]
+    head = next(i for i, r in enumerate(rows) if "Metric Name" in r)
+    cols = rows[head]
+    ki, mi, vi, ui = (cols.index(k) for k in ("Kernel Name", "Metric Name", "Metric Value", "Metric Unit"))
+    idi = cols.index("ID")
+    scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    for r in rows[head + 1:]:
+        if len(r) <= max(ki, mi, vi) or not r[mi].startswith("dram__bytes_"):
+            continue
+        name = r[ki].split("(")[0].split("<")[0].strip().split(" ")[-1]
+        v = float(r[vi].replace(",", "")) * scale.get(r[ui], 1.0)
+        per.setdefault(name, {}).setdefault(r[idi], 0.0)
+        per[name][r[idi]] += v
+    out = {}
+    for name, launches in per.items():
+        out[name] = sum(launches.values()) / len(launches) * bench_sites / sites
+    return out
+
+
+def write_traffic(csv_path: str, sites: int) -> dict:
+    """profiles/traffic.json from an ncu capture of the profile case, keyed
+    by the hash of the kernel sources it was captured with."""
+    k = traffic_from_ncu(csv_path, sites)
+    doc = {"source_sha16": kernel_source_sha(), "captured_sites": sites, "scaled_to_sites": 262144,
+           "bytes_per_launch": k,
+           "note": "dram__bytes_read.sum + dram__bytes_write.sum per launch (ncu starts each launch with flushed "
+                   "caches), averaged over the captured launches and scaled to a 262,144-site launch by the site "
+                   "count"}
+    TRAFFIC_FILE.write_text(json.dumps(doc, indent=1) + "\n")
+    return doc
+
+
+def measured_traffic(kernels):
+    """DRAM bytes per 262,144-site launch of `kernels` summed, from
+    profiles/traffic.json when it was captured for the current kernel
+    sources; else (None, why)."""
+    try:
+        doc = json.loads(TRAFFIC_FILE.read_text())
+    except Exception:
+        return None, "no profiles/traffic.json"
+    if doc.get("source_sha16") != kernel_source_sha():
+        return None, f"stale: profiles/traffic.json was captured for kernel sources {doc.get('source_sha16')}, " \
+                     f"these are {kernel_source_sha()}"
+    b = doc.get("bytes_per_launch", {})
+    if not all(k in b for k in kernels):
+        return None, "profiles/traffic.json lacks " + ", ".join(k for k in kernels if k not in b)
+    return sum(b[k] for k in kernels), "ncu capture of these kernel sources (profiles/traffic.json)"
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     try:
@@ -225,7 +298,7 @@ def time_to_minimum(cells: int, gatol: float, device: int, fp64_cap: int = 0, po
         g.eval(X)  # warm-up (lazy set-up of both forms)
         g.set_precision("mixed")
         g.eval(X)
-        out["autotune_tps"] = g.autotune()[0]
+        out["autotune_tile"] = list(g.autotune_tile()[0])
         g.set_precision("fp64")
         fp64 = {}
         for name, drv in (("fp64", "default"), ("fp64_device_engine", "device")):
@@ -420,8 +493,9 @@ def run_batch_case(args):
         t0 = time.perf_counter()
         b.build_neighbors(X)
         out["neighbor_build_s"] = time.perf_counter() - t0
-        tps, ms = b.autotune(X)
-        out["autotune"] = {"threads_per_site": tps, "ms_per_eval": ms}
+        tile, cands = b.autotune_tile(X)
+        out["autotune"] = {"tile": {"threads_per_site": tile[0], "pass1_block": tile[1], "pass2_block": tile[2]},
+                           "candidates_ms": {"x".join(map(str, t)): ms for t, ms in cands}}
         for name, polish in (("mixed_batch", 0), ("mixed_polish_batch", 1))[:1 if args.batch_mixed_only else 2]:
             t0 = time.perf_counter()
             r = b.minimize(X, polish=polish, **kw)
@@ -604,21 +678,22 @@ def run_ours(args):
             flush.fill_(1.0)
         return g.profile_eval(dX.data_ptr(), df.data_ptr(), dG.data_ptr())
 
-    # autotune the threads-per-site mapping and the pass 2 pair mode of the
-    # mixed kernels (pairs once: each pair evaluated by one of its sites;
-    # both: every site gathers over all its pairs)
-    tune = {}
+    # the library's tile tuner (threads per site, pass-1 and pass-2 block
+    # sizes) for each pass 2 pair mode (pairs once: each pair evaluated by
+    # one of its sites; both: every site gathers over all its pairs), then
+    # the faster mode at its tile
+    g.set_state(X)
+    tune, tiles = {}, {}
     for mode in (("once", "both") if args.pair_mode == "auto" else (args.pair_mode,)):
         g.set_pair_mode(mode)
-        for tps in (1, 2, 4, 8):
-            g.set_threads_per_site(tps)
-            step_profiled()
-            tune[f"{mode}/{tps}"] = min(float(np.sum(step_profiled())) for _ in range(3))
-    best_key = min(tune, key=tune.get)
-    mode = best_key.split("/")[0]
-    best = int(best_key.split("/")[1])
+        tiles[mode], cands = g.autotune_tile(reps=5)
+        tune[mode] = {"x".join(map(str, t)): ms for t, ms in cands}
+        step_profiled()
+        tune[mode]["chosen_ms"] = min(float(np.sum(step_profiled())) for _ in range(3))
+    mode = min(tiles, key=lambda m: tune[m]["chosen_ms"])
     g.set_pair_mode(mode)
-    g.set_threads_per_site(best)
+    g.set_tile(*tiles[mode])
+    best = tiles[mode][0]
     once = g.pair_mode == A.A2C_PAIRS_ONCE
 
     def barrier():
@@ -646,19 +721,17 @@ def run_ours(args):
     G_mixed = dG.cpu().numpy()
 
     # the other pair mode at its best mapping, for comparison (not the headline)
-    modes = {mode: {"threads_per_site": best, "pass2_ms": float(np.mean(st_mixed[:, 2])),
+    modes = {mode: {"tile": list(tiles[mode]), "pass2_ms": float(np.mean(st_mixed[:, 2])),
                     "eval_ms": float(np.mean(st_mixed.sum(axis=1)))}}
     other = "both" if mode == "once" else "once"
-    okeys = [k for k in tune if k.startswith(other)]
-    if okeys:
-        okey = min(okeys, key=tune.get)
+    if other in tiles:
         g.set_pair_mode(other)
-        g.set_threads_per_site(int(okey.split("/")[1]))
+        g.set_tile(*tiles[other])
         st_other = timed(max(3, args.steps // 2), 2)
-        modes[other] = {"threads_per_site": int(okey.split("/")[1]), "pass2_ms": float(np.mean(st_other[:, 2])),
+        modes[other] = {"tile": list(tiles[other]), "pass2_ms": float(np.mean(st_other[:, 2])),
                         "eval_ms": float(np.mean(st_other.sum(axis=1)))}
         g.set_pair_mode(mode)
-        g.set_threads_per_site(best)
+        g.set_tile(*tiles[mode])
 
     # FP64 plain form on the same state
     g.set_precision("fp64")
@@ -713,16 +786,12 @@ def run_ours(args):
     exec2 = fl_once if once else fl["pass2"]
     ach = fl["pass2"] / (pass2_ms * 1e-3)
     pass2_64_ms = float(np.mean(st_64[:, 2]))
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
-        try:
-            traffic = json.loads(tfile.read_text()).get(
-                "k_grad_once_recv_bytes_per_launch" if once else "k_grad_mixed_bytes_per_launch")
-        except Exception:
-            traffic = None
+    traffic, traffic_src = measured_traffic(["k_grad_once", "k_grad_recv"] if once else ["k_grad_mixed"])
+    if traffic is not None:
+        traffic *= Ns / 262144.0
     kname = f"k_grad_once<{best}> + k_grad_recv<8> (pass 2, pairs once)" if once else \
         f"k_grad_mixed<{best}> (pass 2)"
+    kname += f", {tiles[mode][2]} threads per block"
     roofline = {"bound": "fp32", "kernel": kname, "achieved": ach / 1e12,
                 "peak": peak32 / 1e12, "unit": "TFLOP/s", "frac": ach / peak32,
                 "peak_source": "measured in this run: FP32 FMA-chain kernel (a2c_gpp_peak_flops); "
@@ -732,6 +801,8 @@ def run_ours(args):
                 "executed_flops_per_launch": exec2,
                 "executed_achieved": exec2 / (pass2_ms * 1e-3) / 1e12,
                 "executed_frac": exec2 / (pass2_ms * 1e-3) / peak32, "traffic": traffic,
+                "traffic_source": traffic_src,
+                "algorithmic_bytes_per_launch": flop_model.algorithmic_bytes(Ns, n_entries),
                 "hbm_frac": (flop_model.algorithmic_bytes(Ns, n_entries) / ((pass1_ms + pass2_ms) * 1e-3)) /
                             (measured_peaks().get("hbm_gbs", 6800.0) * 1e9),
                 "pass1": {"ms": pass1_ms, "achieved_tflops": fl["pass1"] / (pass1_ms * 1e-3) / 1e12},
@@ -759,6 +830,8 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": dev_time_mixed * 1e3 / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": config_dict({"parallelism": f"replicas x{world}", "threads_per_site": best,
+                                       "tile": {"threads_per_site": tiles[mode][0], "pass1_block": tiles[mode][1],
+                                                "pass2_block": tiles[mode][2]},
                                        "pair_mode": mode, "autotune_ms": tune}),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * 4 * Ns,
                         "d2h_bytes_per_step": 8 * 4 * Ns + 8},
@@ -844,7 +917,13 @@ def main():
     ap.add_argument("--batch-stride", type=int, default=16, help="every k-th instance forms the looped subset")
     ap.add_argument("--batch-mixed-only", action="store_true",
                     help="batched case: only the mixed-precision batch minimization")
+    ap.add_argument("--traffic-from", metavar="CSV",
+                    help="write profiles/traffic.json from an ncu CSV of the profile case (--case-cells cells) "
+                         "and exit")
     args = ap.parse_args()
+    if args.traffic_from:
+        print(json.dumps(write_traffic(args.traffic_from, 8 * args.case_cells ** 3)))
+        return 0
     if args.case == "profile":
         return run_profile_case(args)
     if args.case == "dmd":

@@ -227,6 +227,20 @@ a2c_status a2c_mixed_table_eval(int which, const double *x, int64_t n, double *v
  * context.  tps receives the choice, ms[4] (may be NULL) the mean time per
  * evaluation of each candidate in milliseconds. */
 a2c_status a2c_gpp_autotune(a2c_gpp_ctx *ctx, int reps, int *tps, float *ms);
+/* Tile shape of the mixed-precision pair kernels: threads per site (1, 2,
+ * 4, 8) and threads per block of pass 1 (256, 512, 768 -- its 98 KB of
+ * table copies allow two blocks per SM, so larger blocks mean more resident
+ * warps) and of pass 2 (128, 256, 512); 0 = the library's choice.
+ * a2c_gpp_get_tile reports the tile in use, tile[3] = {tps, pass-1 block,
+ * pass-2 block}.  a2c_gpp_autotune_tile measures candidates by coordinate
+ * descent -- threads per site at 256-thread blocks, then the pass-1 block,
+ * then the pass-2 block, each stage keeping the fastest -- on the context's
+ * current state, sets the fastest and returns it; ms[10] (may be NULL)
+ * receives the mean milliseconds per evaluation of the ten candidates in
+ * that order. */
+a2c_status a2c_gpp_set_tile(a2c_gpp_ctx *ctx, int tps, int rho_block, int grad_block);
+a2c_status a2c_gpp_get_tile(a2c_gpp_ctx *ctx, int *tile);
+a2c_status a2c_gpp_autotune_tile(a2c_gpp_ctx *ctx, int reps, int *tile, float *ms);
 
 /* Which L-BFGS driver a2c_gpp_minimize and a2c_gpp_dmd_run use.
  * A2C_MINIMIZER_DEFAULT: mixed precision device-driven -- each L-BFGS
@@ -330,6 +344,11 @@ typedef struct a2c_dmd_params {
   a2c_lbfgs_params lbfgs;  /* the minimization of every step */
   int neighbor_update;     /* 1: re-derive the neighbor lists (incl. HH1) at the start of every step after the
                               first, through the skin refilter when a skin is set; 0: keep them fixed */
+  int host_steps;          /* 0 (default): with fixed lists and the device-driven minimizer, the first step runs
+                              eagerly and steps 2..nsteps as ONE CUDA graph -- a device loop over outer steps,
+                              each a device loop over L-BFGS ticks followed by the chemical potential, the
+                              Dirichlet condition, the diffusion step and the macro results, with no host
+                              round trip; 1: every step sequenced from the host (same results, bit for bit) */
 } a2c_dmd_params;
 
 /* Runs nsteps outer steps with all state on the device; X (4N), xH, gamma,
@@ -395,6 +414,12 @@ a2c_status a2c_gpp_batch_minimize(a2c_gpp_batch *batch, double *X, const a2c_lbf
 a2c_status a2c_gpp_batch_stats(a2c_gpp_batch *batch, int *ticks, double *seconds);
 /* the autotuner (see a2c_gpp_autotune) over the whole batch at host X */
 a2c_status a2c_gpp_batch_autotune(a2c_gpp_batch *batch, const double *X, int reps, int *tps, float *ms);
+/* The tile of the batch's mixed pair kernels (see a2c_gpp_set_tile):
+ * set, read back, and tuned on the whole batch at X (every instance
+ * evaluated per candidate). */
+a2c_status a2c_gpp_batch_set_tile(a2c_gpp_batch *batch, int tps, int rho_block, int grad_block);
+a2c_status a2c_gpp_batch_get_tile(a2c_gpp_batch *batch, int *tile);
+a2c_status a2c_gpp_batch_autotune_tile(a2c_gpp_batch *batch, const double *X, int reps, int *tile, float *ms);
 
 /* Solution snapshots in the formats of the reference's Output class
  * (Output.cpp:60-90, 133-480): per frame a VTK PolyData file

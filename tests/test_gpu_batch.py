@@ -148,3 +148,20 @@ def test_batch_rejects_bad_input(gpu):
             b.minimize(Y)
         with pytest.raises(A.A2CError):
             b.set_occupancy(np.full(xH.size, 1.5))
+
+
+def test_batch_tile_tuner(gpu):
+    """The batch's tile tuner picks a valid tile on the whole batch; block
+    sizes leave every instance's results unchanged."""
+    inst, X, xH = A.batch_workload(n=6, edge=(3, 5))
+    with A.Batch(inst, precision="mixed") as b:
+        b.set_occupancy(xH)
+        b.build_neighbors(X)
+        b.set_tile(4, 256, 256)
+        f0, G0 = b.eval(X)
+        b.set_tile(4, 512, 128)
+        f1, G1 = b.eval(X)
+        assert np.array_equal(f0, f1) and np.array_equal(G0, G1)
+        tile, cands = b.autotune_tile(X, reps=2)
+        assert tile[0] in (1, 2, 4, 8) and tile[1] in (256, 512, 768) and tile[2] in (128, 256, 512)
+        assert b.tile() == tile and len(cands) == 10

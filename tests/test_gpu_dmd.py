@@ -101,3 +101,29 @@ def test_dmd_mixed_follows_fp64(gpu):
     assert d_mixed.max() <= 4 * d_fp64.max() + 1e-4
     assert x_mixed <= 4 * x_fp64 + 1e-4
     assert res["mixed"]["xH_mean"][-1] > res["mixed"]["xH_mean"][0]
+
+
+@pytest.mark.parametrize("prec,minimizer", [("mixed", "default"), ("fp64", "device")])
+def test_dmd_graph_equals_host_steps(gpu, prec, minimizer):
+    """Steps 2..n of a DMD run as one CUDA graph (a device loop over outer
+    steps, each a device loop over L-BFGS ticks, then the chemical
+    potential, the Dirichlet condition, the diffusion step and the macro
+    results) give the host-sequenced loop's results bit for bit."""
+    X, xH, bd, box, nPd, nH = slab()
+    per = (1, 1, 0)
+    gamma0 = np.zeros(nH)
+    full0 = np.zeros(nH, dtype=np.int32)
+    kw = dict(gatol=1e-5, max_it=300)
+    res = {}
+    for host_steps in (True, False):
+        with A.Gpp(nPd, nH, T=400.0, box=box, periodic=per, precision=prec) as g:
+            g.set_occupancy(xH)
+            g.build_neighbors(X)
+            g.set_minimizer(minimizer)
+            res[host_steps] = g.dmd_run(X, xH, gamma0, full0, bd, bd, 4, gamma_bd=2.0, host_steps=host_steps, **DMD,
+                                        **kw)
+    a, b = res[True], res[False]
+    print("iters", a["iters"], b["iters"], "xH", a["xH_mean"], b["xH_mean"])
+    for k in ("X", "xH", "gamma", "full_H", "fmin", "iters", "xH_mean", "xH_interior"):
+        assert np.array_equal(a[k], b[k]), k
+    assert a["xH_mean"][-1] > a["xH_mean"][0]

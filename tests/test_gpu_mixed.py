@@ -242,3 +242,27 @@ def test_device_driven_minimizer_matches_host_loop(gpu):
         h.build_neighbors(Y)
         ref = h.minimize(Y, gatol=1e-5, max_it=300, polish=0)
     assert np.array_equal(r2.X, ref.X) and r2.iters == ref.iters
+
+
+def test_tile_block_sizes_do_not_change_results(gpu):
+    """The block sizes of the tile only group sites into blocks: a site's
+    arithmetic is the same in every block, so at fixed threads per site every
+    pass-1 and pass-2 block size gives the same bits; the tuner returns a
+    valid tile and sets it."""
+    X, xH, box, per, nPd, nH, pb = make("slab_4x5x6")
+    with A.Gpp(nPd, nH, box=box, periodic=per, precision="mixed") as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        for tps in (2, 4):
+            ref = None
+            for rb in (256, 512, 768):
+                for gb in (128, 256, 512):
+                    g.set_tile(tps, rb, gb)
+                    assert g.tile() == (tps, rb, gb)
+                    f, G = g.eval(X)
+                    if ref is None:
+                        ref = (f, G)
+                    assert f == ref[0] and np.array_equal(G, ref[1]), (tps, rb, gb)
+        tile, cands = g.autotune_tile(reps=2)
+        assert tile[0] in (1, 2, 4, 8) and tile[1] in (256, 512, 768) and tile[2] in (128, 256, 512)
+        assert g.tile() == tile and len(cands) == 10 and all(ms > 0 for _, ms in cands)
