@@ -37,6 +37,7 @@ def build(ref: bool | None = None) -> None:
     if ref:
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_TREE}"], check=True)
         subprocess.run(["make", "-s", "-C", str(HERE), "geo", f"REF={REFERENCE_TREE}"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), "out", f"REF={REFERENCE_TREE}"], check=True)
 
 
 class OrcParams(C.Structure):

@@ -17,6 +17,7 @@ static inline int MPI_Comm_rank(MPI_Comm, int *r) { *r = 0; return 0; }
 static inline int MPI_Comm_size(MPI_Comm, int *s) { *s = 1; return 0; }
 static inline int MPI_Barrier(MPI_Comm) { return 0; }
 static inline int MPI_Abort(MPI_Comm, int code) { std::exit(code); }
+static inline int MPI_Finalize() { return 0; }
 static inline int MPI_Allreduce(const void *s, void *r, int n, MPI_Datatype t, MPI_Op, MPI_Comm) {
   if (s != r) std::memcpy(r, s, (size_t)n * (size_t)t);
   return 0;
