@@ -201,15 +201,18 @@ a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, d
  * driver that forbids allocation during recording.  It has no counterpart
  * in the reference.  Inputs dX (4N doubles) and outputs df (1 double), dG
  * (4N doubles) are device pointers; the context supplies the neighbor lists
- * (build them first) and the occupancy.  All scratch lives in one fixed
- * device array of about 5.8 MB that every GPU loading the library keeps until
- * the process exits, so problems above 131,072 sites are rejected with
- * A2C_ERR_INVALID.  The first call on a device finds the array's address
- * and loads constant tables into it (synchronous copies): make that first
- * call before any stream capture.  Calls share the array and it keeps the
- * last call's contents; nothing in it needs clearing, but calls that
- * overlap on the GPU (two streams, two contexts on one device) race.
- * Stream-ordered on the context's stream, like a2c_gpp_eval_device. */
+ * (build them first) and the occupancy; pass 2 visits pairs from both
+ * sides.  All scratch lives in one fixed device array of about 6.1 MB that
+ * every GPU loading the library keeps until the process exits, so problems
+ * above 131,072 sites are rejected with A2C_ERR_INVALID.  The first call on
+ * a device finds the array's address and loads constant tables into it
+ * (synchronous copies): make that first call before any stream capture.  A
+ * device reset (a new context) is noticed on the next call, which loads
+ * them again.  Calls share the array and it keeps the last call's contents;
+ * nothing in it needs clearing, but calls that overlap on the GPU (two
+ * streams, two contexts on one device) race.  Stream-ordered on the
+ * context's stream, like a2c_gpp_eval_device. */
+a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG);
 /* Host-only checks of the mixed form's functions (no GPU needed).
  * a2c_eam_analytic: value and exact derivative (forward mode, FP64) of the
  * EAM function numbered as in a2c_gpp_eam_eval (0 F_Pd, 2 F_H, 4 f_Pd,
@@ -254,21 +257,6 @@ a2c_status a2c_gpp_autotune_tile(a2c_gpp_ctx *ctx, int reps, int *tile, float *m
 enum { A2C_MINIMIZER_DEFAULT = 0, A2C_MINIMIZER_HOST = 1, A2C_MINIMIZER_DEVICE = 2 };
 a2c_status a2c_gpp_set_minimizer(a2c_gpp_ctx *ctx, int mode);
 
-/* Allocation-free mixed-precision evaluation.  No counterpart in the
- * reference: it is for callers that cannot allocate device memory while they
- * evaluate -- a solver callback running inside another framework's memory
- * pool, or work recorded under a driver that forbids allocation while it
- * records.  Same arguments and results as a2c_gpp_eval_device in mixed
- * precision (device pointers, stream-ordered on the context's stream), with
- * the pass-2 pairs visited from both sides.  Its scratch is one fixed
- * device array inside the library (about 5.8 MB, held by every GPU that
- * loads the library until the process exits), so it serves at most 131,072
- * sites and returns A2C_ERR_INVALID above that; it calls no allocator.  The
- * first call on a device resolves the array and loads the function tables
- * into it (make that call before any stream capture); a device reset is
- * noticed on the next call, which loads them again.  Every call shares the
- * array: calls that overlap on one GPU race. */
-a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *ctx, const double *dX, double *df, double *dG);
 /* Profiling aid: one stream-ordered evaluation on device pointers with CUDA
  * events between its launches; stage_ms[4] receives the durations of the
  * state preparation, pass 1 (densities), pass 2 (energy and gradient) and
