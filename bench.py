@@ -867,7 +867,9 @@ def run_profile_case(args):
     with A.Gpp(nPd, nH, box=box, periodic=w["periodic"], precision="mixed") as g:
         g.set_occupancy(xH)
         g.build_neighbors(X)
-        if args.case_tps:
+        if args.case_tile:
+            g.set_tile(*[int(v) for v in args.case_tile.split(",")])
+        elif args.case_tps:
             g.set_threads_per_site(args.case_tps)
         g.set_pair_mode(args.case_pairs)
         dX = torch.tensor(X, device="cuda")
@@ -902,6 +904,8 @@ def main():
                     help="profile: the small untimed case used for ncu captures")
     ap.add_argument("--case-cells", type=int, default=40)
     ap.add_argument("--case-tps", type=int, default=0, help="threads per site in the profile case (0 = library)")
+    ap.add_argument("--case-tile", default="", help="tile of the profile case: threads per site, pass-1 block, "
+                                                    "pass-2 block (e.g. 2,512,256; empty = library)")
     ap.add_argument("--case-pairs", choices=["once", "both"], default="once",
                     help="pass 2 pair mode of the profile case")
     ap.add_argument("--pair-mode", choices=["auto", "once", "both"], default="auto",
