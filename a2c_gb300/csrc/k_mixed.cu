@@ -52,9 +52,9 @@ struct Mixed {
   int4 *P = nullptr;        // per site: fixed-point x, y, z; sigma (FP32 bits)
   float *occ = nullptr;     // per site occupancy (1 for Pd)
   float2 *FF = nullptr;     // per site (F'(rho), F(rho))
-  float4 *tabPair = nullptr;  // cubics of f_Pd, f_Pd', phi_Pd, phi_Pd' (kTabN each, midpoint-centred)
+  float4 *tabPair = nullptr;  // f_Pd cubics, phi_Pd cubics, f_Pd' quadratics (kTabN each)
   int grid_cap[9] = {};       // persistent grid size per threads-per-site
-  float4 *tabEmb = nullptr;   // per rho interval the cubics of F and F': Pd intervals, then H
+  float4 *tabEmb = nullptr;   // per rho interval: F_Pd cubics, then F_H cubics
   int tps = 0;                // threads per site (0 = choose)
   int rho_block = 0, grad_block = 0;  // threads per block of pass 1 and pass 2 (0 = 256)
   // Pass 2 with every pair evaluated once (sorted, symmetric lists): per
@@ -177,7 +177,9 @@ __device__ __forceinline__ SiteRef<LIST> site_ref(const MixArgs &a, int64_t k) {
 }
 
 __device__ __forceinline__ float hv(float4 c, float t) { return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x); }
-
+__device__ __forceinline__ float hd(float4 c, float t) { return fmaf(fmaf(3.0f * c.w, t, 2.0f * c.z), t, c.y); }
+// h times the derivative from its own coefficients (c1, 2 c2, 3 c3)
+__device__ __forceinline__ float dq(float4 d, float t) { return fmaf(fmaf(d.z, t, d.y), t, d.x); }
 
 // Interval of the pair tables and the offset t in [-1/2, 1/2] from its
 // midpoint (the tables hold midpoint-centred cubics), without a float-to-int
@@ -286,9 +288,7 @@ constexpr size_t kRhoSmem = sizeof(float4) * kRhoTabN * kRhoCopies;  // 98,304 B
 #endif
 constexpr int kGradCopies = A2C_GRAD_COPIES;
 constexpr int kGradTabN = kGradCopies > 1 ? kRhoTabN : kTabN;
-// three tables: f_Pd', phi_Pd, phi_Pd' (the derivatives are their own
-// interpolants, as accurate as the values)
-constexpr size_t kGradSmem = 3 * sizeof(float4) * kGradTabN * kGradCopies;
+constexpr size_t kGradSmem = 2 * sizeof(float4) * kGradTabN * kGradCopies;
 
 template <int TPS, bool LIST, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, rho_min_blocks<BLOCK>()) k_rho_mixed(MixArgs a) {
@@ -357,8 +357,8 @@ __global__ void __launch_bounds__(BLOCK, rho_min_blocks<BLOCK>()) k_rho_mixed(Mi
     float x = fminf(fmaxf(rho * (float)kEmbInvH, 0.0f), (float)kEmbN - 0.5f);
     const int i = (int)x;
     const float tt = x - (float)i;
-    const float4 *c = a.tabEmb + 2 * ((iPd ? 0 : kEmbN) + i);  // F's cubic, then F''s
-    a.FF[s] = make_float2(hv(__ldg(c + 1), tt), hv(__ldg(c), tt));
+    const float4 c = __ldg(&a.tabEmb[(iPd ? 0 : kEmbN) + i]);
+    a.FF[s] = make_float2(hd(c, tt) * (float)kEmbInvH, hv(c, tt));
   }
   }
 }
@@ -411,9 +411,11 @@ __device__ __forceinline__ void pair_terms(const ExpTerms &x, const float4 *sF, 
       if (TYPE == 0) {
         float tt;
         const int i = kGradCopies * tab_index<kGradTabN>(r, tt);
-        const float4 cf = sF[i], cp = sP[i], cd = sP[kGradTabN * kGradCopies + i];
-        phi = hv(cp, tt);
-        g = fmaf(Fa + Fb, hv(cf, tt), hv(cd, tt));
+        const float4 cf = sF[i], cp = sP[i];
+        // phi and h phi' share one Horner chain
+        const float hp = fmaf(cp.w, tt, cp.z), hq = fmaf(hp, tt, cp.y);
+        phi = fmaf(hq, tt, cp.x);
+        g = fmaf(Fa + Fb, dq(cf, tt), fmaf(fmaf(cp.w, tt, hp), tt, hq)) * (float)kTabInvH;
       } else if (TYPE == 3) {
         const float nfhd = fHd_neg(x, r);  // -f_H'
         float dphi;
@@ -423,7 +425,7 @@ __device__ __forceinline__ void pair_terms(const ExpTerms &x, const float4 *sF, 
       } else {
         float tt;
         const int i = kGradCopies * tab_index<kGradTabN>(r, tt);
-        const float fpd = hv(sF[i], tt);
+        const float fpd = dq(sF[i], tt) * (float)kTabInvH;
         const float nfhd = fHd_neg(x, r);
         float dphi;
         if (TAIL) morse(x.pdh, r, phi, dphi);
@@ -458,11 +460,10 @@ __global__ void __launch_bounds__(BLOCK, grad_min_blocks<BLOCK>()) k_grad_mixed(
   constexpr int kSitesPerBlock = BLOCK / TPS;
   const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
-  extern __shared__ float4 sTab[];  // f_Pd', phi_Pd, phi_Pd' cubics, kGradCopies-way interleaved
+  extern __shared__ float4 sTab[];  // f_Pd' quadratics, then phi_Pd cubics, kGradCopies-way interleaved
   for (int i = threadIdx.x; i < kGradTabN * kGradCopies; i += blockDim.x) {
-    sTab[i] = __ldg(&a.tabPair[kTabN + i / kGradCopies]);
-    sTab[kGradTabN * kGradCopies + i] = __ldg(&a.tabPair[2 * kTabN + i / kGradCopies]);
-    sTab[2 * kGradTabN * kGradCopies + i] = __ldg(&a.tabPair[3 * kTabN + i / kGradCopies]);
+    sTab[i] = __ldg(&a.tabPair[2 * kTabN + i / kGradCopies]);
+    sTab[kGradTabN * kGradCopies + i] = __ldg(&a.tabPair[kTabN + i / kGradCopies]);
   }
   __syncthreads();
   const float4 *sF = sTab + threadIdx.x % kGradCopies, *sP = sF + kGradTabN * kGradCopies;
@@ -556,11 +557,10 @@ __global__ void __launch_bounds__(BLOCK, grad_min_blocks<BLOCK>()) k_grad_once(M
   constexpr int kSitesPerBlock = BLOCK / TPS;
   const int64_t n = LIST ? (int64_t)*a.bv.count : a.N;
   if ((int64_t)blockIdx.x * kSitesPerBlock >= n) return;
-  extern __shared__ float4 sTab[];  // f_Pd', phi_Pd, phi_Pd' cubics, kGradCopies-way interleaved
+  extern __shared__ float4 sTab[];  // f_Pd' quadratics, then phi_Pd cubics, kGradCopies-way interleaved
   for (int i = threadIdx.x; i < kGradTabN * kGradCopies; i += blockDim.x) {
-    sTab[i] = __ldg(&a.tabPair[kTabN + i / kGradCopies]);
-    sTab[kGradTabN * kGradCopies + i] = __ldg(&a.tabPair[2 * kTabN + i / kGradCopies]);
-    sTab[2 * kGradTabN * kGradCopies + i] = __ldg(&a.tabPair[3 * kTabN + i / kGradCopies]);
+    sTab[i] = __ldg(&a.tabPair[2 * kTabN + i / kGradCopies]);
+    sTab[kGradTabN * kGradCopies + i] = __ldg(&a.tabPair[kTabN + i / kGradCopies]);
   }
   __syncthreads();
   const float4 *sF = sTab + threadIdx.x % kGradCopies, *sP = sF + kGradTabN * kGradCopies;
@@ -912,17 +912,26 @@ void launch_tile(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, bool once, 
   }
 }
 
-// The pair tables as the kernels read them (4 kTabN float4): the cubics of
-// f_Pd (pass 1), f_Pd', phi_Pd and phi_Pd' (pass 2), each table contiguous.
-constexpr int kPairTabs = 4;
+// The pair tables as the kernels read them (3 kTabN float4): the f_Pd
+// cubics (pass 1), the phi_Pd cubics, and the f_Pd' quadratics
+// (c1, 2 c2, 3 c3) of pass 2, which needs only the derivative.
 void pair_tables(float *out) {
   static std::mutex m;  // guards the static scratch below
   std::lock_guard<std::mutex> lock(m);
-  static float inter[kPairTabFloats * kTabN];
+  static float inter[8 * kTabN];
   build_pair_table_raw(kTabR0, 1.0 / kTabInvH, kTabN, inter);
-  for (int i = 0; i < kTabN; ++i)
-    for (int t = 0; t < kPairTabs; ++t)
-      for (int k = 0; k < 4; ++k) out[4 * (t * kTabN + i) + k] = inter[kPairTabFloats * i + 4 * t + k];
+  for (int i = 0; i < kTabN; ++i) {
+    const float *f = inter + 8 * i, *p = inter + 8 * i + 4;
+    for (int k = 0; k < 4; ++k) {
+      out[4 * i + k] = f[k];
+      out[4 * (kTabN + i) + k] = p[k];
+    }
+    float *d = out + 4 * (2 * kTabN + i);
+    d[0] = f[1];
+    d[1] = 2.0f * f[2];
+    d[2] = 3.0f * f[3];
+    d[3] = 0.0f;
+  }
 }
 
 a2c_status ensure_mixed(a2c_gpp_ctx *c) {
@@ -934,16 +943,16 @@ a2c_status ensure_mixed(a2c_gpp_ctx *c) {
   const int64_t n = std::max<int64_t>(c->N, 1);
   if (cudaMalloc(&M->P, sizeof(int4) * n) != cudaSuccess || cudaMalloc(&M->occ, sizeof(float) * n) != cudaSuccess ||
       cudaMalloc(&M->FF, sizeof(float2) * n) != cudaSuccess ||
-      cudaMalloc(&M->tabPair, sizeof(float4) * kPairTabs * kTabN) != cudaSuccess ||
-      cudaMalloc(&M->tabEmb, sizeof(float) * 2 * kEmbTabFloats * kEmbN) != cudaSuccess)
+      cudaMalloc(&M->tabPair, sizeof(float4) * 3 * kTabN) != cudaSuccess ||
+      cudaMalloc(&M->tabEmb, sizeof(float4) * 2 * kEmbN) != cudaSuccess)
     return A2C_ERR_NOMEM;
-  std::vector<float> pair((size_t)4 * kPairTabs * kTabN), embPd, embH;
+  std::vector<float> pair((size_t)12 * kTabN), embPd, embH;
   pair_tables(pair.data());
   build_embed_table(0, 1.0 / kEmbInvH, kEmbN, embPd);
   build_embed_table(1, 1.0 / kEmbInvH, kEmbN, embH);
   A2C_CUDA(cudaMemcpyAsync(M->tabPair, pair.data(), sizeof(float) * pair.size(), cudaMemcpyHostToDevice, c->stream));
   A2C_CUDA(cudaMemcpyAsync(M->tabEmb, embPd.data(), sizeof(float) * embPd.size(), cudaMemcpyHostToDevice, c->stream));
-  A2C_CUDA(cudaMemcpyAsync(M->tabEmb + 2 * kEmbN, embH.data(), sizeof(float) * embH.size(), cudaMemcpyHostToDevice,
+  A2C_CUDA(cudaMemcpyAsync(M->tabEmb + kEmbN, embH.data(), sizeof(float) * embH.size(), cudaMemcpyHostToDevice,
                            c->stream));
   A2C_CUDA(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
   return A2C_OK;
@@ -1202,7 +1211,7 @@ a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const B
 // records -- this entry point evaluates the mixed-precision form with all of
 // its scratch in one file-scope device array of fixed size instead of
 // memory from cudaMalloc.  Every GPU that loads the library holds the array
-// (about 6.1 MB) until the process exits.
+// (about 5.8 MB) until the process exits.
 // ---------------------------------------------------------------------------
 namespace a2c {
 
@@ -1221,8 +1230,8 @@ constexpr size_t kNaVs = kNaFF + 8 * (size_t)kNaMaxSites;
 constexpr size_t kNaSs = kNaVs + 8 * (size_t)kNaMaxSites;
 constexpr size_t kNaPart = kNaSs + 8 * (size_t)kNaMaxSites;
 constexpr size_t kNaTabPair = kNaPart + 8 * 2 * (size_t)kNaRedGrid;
-constexpr size_t kNaTabEmb = kNaTabPair + 16 * (size_t)kPairTabs * kTabN;
-constexpr size_t kNaBytes = kNaTabEmb + 4 * 2 * (size_t)kEmbTabFloats * kEmbN;
+constexpr size_t kNaTabEmb = kNaTabPair + 16 * 3 * (size_t)kTabN;
+constexpr size_t kNaBytes = kNaTabEmb + 16 * 2 * (size_t)kEmbN;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
@@ -1234,8 +1243,8 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 unsigned char *g_na_base[kMaxDevices] = {};
 unsigned long long g_na_ctx[kMaxDevices] = {};
 std::mutex g_na_mutex;
-float g_na_pair_host[4 * kPairTabs * kTabN];
-float g_na_emb_host[2 * kEmbTabFloats * kEmbN];
+float g_na_pair_host[12 * kTabN];
+float g_na_emb_host[2 * 4 * kEmbN];
 bool g_na_host_ready = false;
 
 // The current context's id through the driver entry point (no link-time
@@ -1275,7 +1284,7 @@ a2c_status na_setup(int dev, unsigned char **base) {
   if (!g_na_host_ready) {
     pair_tables(g_na_pair_host);
     build_embed_table_raw(0, 1.0 / kEmbInvH, kEmbN, g_na_emb_host);
-    build_embed_table_raw(1, 1.0 / kEmbInvH, kEmbN, g_na_emb_host + kEmbTabFloats * kEmbN);
+    build_embed_table_raw(1, 1.0 / kEmbInvH, kEmbN, g_na_emb_host + 4 * kEmbN);
     g_na_host_ready = true;
   }
   unsigned char *b = (unsigned char *)ptr;

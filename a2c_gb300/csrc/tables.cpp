@@ -25,28 +25,6 @@ namespace tables {
 struct Dual {
   double v, d;
 };
-// Second-order forward mode: value, first and second derivative.  The
-// derivative tables (f_Pd', phi_Pd', F') are Hermite interpolants of the
-// first derivative, built from its values and slopes (the second
-// derivative), so a table's derivative is as accurate as its values.
-struct D2 {
-  double v, d, dd;
-};
-inline D2 operator+(D2 a, D2 b) { return {a.v + b.v, a.d + b.d, a.dd + b.dd}; }
-inline D2 operator-(D2 a, D2 b) { return {a.v - b.v, a.d - b.d, a.dd - b.dd}; }
-inline D2 operator*(D2 a, D2 b) { return {a.v * b.v, a.d * b.v + a.v * b.d, a.dd * b.v + 2.0 * a.d * b.d + a.v * b.dd}; }
-inline D2 operator+(D2 a, double b) { return {a.v + b, a.d, a.dd}; }
-inline D2 operator-(D2 a, double b) { return {a.v - b, a.d, a.dd}; }
-inline D2 operator*(D2 a, double b) { return {a.v * b, a.d * b, a.dd * b}; }
-inline D2 operator*(double b, D2 a) { return {a.v * b, a.d * b, a.dd * b}; }
-inline D2 dexp(D2 a) {
-  const double e = std::exp(a.v);
-  return {e, e * a.d, e * (a.dd + a.d * a.d)};
-}
-inline D2 dpow(D2 u, double y) {
-  const double p2 = std::pow(u.v, y - 2.0), p1 = p2 * u.v;
-  return {p1 * u.v, y * p1 * u.d, y * (y - 1.0) * p2 * u.d * u.d + y * p1 * u.dd};
-}
 inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
 inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
 inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
@@ -61,28 +39,26 @@ inline Dual dexp(Dual a) {
 inline Dual dpow(Dual u, double y) { return {std::pow(u.v, y), y * std::pow(u.v, y - 1.0) * u.d}; }
 
 // potential.cpp:64-98; `branch` is the radius that selects the branch
-template <class T>
-T f_Pd(T r, double branch) {
+Dual f_Pd(Dual r, double branch) {
   const double a[7][2] = {{2.7267629107325706, 1.8716766113599643}, {2.50290548851635, 1.668549182690922},
                           {2.0924467509943674, 1.3150372774478005}, {1.564328475106985, 0.8987511149780485},
                           {1.009780903403673, 0.5124363774128722},  {0.5304054524800665, 0.2169886022464641},
                           {0.1356566408715063, 0.035852347523891395}};
   if (branch > 5.0) return 0.001510569378297 * dexp((-0.077976566126292 / 0.001510569378297) * (r - 5.0));
-  const T z = r * 0.2;
-  T ra = z;
+  const Dual z = r * 0.2;
+  Dual ra = z;
   for (int m = 0; m < 7; ++m) ra = ra * (z * (z - a[m][0]) + a[m][1]);
   return z * (z * (z * (ra * -2.597301181336601e7 + 14673.409149169922) + -255.8965835571289) + 0.6676807403564453) +
          -0.02972698211669922;
 }
 
 // potential.cpp:126-155
-template <class T>
-T phi_Pd(T r, double branch) {
+Dual phi_Pd(Dual r, double branch) {
   if (branch > 5.05) return -0.016958780164980 * dexp((0.089019679316328 / -0.016958780164980) * (r - 5.05));
   const double b[4][2] = {{2.0586473420376348, 1.0683922574015199}, {1.6696359816422877, 0.7337878627470482},
                           {1.1690370066230809, 0.3909805777737639}, {0.2635598721249787, 0.033551116514910245}};
-  const T z = r * 0.2;
-  T y = (z - 1.0699996145674568) * -79415.24035137112;
+  const Dual z = r * 0.2;
+  Dual y = (z - 1.0699996145674568) * -79415.24035137112;
   y = y * (z - 1.06015072612581);
   y = y * (z - 0.42433991011376526);
   y = y * (z + 0.06169160085238687);
@@ -91,13 +67,12 @@ T phi_Pd(T r, double branch) {
 }
 
 // potential.cpp:16-38
-template <class T>
-T F_Pd(T rho) {
+Dual F_Pd(Dual rho) {
   const double b[5][2] = {{2.4242616904962846, 1.4791899886249564}, {2.1376274623740064, 1.2169215689822592},
                           {1.6486007989726832, 0.8159825255339774}, {1.0749204110338482, 0.42007491336688396},
                           {0.5128056047933808, 0.12468685331167456}};
-  const T z = rho * 0.02;
-  T y = (z - 0.20581955357385892) * 295878.9003038662;
+  const Dual z = rho * 0.02;
+  Dual y = (z - 0.20581955357385892) * 295878.9003038662;
   y = y * (z - 0.081228755904399);
   y = y * z;
   y = y * (z + 0.05298811034615951);
@@ -106,11 +81,10 @@ T F_Pd(T rho) {
 }
 
 // potential.cpp:45-57
-template <class T>
-T F_H(T rho) {
+Dual F_H(Dual rho) {
   const double c = 0.000197047, d = 1.18860, a = 9.99780, b = 60.0155, eps1 = 0.0540638;
-  const T u = rho + eps1;
-  T y = dpow(u, 2.0 + d) * (1.0 / (2.0 + d)) - dpow(u, 1.0 + d) * ((a + b) / (1.0 + d)) + dpow(u, d) * (a * b / d);
+  const Dual u = rho + eps1;
+  Dual y = dpow(u, 2.0 + d) * (1.0 / (2.0 + d)) - dpow(u, 1.0 + d) * ((a + b) / (1.0 + d)) + dpow(u, d) * (a * b / d);
   return y * -c - rho * -0.0296604;
 }
 
@@ -155,51 +129,52 @@ void hermite_mid(Dual p0, Dual p1, double h, float *c) {
   c[3] = (float)c3;
 }
 
-// value (v, d) and derivative (d, dd) of a second-order result as the
-// end points of the value and the derivative interpolants
-inline Dual val(D2 a) { return {a.v, a.d}; }
-inline Dual der(D2 a) { return {a.d, a.dd}; }
-
 }  // namespace tables
 
-// The tables written into caller-provided arrays, with no heap allocation.
-// Pair tables: per interval 16 floats, the midpoint-centred cubics of f_Pd,
-// f_Pd', phi_Pd and phi_Pd' (kPairTabFloats).
-void build_pair_table_raw(double r0, double h, int n, float *out) {
-  using tables::D2;
+// Pair table: per interval 8 floats, f_Pd's cubic then phi_Pd's cubic.
+void build_pair_table(double r0, double h, int n, std::vector<float> &out) {
+  out.assign((size_t)n * 8, 0.0f);
   for (int i = 0; i < n; ++i) {
     const double xa = r0 + h * i, xb = r0 + h * (i + 1), mid = r0 + h * (i + 0.5);
-    const D2 fa = tables::f_Pd(D2{xa, 1.0, 0.0}, mid), fb = tables::f_Pd(D2{xb, 1.0, 0.0}, mid);
-    const D2 pa = tables::phi_Pd(D2{xa, 1.0, 0.0}, mid), pb = tables::phi_Pd(D2{xb, 1.0, 0.0}, mid);
-    float *o = out + (size_t)kPairTabFloats * i;
-    tables::hermite_mid(tables::val(fa), tables::val(fb), h, o);
-    tables::hermite_mid(tables::der(fa), tables::der(fb), h, o + 4);
-    tables::hermite_mid(tables::val(pa), tables::val(pb), h, o + 8);
-    tables::hermite_mid(tables::der(pa), tables::der(pb), h, o + 12);
+    tables::hermite_mid(tables::f_Pd({xa, 1.0}, mid), tables::f_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i]);
+    tables::hermite_mid(tables::phi_Pd({xa, 1.0}, mid), tables::phi_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i + 4]);
   }
 }
 
-// Embedding tables: per interval 8 floats, the cubics (in t from the
-// interval's start) of F and of F' (kEmbTabFloats); species 0 = Pd, 1 = H.
-void build_embed_table_raw(int species, double h, int n, float *out) {
-  using tables::D2;
-  for (int i = 0; i < n; ++i) {
-    const D2 a = {h * i, 1.0, 0.0}, b = {h * (i + 1), 1.0, 0.0};
-    const D2 ya = species == 0 ? tables::F_Pd(a) : tables::F_H(a), yb = species == 0 ? tables::F_Pd(b) : tables::F_H(b);
-    float *o = out + (size_t)kEmbTabFloats * i;
-    tables::hermite(tables::val(ya), tables::val(yb), h, o);
-    tables::hermite(tables::der(ya), tables::der(yb), h, o + 4);
-  }
-}
-
-void build_pair_table(double r0, double h, int n, std::vector<float> &out) {
-  out.assign((size_t)n * kPairTabFloats, 0.0f);
-  build_pair_table_raw(r0, h, n, out.data());
-}
-
+// Embedding tables: per interval 4 floats; species 0 = Pd, 1 = H.
 void build_embed_table(int species, double h, int n, std::vector<float> &out) {
-  out.assign((size_t)n * kEmbTabFloats, 0.0f);
-  build_embed_table_raw(species, h, n, out.data());
+  out.assign((size_t)n * 4, 0.0f);
+  for (int i = 0; i < n; ++i) {
+    const tables::Dual a = {h * i, 1.0}, b = {h * (i + 1), 1.0};
+    if (species == 0)
+      tables::hermite(tables::F_Pd(a), tables::F_Pd(b), h, &out[(size_t)4 * i]);
+    else
+      tables::hermite(tables::F_H(a), tables::F_H(b), h, &out[(size_t)4 * i]);
+  }
+}
+
+}  // namespace a2c
+
+namespace a2c {
+
+// The same tables written into caller-provided arrays (8n and 4n floats),
+// with no heap allocation.
+void build_pair_table_raw(double r0, double h, int n, float *out) {
+  for (int i = 0; i < n; ++i) {
+    const double xa = r0 + h * i, xb = r0 + h * (i + 1), mid = r0 + h * (i + 0.5);
+    tables::hermite_mid(tables::f_Pd({xa, 1.0}, mid), tables::f_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i]);
+    tables::hermite_mid(tables::phi_Pd({xa, 1.0}, mid), tables::phi_Pd({xb, 1.0}, mid), h, &out[(size_t)8 * i + 4]);
+  }
+}
+
+void build_embed_table_raw(int species, double h, int n, float *out) {
+  for (int i = 0; i < n; ++i) {
+    const tables::Dual a = {h * i, 1.0}, b = {h * (i + 1), 1.0};
+    if (species == 0)
+      tables::hermite(tables::F_Pd(a), tables::F_Pd(b), h, &out[(size_t)4 * i]);
+    else
+      tables::hermite(tables::F_H(a), tables::F_H(b), h, &out[(size_t)4 * i]);
+  }
 }
 
 }  // namespace a2c
@@ -218,11 +193,11 @@ extern "C" a2c_status a2c_eam_analytic(int which, const double *x, int64_t n, do
     const Dual d{x[k], 1.0};
     Dual y{0.0, 0.0};
     switch (which) {
-      case 0: y = a2c::tables::F_Pd<Dual>(d); break;
-      case 2: y = a2c::tables::F_H<Dual>(d); break;
-      case 4: y = a2c::tables::f_Pd<Dual>(d, x[k]); break;
+      case 0: y = a2c::tables::F_Pd(d); break;
+      case 2: y = a2c::tables::F_H(d); break;
+      case 4: y = a2c::tables::f_Pd(d, x[k]); break;
       case 6: y = a2c::tables::f_H(d); break;
-      case 8: y = a2c::tables::phi_Pd<Dual>(d, x[k]); break;
+      case 8: y = a2c::tables::phi_Pd(d, x[k]); break;
       case 10: y = a2c::tables::phi_PdH(d); break;
       default: y = a2c::tables::phi_H(d); break;
     }
@@ -234,6 +209,7 @@ extern "C" a2c_status a2c_eam_analytic(int which, const double *x, int64_t n, do
 
 namespace {
 float hv(const float *c, float t) { return std::fma(std::fma(std::fma(c[3], t, c[2]), t, c[1]), t, c[0]); }
+float hd(const float *c, float t) { return std::fma(std::fma(3.0f * c[3], t, 2.0f * c[2]), t, c[1]); }
 }  // namespace
 
 // The mixed form's FP32 table interpolants evaluated on the host with the
@@ -256,9 +232,9 @@ extern "C" a2c_status a2c_mixed_table_eval(int which, const double *x, int64_t n
       float u = std::fmin(std::fmax(s * (float)a2c::kEmbInvH, 0.0f), (float)a2c::kEmbN - 0.5f);
       const int i = (int)u;
       const float t = u - (float)i;
-      const float *c = (which == 0 ? embPd : embH).data() + a2c::kEmbTabFloats * i;
+      const float *c = (which == 0 ? embPd : embH).data() + 4 * i;
       value[k] = hv(c, t);
-      deriv[k] = hv(c + 4, t);  // the F' table
+      deriv[k] = hd(c, t) * (float)a2c::kEmbInvH;
     } else {
       // the pair kernels' indexing (k_mixed.cu tab_index): interval and
       // midpoint offset by the 1.5 * 2^23 rounding of an FMA result
@@ -269,9 +245,9 @@ extern "C" a2c_status a2c_mixed_table_eval(int which, const double *x, int64_t n
       int32_t bits;
       std::memcpy(&bits, &y, 4);
       const int i = bits - 0x4B400000;
-      const float *c = pair.data() + a2c::kPairTabFloats * i + (which == 4 ? 0 : 8);
+      const float *c = pair.data() + 8 * i + (which == 4 ? 0 : 4);
       value[k] = hv(c, t);
-      deriv[k] = hv(c + 4, t);  // the derivative table (f_Pd' or phi_Pd')
+      deriv[k] = hd(c, t) * (float)a2c::kTabInvH;
     }
   }
   return A2C_OK;

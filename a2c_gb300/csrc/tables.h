@@ -9,9 +9,5 @@ constexpr double kTabInvH = 160.0;  // ... h = 1/160 A (knots on the 5.0 / 5.05 
 constexpr int kTabN = 960;
 constexpr double kEmbInvH = 64.0;   // embedding tables: rho in [0, 64), h = 1/64
 constexpr int kEmbN = 4096;
-// Floats per interval: pair tables hold the cubics of f_Pd, f_Pd', phi_Pd,
-// phi_Pd'; embedding tables those of F and F'.
-constexpr int kPairTabFloats = 16;
-constexpr int kEmbTabFloats = 8;
 
 }  // namespace a2c

@@ -172,7 +172,7 @@ def traffic_from_ncu(csv_path: str, sites: int, bench_sites: int = 262144) -> di
     for r in rows[head + 1:]:
         if len(r) <= max(ki, mi, vi) or not r[mi].startswith("dram__bytes_"):
             continue
-        name = r[ki].split("(")[0].split("<")[0].strip().split(" ")[-1]
+        name = r[ki].split("(")[0].split("<")[0].strip().split(" ")[-1].split("::")[-1]
         v = float(r[vi].replace(",", "")) * scale.get(r[ui], 1.0)
         per.setdefault(name, {}).setdefault(r[idi], 0.0)
         per[name][r[idi]] += v
@@ -897,9 +897,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--ttm-cells", type=int, default=32,
                     help="time-to-minimum leg on a cells^3 nucleus lattice (0 = skip; 64 = the full 2,097,152 sites)")
-    ap.add_argument("--ttm-gatol", type=float, default=1e-5,
-                    help="gradient-norm tolerance both forms run to in the time-to-minimum leg (the FP64 form's "
-                         "finite-difference gradient cannot go much below 5e-6 at 262,144 sites)")
+    ap.add_argument("--ttm-gatol", type=float, default=2e-5,
+                    help="gradient-norm tolerance both forms run to in the time-to-minimum leg: the tightest both "
+                         "reach on their own gradients at 262,144 sites (the FP64 finite-difference gradient floors "
+                         "near 5e-6, the mixed one near 1.5e-5 to 2.5e-5)")
     ap.add_argument("--case", choices=["bench", "profile", "ttm", "dmd", "batch"], default="bench",
                     help="profile: the small untimed case used for ncu captures")
     ap.add_argument("--case-cells", type=int, default=40)

@@ -202,7 +202,7 @@ a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, d
  * in the reference.  Inputs dX (4N doubles) and outputs df (1 double), dG
  * (4N doubles) are device pointers; the context supplies the neighbor lists
  * (build them first) and the occupancy; pass 2 visits pairs from both
- * sides.  All scratch lives in one fixed device array of about 6.1 MB that
+ * sides.  All scratch lives in one fixed device array of about 5.8 MB that
  * every GPU loading the library keeps until the process exits, so problems
  * above 131,072 sites are rejected with A2C_ERR_INVALID.  The first call on
  * a device finds the array's address and loads constant tables into it

