@@ -46,6 +46,7 @@ struct GridArgs {
   const float4 *Xf = nullptr;
   const unsigned *qmax_bits = nullptr;
   float boxf[3] = {0.f, 0.f, 0.f}, invboxf[3] = {0.f, 0.f, 0.f}, Lmaxf = 0.f, rcf = 0.f;
+  float rc2f = 0.f, A75f = 0.f, A125f = 0.f;  // the FP64 thresholds rounded to float
 };
 
 __device__ __forceinline__ int cell_coord(const GridArgs &g, double x, int d) {
@@ -96,9 +97,14 @@ __device__ __forceinline__ float prefilter_guard(const GridArgs &g) {
   const float qmax = __uint_as_float(*g.qmax_bits);
   return 1e-4f + 1.9073486328125e-6f * (qmax + g.Lmaxf + g.rcf);  // 2^-19 (qmax + L + rc)
 }
-__device__ __forceinline__ bool prefilter(const GridArgs &g, float4 fi, int64_t j, float lim, int m[3]) {
+// The FP32 pass over one candidate: coordinate differences with the image
+// m, and their squared length.  false: farther than rc + guard (rejected).
+__device__ __forceinline__ bool prefilter(const GridArgs &g, float4 fi, int64_t j, float lim, int m[3], float dd[3],
+                                          float &d2f) {
   const float4 fj = g.Xf[j];
-  float dd[3] = {fj.x - fi.x, fj.y - fi.y, fj.z - fi.z};
+  dd[0] = fj.x - fi.x;
+  dd[1] = fj.y - fi.y;
+  dd[2] = fj.z - fi.z;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     m[d] = 0;
@@ -109,18 +115,45 @@ __device__ __forceinline__ bool prefilter(const GridArgs &g, float4 fi, int64_t 
     }
     if (fabsf(dd[d]) > lim) return false;
   }
-  return dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2] <= lim * lim;
+  d2f = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
+  return d2f <= lim * lim;
 }
 
-// Candidate j of site i: the prefilter, then the FP64 test.  lim <= 0
+// Whether the FP32 values decide every comparison the FP64 test and the
+// shell counts make: each |coordinate difference| at least guard inside rc,
+// and d^2 at least `band` away from rc^2, 0.75 a^2 and 1.25 a^2.  A
+// coordinate difference is off by at most guard/4 (see prefilter_guard), so
+// d^2 is off by at most 2 sqrt(3) |d| guard/4 + 3 (guard/4)^2 plus three
+// FP32 roundings of d^2, which band = 2 guard (rc + 1) + 1e-5 bounds for
+// every d up to rc + guard.
+__device__ __forceinline__ bool fp32_decides(const GridArgs &g, const float dd[3], float d2f, float guard) {
+  const float band = 2.0f * guard * (g.rcf + 1.0f) + 1e-5f, inner = g.rcf - guard;
+  return fabsf(dd[0]) < inner && fabsf(dd[1]) < inner && fabsf(dd[2]) < inner && d2f < g.rc2f - band &&
+         fabsf(d2f - g.A75f) > band && fabsf(d2f - g.A125f) > band;
+}
+
+__device__ __forceinline__ uint32_t encode(int64_t j, const int m[3]) {
+  return (uint32_t)j | ((uint32_t)((m[0] + 1) + 3 * (m[1] + 1) + 9 * (m[2] + 1)) << kIdBits);
+}
+
+// Candidate j of site i.  The FP32 pass rejects everything farther than
+// rc + guard and accepts, with its d^2, every pair whose decisions it
+// settles (fp32_decides: nearly all); the rest take the FP64 test.  lim <= 0
 // (the prefilter cannot be used: a periodic box of at most 2 (rc + guard))
-// takes the image from the FP64 division instead.
+// takes the image from the FP64 division and the FP64 test.
 __device__ __forceinline__ bool pair_test(const GridArgs &g, int64_t i, float4 fi, float lim, int64_t j,
                                           uint32_t &entry, double &d2) {
   int m[3];
   if (i == j) return false;
   if (lim > 0.0f) {
-    if (!prefilter(g, fi, j, lim, m)) return false;
+    float dd[3], d2f;
+    if (!prefilter(g, fi, j, lim, m, dd, d2f)) return false;
+    if (fp32_decides(g, dd, d2f, lim - g.rcf) && m[0] >= -1 && m[0] <= 1 && m[1] >= -1 && m[1] <= 1 && m[2] >= -1 &&
+        m[2] <= 1) {
+      entry = encode(j, m);
+      d2 = (double)d2f;
+      return true;
+    }
   } else {
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -302,11 +335,9 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, Src src, const 
       const uint32_t ent = nbr[t];
       const int64_t j = ent & kIdMask;
       if (j < g.nPd) continue;
-      const int code = (int)(ent >> kIdBits);  // the entry's image: (mx+1) + 3(my+1) + 9(mz+1)
-      const int m[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
       uint32_t en;
       double d2;
-      if (exact_test(g, i, j, m, en, d2) && d2 < g.A75) {
+      if (pair_test(g, i, fi, lim, j, en, d2) && d2 < g.A75) {
         if (w1 < hh1_off[h + 1]) hh1[w1] = (int)(j - g.nPd);
         ++w1;
       }
@@ -364,6 +395,9 @@ int64_t make_grid(const a2c_gpp_ctx *c, const double *h_X, double cut, GridArgs 
   g.A75 = p.a_Pd * p.a_Pd * 0.75;
   g.A125 = p.a_Pd * p.a_Pd * 1.25;
   g.rcf = (float)cut;
+  g.rc2f = (float)g.rc2;
+  g.A75f = (float)g.A75;
+  g.A125f = (float)g.A125;
   for (int d = 0; d < 3; ++d)
     if (p.periodic[d]) {
       g.boxf[d] = (float)p.box[d];

@@ -182,10 +182,13 @@ def traffic_from_ncu(csv_path: str, sites: int, bench_sites: int = 262144) -> di
     return out
 
 
-def write_traffic(csv_path: str, sites: int) -> dict:
-    """profiles/traffic.json from an ncu capture of the profile case, keyed
-    by the hash of the kernel sources it was captured with."""
-    k = traffic_from_ncu(csv_path, sites)
+def write_traffic(csv_paths: str, sites: int) -> dict:
+    """profiles/traffic.json from ncu captures of the profile case (one CSV
+    per captured kernel, comma-separated paths), keyed by the hash of the
+    kernel sources they were captured with."""
+    k = {}
+    for path in csv_paths.split(","):
+        k.update(traffic_from_ncu(path, sites))
     doc = {"source_sha16": kernel_source_sha(), "captured_sites": sites, "scaled_to_sites": 262144,
            "bytes_per_launch": k,
            "note": "dram__bytes_read.sum + dram__bytes_write.sum per launch (ncu starts each launch with flushed "
@@ -922,8 +925,8 @@ def main():
     ap.add_argument("--batch-stride", type=int, default=16, help="every k-th instance forms the looped subset")
     ap.add_argument("--batch-mixed-only", action="store_true",
                     help="batched case: only the mixed-precision batch minimization")
-    ap.add_argument("--traffic-from", metavar="CSV",
-                    help="write profiles/traffic.json from an ncu CSV of the profile case (--case-cells cells) "
+    ap.add_argument("--traffic-from", metavar="CSV[,CSV...]",
+                    help="write profiles/traffic.json from ncu CSVs of the profile case (--case-cells cells) "
                          "and exit")
     args = ap.parse_args()
     if args.traffic_from:
