@@ -254,6 +254,23 @@ __global__ void k_cell_fill(GridArgs g, const int *cell, const int64_t *cstart, 
   items[cstart[c] + slot] = (int)s;
 }
 
+// Each cell's sites in increasing id (the fill above leaves them in the
+// order its atomics ran).
+__global__ void k_cell_sort(int64_t ncell, const int64_t *cstart, int *items) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int64_t b = cstart[c], e = cstart[c + 1];
+  for (int64_t t = b + 1; t < e; ++t) {
+    const int v = items[t];
+    int64_t u = t - 1;
+    while (u >= b && items[u] > v) {
+      items[u + 1] = items[u];
+      --u;
+    }
+    items[u + 1] = v;
+  }
+}
+
 // Counts per site; npd, shell and hh1count may be null (extended lists).
 template <class Src>
 __global__ void __launch_bounds__(kBlock) k_nbr_count(GridArgs g, Src src, int64_t *count, int *npd,
@@ -296,28 +313,9 @@ __global__ void __launch_bounds__(kBlock) k_nbr_count(GridArgs g, Src src, int64
   if (n > kMaxPerSite) atomicOr(status, kStatusOverflow);
 }
 
-// Fills the lists (sorted by id); hh1 may be null (extended lists).
-template <class Src>
-__global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, Src src, const int64_t *off, uint32_t *nbr,
-                                                     const int64_t *hh1_off, int *hh1, int *status) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= g.N) return;
-  const int64_t b = off[i], e = off[i + 1];
-  int64_t w = b;
-  const float4 fi = g.Xf[i];
-  const float lim = prefilter_lim(g);
-  src.each(g, i, [&](int64_t j) {
-    uint32_t en;
-    double d2;
-    if (!pair_test(g, i, fi, lim, j, en, d2)) return;
-    if (w < e) nbr[w] = en;
-    ++w;
-  });
-  if (w != e) {
-    atomicOr(status, kStatusBadIndex);
-    return;
-  }
-  // insertion sort of the segment by global id
+// Insertion sort of nbr[b, e) by global id; cheap when the entries arrive
+// nearly sorted, as they do here (see k_nbr_fill).
+__device__ __forceinline__ void sort_by_id(uint32_t *nbr, int64_t b, int64_t e) {
   for (int64_t t = b + 1; t < e; ++t) {
     const uint32_t v = nbr[t];
     const uint32_t key = v & kIdMask;
@@ -328,6 +326,41 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, Src src, const 
     }
     nbr[u + 1] = v;
   }
+}
+
+// Fills the lists (sorted by id); hh1 may be null (extended lists).  The Pd
+// neighbors go to the head of the list (npd of them, from the count pass)
+// and the H neighbors after them, so each part is sorted on its own: the
+// candidates arrive as runs sorted by id (cells' site lists are sorted,
+// cells are visited in the order site ids follow on lattice inputs, an
+// extended list is sorted), which leaves the insertion sort little to move.
+template <class Src>
+__global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, Src src, const int64_t *off, const int *npd,
+                                                     uint32_t *nbr, const int64_t *hh1_off, int *hh1, int *status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.N) return;
+  const int64_t b = off[i], e = off[i + 1], m = b + npd[i];
+  int64_t wP = b, wH = m;
+  const float4 fi = g.Xf[i];
+  const float lim = prefilter_lim(g);
+  src.each(g, i, [&](int64_t j) {
+    uint32_t en;
+    double d2;
+    if (!pair_test(g, i, fi, lim, j, en, d2)) return;
+    if (j < g.nPd) {
+      if (wP < m) nbr[wP] = en;
+      ++wP;
+    } else {
+      if (wH < e) nbr[wH] = en;
+      ++wH;
+    }
+  });
+  if (wP != m || wH != e) {
+    atomicOr(status, kStatusBadIndex);
+    return;
+  }
+  sort_by_id(nbr, b, m);
+  sort_by_id(nbr, m, e);
   if (hh1 && i >= g.nPd) {
     const int64_t h = i - g.nPd;
     int64_t w1 = hh1_off[h];
@@ -462,7 +495,7 @@ a2c_status make_lists(a2c_gpp_ctx *c, const GridArgs &g0, Src src, bool ext) {
   const int64_t N = c->N;
   const a2c_gpp_params &p = c->p;
   cudaStream_t st = c->stream;
-  DevBuf counts(st), hh1c(st), maxc(st), xf(st), qmax(st);
+  DevBuf counts(st), hh1c(st), maxc(st), xf(st), qmax(st), npd_ext(st);
   GridArgs g = g0;  // with the prefilter's positions
   A2C_CUDA(cudaMallocAsync(&xf.p, sizeof(float4) * std::max<int64_t>(N, 1), st));
   A2C_CUDA(cudaMallocAsync(&qmax.p, sizeof(unsigned), st));
@@ -480,8 +513,11 @@ a2c_status make_lists(a2c_gpp_ctx *c, const GridArgs &g0, Src src, bool ext) {
   A2C_CUDA(cudaMemsetAsync(hh1c.p, 0, sizeof(int64_t) * (p.nH + 1), st));
   A2C_CUDA(cudaMemsetAsync(maxc.p, 0, sizeof(int), st));
   int64_t *off = ext ? c->d_ext_off : c->d_off;
+  // the Pd head of each list (the extended lists keep theirs only for the fill)
+  if (ext) A2C_CUDA(cudaMallocAsync(&npd_ext.p, sizeof(int) * std::max<int64_t>(N, 1), st));
+  int *npd = ext ? (int *)npd_ext.p : c->d_npd;
   if (N > 0) {
-    k_nbr_count<Src><<<grid_for(N, kBlock), kBlock, 0, st>>>(g, src, (int64_t *)counts.p, ext ? nullptr : c->d_npd,
+    k_nbr_count<Src><<<grid_for(N, kBlock), kBlock, 0, st>>>(g, src, (int64_t *)counts.p, npd,
                                                              ext ? nullptr : (int64_t *)hh1c.p,
                                                              ext ? nullptr : c->d_shell, c->d_status);
     A2C_CUDA(cudaGetLastError());
@@ -509,7 +545,7 @@ a2c_status make_lists(a2c_gpp_ctx *c, const GridArgs &g0, Src src, bool ext) {
     c->max_neighbors = maxn;
   }
   if (N > 0) {
-    k_nbr_fill<Src><<<grid_for(N, kBlock), kBlock, 0, st>>>(g, src, off, ext ? c->d_ext_nbr : c->d_nbr,
+    k_nbr_fill<Src><<<grid_for(N, kBlock), kBlock, 0, st>>>(g, src, off, npd, ext ? c->d_ext_nbr : c->d_nbr,
                                                             c->d_hh1_off, ext ? nullptr : c->d_hh1, c->d_status);
     A2C_CUDA(cudaGetLastError());
   }
@@ -549,6 +585,7 @@ a2c_status lists_from_cells(a2c_gpp_ctx *c, const double *h_X, double cut, bool 
   if (N > 0) {
     k_cell_fill<<<grid_for(N, 256), 256, 0, st>>>(g, (const int *)cell.p, (const int64_t *)cstart.p,
                                                    (int *)cfill.p, (int *)items.p);
+    k_cell_sort<<<grid_for(ncell, 256), 256, 0, st>>>(ncell, (const int64_t *)cstart.p, (int *)items.p);
     A2C_CUDA(cudaGetLastError());
   }
   return make_lists(c, g, CellSrc{(const int64_t *)cstart.p, (const int *)items.p}, ext);
