@@ -308,6 +308,7 @@ a2c_status a2c_gpp_create(const a2c_gpp_params *p, a2c_gpp_ctx **out) {
   if (!s) s = dalloc(&c->d_hh1_off, (int64_t)p->nH + 1);
   for (int d = 0; d < 3; ++d) c->list_reach[d] = HUGE_VAL;  // no lists yet
   if (!s && (!p->periodic[0] || !p->periodic[1] || !p->periodic[2])) s = dalloc(&c->d_xlist, 4 * N);
+  if (!s) s = dalloc(&c->d_order, N);
   if (!s && cudaMallocHost((void **)&c->h_small, 64) != cudaSuccess) s = A2C_ERR_NOMEM;
   if (!s) {
     if (N > 0) {
@@ -338,7 +339,7 @@ a2c_status a2c_gpp_destroy(a2c_gpp_ctx *c) {
   for (void *p : {(void *)c->d_X, (void *)c->d_G, (void *)c->d_occ, (void *)c->d_rho, (void *)c->d_Fp,
                   (void *)c->d_Vs, (void *)c->d_Ss, (void *)c->d_red, (void *)c->d_status, (void *)c->d_off,
                   (void *)c->d_nbr, (void *)c->d_npd, (void *)c->d_shell, (void *)c->d_hh1_off, (void *)c->d_hh1,
-                  (void *)c->d_ext_off, (void *)c->d_ext_nbr, (void *)c->d_xref, (void *)c->d_xlist})
+                  (void *)c->d_ext_off, (void *)c->d_ext_nbr, (void *)c->d_xref, (void *)c->d_xlist, (void *)c->d_order})
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->h_small) cudaFreeHost(c->h_small);
@@ -925,16 +926,19 @@ a2c_status a2c_gpp_chem_potential(a2c_gpp_ctx *c, double gamma_bd, double *gamma
   if (cudaMemcpyAsync(dg, gamma, sizeof(double) * nH, cudaMemcpyHostToDevice, c->stream) ||
       cudaMemcpyAsync(dfull, full_H, sizeof(int) * nH, cudaMemcpyHostToDevice, c->stream))
     s = A2C_ERR_CUDA;
-  // minimizer.cpp:607-633: densities at the current state, always FP64
-  if (!s) s = launch_density64(c, c->d_X);
-  if (!s) s = launch_chem64(c, c->d_X, gamma_bd, dsend, dfull);
+  // minimizer.cpp:607-789: densities at the current state and the pair
+  // sums, FP64 (the reference's arithmetic) or, in the mixed form, with
+  // the pair quadrature in FP32
+  const bool mixed = c->p.precision == A2C_MIXED;
+  if (!s) s = mixed ? mixed_chem(c, c->d_X, dsend, dfull) : launch_density64(c, c->d_X);
+  if (!s && !mixed) s = launch_chem64(c, c->d_X, gamma_bd, dsend, dfull);
   if (!s) s = launch_gamma_update(c, dsend, gamma_bd, dg, dfull);
   if (!s && (cudaMemcpyAsync(gamma, dg, sizeof(double) * nH, cudaMemcpyDeviceToHost, c->stream) ||
              cudaMemcpyAsync(full_H, dfull, sizeof(int) * nH, cudaMemcpyDeviceToHost, c->stream)))
     s = A2C_ERR_CUDA;
   free_hscratch(c, dg, dsend, dx, dfull);
   if (s) return s;
-  c->has_density = true;
+  c->has_density = !mixed;
   return finish(c);
 }
 
@@ -1109,8 +1113,10 @@ a2c_status a2c_gpp_dmd_run(a2c_gpp_ctx *c, double *X, double *xH, double *gamma,
       if (s) break;
     }
     s = lbfgs_minimize(c, c->d_X, &dp->lbfgs, &f, &it, &fev, &gn, &why);  // minimizer.cpp:548
-    if (!s) s = launch_density64(c, c->d_X);                              // minimizer.cpp:607-633
-    if (!s) s = launch_chem64(c, c->d_X, dp->gamma_bd, dsend, dfull);     // minimizer.cpp:658-789
+    // minimizer.cpp:607-789: densities and chemical potential at the
+    // minimum (pair quadrature in FP32 for the mixed form)
+    if (!s) s = c->p.precision == A2C_MIXED ? mixed_chem(c, c->d_X, dsend, dfull) : launch_density64(c, c->d_X);
+    if (!s && c->p.precision != A2C_MIXED) s = launch_chem64(c, c->d_X, dp->gamma_bd, dsend, dfull);
     if (!s) s = launch_gamma_update(c, dsend, dp->gamma_bd, dg, dfull);   // minimizer.cpp:793-800
     if (!s) s = launch_dirichlet(c, dbd, n_bd, dp->gamma_bd, dp->x_bd, dg, dfull);  // boundaryconditions.cpp:47-51
     if (!s && cudaMemcpyAsync(dx, c->d_occ + c->p.nPd, sizeof(double) * nH, cudaMemcpyDeviceToDevice, st))

@@ -1510,12 +1510,17 @@ __global__ void k_dmd_record(const Inst *st, const double *macro, int *counters,
 
 // The launches of one outer step after its minimization (minimizer.cpp:588
 // -> boundaryconditions.cpp:30 -> integrate.cpp:9 -> calculateresults.cpp:8),
-// as the host-sequenced loop issues them.
+// as the host-sequenced loop issues them (the chemical potential's pair
+// quadrature in FP32 for the mixed form).
 a2c_status dmd_post(a2c_gpp_ctx *c, const a2c_dmd_params *dp, const DmdDev &dd) {
   cudaStream_t s = c->stream;
   const int nH = c->p.nH;
-  A2C_TRY(launch_density64(c, c->d_X));
-  A2C_TRY(launch_chem64(c, c->d_X, dp->gamma_bd, dd.send, dd.full));
+  if (c->p.precision == A2C_MIXED) {
+    A2C_TRY(mixed_chem(c, c->d_X, dd.send, dd.full));
+  } else {
+    A2C_TRY(launch_density64(c, c->d_X));
+    A2C_TRY(launch_chem64(c, c->d_X, dp->gamma_bd, dd.send, dd.full));
+  }
   A2C_TRY(launch_gamma_update(c, dd.send, dp->gamma_bd, dd.gamma, dd.full));
   A2C_TRY(launch_dirichlet(c, dd.bd, dd.n_bd, dp->gamma_bd, dp->x_bd, dd.gamma, dd.full));
   A2C_CUDA(cudaMemcpyAsync(dd.x, c->d_occ + c->p.nPd, sizeof(double) * nH, cudaMemcpyDeviceToDevice, s));

@@ -106,6 +106,10 @@ struct a2c_gpp_ctx {
   // how far apart a listed pair was at most then (infinite when unknown).
   double *d_xlist;
   double list_reach[3];
+  // visiting order of the mixed pair kernels (N; k_neighbors.cu), valid
+  // once a cell-list build made it
+  int *d_order;
+  bool has_order;
   // host staging
   double *h_pinned;
   int64_t h_pinned_n;
@@ -215,6 +219,9 @@ Tile effective_tile(const Tile &t, int64_t n_sites, int sms);
 // batched: prep + both passes over the listed sites (G, Vs, Ss; no objective)
 a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const BatchView &bv, const Tile &tile);
 a2c_status mixed_prepare(a2c_gpp_ctx *c);  // tables and buffers, before any graph capture
+// the H sites' chemical potential (k_chem64's d_send) with the pair
+// quadrature in FP32: pass 1 at dX, then the per-site sums; stream-ordered
+a2c_status mixed_chem(a2c_gpp_ctx *c, const double *dX, double *d_send, const int *d_full);
 // pass 2 pair visiting (A2C_PAIRS_*); the pairs-once index is rebuilt when
 // the lists change (mixed_lists_changed, called after every list build)
 a2c_status mixed_set_pair_mode(a2c_gpp_ctx *c, int mode);

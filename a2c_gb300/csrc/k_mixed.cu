@@ -38,6 +38,7 @@
 #include <mutex>
 #include <vector>
 
+#include "ddmath.cuh"
 #include "internal.cuh"
 #include "tables.h"
 
@@ -121,6 +122,7 @@ struct MixArgs {
   double *G, *Vs, *Ss;
   double T;
   BatchView bv;  // batched list launch (LIST kernels)
+  const int *order;  // visiting order of the single-system pass kernels (null: site order)
   const uint32_t *rev;  // pairs evaluated once (k_grad_once, k_grad_recv)
   const int *npre;
   float4 *recv;
@@ -168,8 +170,8 @@ __device__ __forceinline__ SiteRef<LIST> site_ref(const MixArgs &a, int64_t k) {
     r.sc = make_float3(g.sc[0], g.sc[1], g.sc[2]);
     r.T = g.T;
   } else {
-    r.s = k;
-    r.iPd = k < a.nPd;
+    r.s = a.order ? (int64_t)__ldg(&a.order[k]) : k;
+    r.iPd = r.s < a.nPd;
     r.sc = make_float3(a.sc[0], a.sc[1], a.sc[2]);
     r.T = a.T;
   }
@@ -447,11 +449,16 @@ struct SiteAcc {
   float s[5], c[5];  // Fq x, y, z, Fsigma, V  with Kahan compensations
 };
 
+// The gradient components are plain FP32 sums: compensating them measured
+// no change in the gradient's error (1.28e-5 relative to the FP64 form
+// either way at 262,144 sites -- it is set by the FP32 rounding of the pair
+// terms, not by their summation) and cost pass 2 3%.  The energy, whose
+// terms do not cancel, keeps its compensation.
 __device__ __forceinline__ void add_pair(SiteAcc &A, const PairAcc &p, float3 D, float wx, float vx) {
-  kahan(A.s[0], A.c[0], wx * fmaf(D.x, p.csum, p.e[0]));
-  kahan(A.s[1], A.c[1], wx * fmaf(D.y, p.csum, p.e[1]));
-  kahan(A.s[2], A.c[2], wx * fmaf(D.z, p.csum, p.e[2]));
-  kahan(A.s[3], A.c[3], wx * p.sig);
+  A.s[0] = fmaf(wx, fmaf(D.x, p.csum, p.e[0]), A.s[0]);
+  A.s[1] = fmaf(wx, fmaf(D.y, p.csum, p.e[1]), A.s[1]);
+  A.s[2] = fmaf(wx, fmaf(D.z, p.csum, p.e[2]), A.s[2]);
+  A.s[3] = fmaf(wx, p.sig, A.s[3]);
   kahan(A.s[4], A.c[4], vx * p.v);
 }
 
@@ -677,6 +684,74 @@ __global__ void __launch_bounds__(kBlock) k_grad_recv(MixArgs a) {
   }
 }
 
+// Chemical potential of the H sites in the mixed form (the DMD loop's
+// step after each minimization; minimizer.cpp:658-789): per H site the
+// quadrature sums  sum_{j in HPd} sum_k W [F'_Pd(rho_j) f_H(s) + phi_PdH(s)]
+// and  sum_{j in HH} x_j sum_k W [F'_H(rho_j) f_H(s) + phi_H(s)]  in FP32 with
+// compensated sums over neighbors (F' and F from pass 1 of the same state),
+// then F_H(rho_i), the correction terms (FP64; zero unless coe_* are set)
+// and log(x/(1-x)) + chi/(kB T) in FP64.  One thread per H site; send as in
+// k_chem64.
+__global__ void __launch_bounds__(kBlock) k_chem_mixed(MixArgs a, int nH, double coePd0, double coePd2, double coePd3,
+                                                       double coeH0, double coeH1, double coeH2, double coeH3,
+                                                       const double *occ64, const int *full, double *send) {
+  const int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= nH) return;
+  send[h] = 0.0;
+  if (full[h] == 1) return;
+  const int64_t s = (int64_t)a.nPd + h;
+  const int4 pi = a.P[s];
+  const float ui = kSqrt6 * __int_as_float(pi.w), ui2 = ui * ui;
+  const float3 sc = make_float3(a.sc[0], a.sc[1], a.sc[2]);
+  const int64_t b = a.off[s], m = b + a.npd[s], e = a.off[s + 1];
+  float acc = 0.0f, cmp = 0.0f;
+  for (int64_t t = b; t < e; ++t) {
+    const int64_t j = __ldg(&a.nbr[t]) & kIdMask;
+    const int4 pj = __ldg(&a.P[j]);
+    const float3 D = pair_vec(sc, pi, pj);
+    const float uj = kSqrt6 * __int_as_float(pj.w);
+    const float D2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
+    const float Ai = D2 + ui2, Aj = fmaf(uj, uj, D2);
+    const float Fj = __ldg(&a.FF[j].x);
+    const bool jPd = t < m;
+    const MorseExp &mo = jPd ? a.ex.pdh : a.ex.hh;
+    float part = 0.0f;
+    const float Dv[3] = {D.x, D.y, D.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      A2C_RADII(c, Dv[c])
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float r = s2[q] * rsq(s2[q]);
+        float phi, dphi;
+        morse(mo, r, phi, dphi);
+        part += fmaf(Fj, fH(a.ex, r), phi);
+      }
+    }
+    kahan(acc, cmp, part * (jPd ? a.W : a.W * __ldg(&a.occ[j])));
+  }
+  const double T = a.T;
+  double sum = (double)a.FF[s].y + (double)(acc - cmp);
+  if (coeH0 != 0.0 || coeH1 != 0.0 || coeH2 != 0.0 || coeH3 != 0.0 || coePd0 != 0.0) {
+    // the correction terms (minimizer.cpp:667-719), in FP64
+    const double nHPd = (double)(m - b);
+    double xs = 0.0;
+    for (int64_t t = m; t < e; ++t) xs += occ64[a.nbr[t] & kIdMask];
+    const double tmp = (coeH1 * nHPd) * nHPd + (2.0 * coeH2) * nHPd * xs + coeH3 * xs * xs;
+    sum += ((0.5 * T) * coeH0) * tmp;
+    for (int64_t t = b; t < e; ++t) {
+      const int64_t j = a.nbr[t] & kIdMask;
+      const int64_t bj = a.off[j], mj = bj + a.npd[j], ej = a.off[j + 1];
+      double xl = 0.0;
+      for (int64_t u = mj; u < ej; ++u) xl += occ64[a.nbr[u] & kIdMask];
+      if (t < m) sum += ((T * coePd0) * coePd2) * (double)(mj - bj) + ((T * coePd0) * coePd3) * xl;
+      else sum += occ64[j] * T * coeH0 * (coeH2 * (double)(mj - bj) + coeH3 * xl);
+    }
+  }
+  const double x0 = occ64[s];
+  if (x0 > 0.0 && x0 < 1.0) send[h] = dd::cr_log(x0 / (1.0 - x0)) + sum / (kB * T);
+}
+
 // The index of the pairs-once scheme for lists off/nbr over sites [0, N):
 // per site the count of neighbors with a smaller id (npre), per owned entry
 // the slot of the reverse entry (rev).  Sets *bad when a list is not
@@ -829,6 +904,15 @@ const ExpTerms &exp_consts() {
 // once = true: pass 2 evaluates every pair once (k_grad_once + k_grad_recv;
 // a.rev, a.npre, a.recv set), else from both sides (k_grad_mixed).
 constexpr int kRecvTps = 8;  // lanes per site summing the received shares
+// The pass kernels walk the sites in the cell-coherent order of the last
+// cell-list build (Pd sites cell by cell, then H sites), so the sites of a
+// block are spatially close and their neighbors' state is reused from L1.
+// The order does not change any site's arithmetic.
+#ifndef A2C_SITE_ORDER
+#define A2C_SITE_ORDER 1
+#endif
+const int *site_order(const a2c_gpp_ctx *c) { return (A2C_SITE_ORDER && c->has_order) ? c->d_order : nullptr; }
+
 // Persistent grid size of a kernel at a block size on the current device
 // (resident blocks x SMs), computed once per (kernel, block, device) under
 // a lock, with the dynamic shared-memory limit raised on that device first.
@@ -886,9 +970,11 @@ void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, boo
     case 512: launch_grad<TPS, LIST, 512>(a, st, once); break;
     default: launch_grad<TPS, LIST, 256>(a, st, once); break;
   }
-  if (once) {
+  if (once) {  // in site order: the sites of a warp write one contiguous run of G
+    MixArgs r = a;
+    r.order = nullptr;
     const void *fn = (const void *)k_grad_recv<kRecvTps, LIST>;
-    k_grad_recv<kRecvTps, LIST><<<persistent_grid(a.N, kBlock / kRecvTps, grid_cap(fn, kBlock, 0)), kBlock, 0, st>>>(a);
+    k_grad_recv<kRecvTps, LIST><<<persistent_grid(a.N, kBlock / kRecvTps, grid_cap(fn, kBlock, 0)), kBlock, 0, st>>>(r);
   }
   if (ev) cudaEventRecord(ev[3], st);
 }
@@ -1129,6 +1215,7 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   a.npre = M->npre;
   a.recv = M->recv;
   a.Gown = M->Gown;
+  a.order = site_order(c);
   if (ev) cudaEventRecord(ev[0], c->stream);
   if (N > 0) {
     const SpanArgs sg = span_args(c);
@@ -1195,6 +1282,51 @@ a2c_status mixed_eval_list(a2c_gpp_ctx *c, const double *dX, double *dG, const B
   k_prep_list<<<(unsigned)std::min<int64_t>(grid_for(N, 256), prep_cap), 256, 0, c->stream>>>(
       dX, c->d_occ, bv, M->P, M->occ, c->d_xlist, c->d_status);
   launch_tile(a, c->stream, nullptr, once, effective_tile(tile, N, device_sms(c->device)), true);
+  A2C_CUDA(cudaGetLastError());
+  return A2C_OK;
+}
+
+}  // namespace a2c
+
+namespace a2c {
+
+a2c_status mixed_chem(a2c_gpp_ctx *c, const double *dX, double *d_send, const int *d_full) {
+  const int nH = c->p.nH;
+  if (nH == 0) return A2C_OK;
+  A2C_TRY(ensure_mixed(c));
+  Mixed *M = c->mixed;
+  const int64_t N = c->N;
+  MixArgs a{};
+  a.N = N;
+  a.nPd = c->p.nPd;
+  a.W = (float)c->p.QWp;
+  double k[3];
+  for (int d = 0; d < 3; ++d) {
+    const double S = c->p.periodic[d] ? c->p.box[d] : kFreeSpan;
+    k[d] = 4294967296.0 / S;
+    a.sc[d] = (float)(S / 4294967296.0);
+  }
+  a.P = M->P;
+  a.occ = M->occ;
+  a.off = c->d_off;
+  a.nbr = c->d_nbr;
+  a.npd = c->d_npd;
+  a.ex = exp_consts();
+  a.tabPair = M->tabPair;
+  a.tabEmb = M->tabEmb;
+  a.FF = M->FF;
+  a.T = c->p.T;
+  // the state's fixed-point form and pass 1 (F and F' of every site)
+  k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], M->P, M->occ, span_args(c));
+  const Tile t = effective_tile(mixed_tile(c), N, device_sms(c->device));
+  switch (t.rho_block) {
+    case 512: launch_rho<1, false, 512>(a, c->stream); break;
+    case 768: launch_rho<1, false, 768>(a, c->stream); break;
+    default: launch_rho<1, false, 256>(a, c->stream); break;
+  }
+  const double *cp = c->p.coe_Pd, *ch = c->p.coe_H;
+  k_chem_mixed<<<grid_for(nH, kBlock), kBlock, 0, c->stream>>>(a, nH, cp[0], cp[2], cp[3], ch[0], ch[1], ch[2], ch[3],
+                                                               c->d_occ, d_full, d_send);
   A2C_CUDA(cudaGetLastError());
   return A2C_OK;
 }

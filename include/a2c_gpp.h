@@ -287,7 +287,10 @@ a2c_status a2c_gpp_minimize(a2c_gpp_ctx *ctx, double *X, const a2c_lbfgs_params 
 
 /* Occupancy gradient / chemical potential at the current state.  Replaces
  * Minimizer::calculateChemicalPotential (minimizer.cpp:588-802); gamma and
- * full_H are nH arrays, read and updated in place. */
+ * full_H are nH arrays, read and updated in place.  A mixed-precision
+ * context evaluates the pair quadrature in FP32 (compensated per-site sums,
+ * F and F' from its pass 1) and the rest in FP64; an FP64 context follows
+ * the reference's arithmetic. */
 a2c_status a2c_gpp_chem_potential(a2c_gpp_ctx *ctx, double gamma_bd, double *gamma, int *full_H);
 
 /* Dirichlet condition on the listed H sites: gamma = gamma_bd, full_H = 1,

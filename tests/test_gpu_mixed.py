@@ -266,3 +266,53 @@ def test_tile_block_sizes_do_not_change_results(gpu):
         tile, cands = g.autotune_tile(reps=2)
         assert tile[0] in (1, 2, 4, 8) and tile[1] in (256, 512, 768) and tile[2] in (128, 256, 512)
         assert g.tile() == tile and len(cands) == 10 and all(ms > 0 for _, ms in cands)
+
+
+def test_mixed_chemical_potential_follows_fp64(gpu):
+    """The mixed form's chemical potential (pair quadrature in FP32,
+    compensated per-site sums, F' from its pass 1; the correction terms and
+    log(x/(1-x)) in FP64) against the FP64 form's on the same state: gamma
+    within 1e-4 absolute (gamma ~ chi/kT ~ 1e2 here, so ~1e-6 relative) and
+    the same full_H flags, with and without correction coefficients."""
+    X, xH, box, per, nPd, nH, pb = make("slab_4x5x6")
+    rng = np.random.default_rng(5)
+    gamma0 = rng.normal(size=nH)
+    full0 = (rng.random(nH) < 0.1).astype(np.int32)
+    xH = xH.copy()
+    xH[:4] = [1e-3, 0.99995, 0.5, 0.2]
+    for coe in (dict(), dict(coe_Pd=(0.3, 0.0, 0.02, -0.01), coe_H=(0.2, 0.01, -0.03, 0.004))):
+        res = {}
+        for prec in ("fp64", "mixed"):
+            with A.Gpp(nPd, nH, box=box, periodic=per, precision=prec, **coe) as g:
+                g.set_occupancy(xH)
+                g.build_neighbors(X)
+                res[prec] = g.chem_potential(2.5, gamma0, full0)
+        g64, f64 = res["fp64"]
+        gm, fm = res["mixed"]
+        err = np.abs(gm - g64).max()
+        print(f"coe={bool(coe)}: max |dgamma| = {err:.2e}, |gamma| max {np.abs(g64).max():.1f}")
+        assert np.array_equal(fm, f64)
+        assert err < 1e-4
+
+
+def test_visiting_order_does_not_change_results(gpu):
+    """A context whose lists came from a cell-list build walks its sites in
+    the cell-coherent order of that build; a fresh context given the same
+    lists (no build, so no such order) walks them in site order.  A site's
+    arithmetic is the same either way: identical bits."""
+    from a2c_gb300 import _native as N
+
+    X, xH, box, per, nPd, nH, pb = make("config2_16cube")
+    with A.Gpp(nPd, nH, box=box, periodic=per, precision="mixed") as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        g.set_tile(2, 512, 256)
+        f1, G1 = g.eval(X)
+        lists = {lid: g.neighbors(lid) for lid in (N.LIST_PDPD, N.LIST_PDH, N.LIST_HPD, N.LIST_HH, N.LIST_HH1)}
+        shells = g.shell_counts()
+    with A.Gpp(nPd, nH, box=box, periodic=per, precision="mixed") as g:
+        g.set_occupancy(xH)
+        g.set_neighbor_lists(X, lists, shells)
+        g.set_tile(2, 512, 256)
+        f2, G2 = g.eval(X)
+    assert f1 == f2 and np.array_equal(G1, G2)
