@@ -308,7 +308,6 @@ a2c_status a2c_gpp_create(const a2c_gpp_params *p, a2c_gpp_ctx **out) {
   if (!s) s = dalloc(&c->d_hh1_off, (int64_t)p->nH + 1);
   for (int d = 0; d < 3; ++d) c->list_reach[d] = HUGE_VAL;  // no lists yet
   if (!s && (!p->periodic[0] || !p->periodic[1] || !p->periodic[2])) s = dalloc(&c->d_xlist, 4 * N);
-  if (!s) s = dalloc(&c->d_order, N);
   if (!s && cudaMallocHost((void **)&c->h_small, 64) != cudaSuccess) s = A2C_ERR_NOMEM;
   if (!s) {
     if (N > 0) {
@@ -339,7 +338,7 @@ a2c_status a2c_gpp_destroy(a2c_gpp_ctx *c) {
   for (void *p : {(void *)c->d_X, (void *)c->d_G, (void *)c->d_occ, (void *)c->d_rho, (void *)c->d_Fp,
                   (void *)c->d_Vs, (void *)c->d_Ss, (void *)c->d_red, (void *)c->d_status, (void *)c->d_off,
                   (void *)c->d_nbr, (void *)c->d_npd, (void *)c->d_shell, (void *)c->d_hh1_off, (void *)c->d_hh1,
-                  (void *)c->d_ext_off, (void *)c->d_ext_nbr, (void *)c->d_xref, (void *)c->d_xlist, (void *)c->d_order})
+                  (void *)c->d_ext_off, (void *)c->d_ext_nbr, (void *)c->d_xref, (void *)c->d_xlist})
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->h_small) cudaFreeHost(c->h_small);

@@ -106,10 +106,6 @@ struct a2c_gpp_ctx {
   // how far apart a listed pair was at most then (infinite when unknown).
   double *d_xlist;
   double list_reach[3];
-  // visiting order of the mixed pair kernels (N; k_neighbors.cu), valid
-  // once a cell-list build made it
-  int *d_order;
-  bool has_order;
   // host staging
   double *h_pinned;
   int64_t h_pinned_n;

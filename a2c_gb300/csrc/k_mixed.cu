@@ -122,7 +122,6 @@ struct MixArgs {
   double *G, *Vs, *Ss;
   double T;
   BatchView bv;  // batched list launch (LIST kernels)
-  const int *order;  // visiting order of the single-system pass kernels (null: site order)
   const uint32_t *rev;  // pairs evaluated once (k_grad_once, k_grad_recv)
   const int *npre;
   float4 *recv;
@@ -170,8 +169,8 @@ __device__ __forceinline__ SiteRef<LIST> site_ref(const MixArgs &a, int64_t k) {
     r.sc = make_float3(g.sc[0], g.sc[1], g.sc[2]);
     r.T = g.T;
   } else {
-    r.s = a.order ? (int64_t)__ldg(&a.order[k]) : k;
-    r.iPd = r.s < a.nPd;
+    r.s = k;
+    r.iPd = k < a.nPd;
     r.sc = make_float3(a.sc[0], a.sc[1], a.sc[2]);
     r.T = a.T;
   }
@@ -904,15 +903,6 @@ const ExpTerms &exp_consts() {
 // once = true: pass 2 evaluates every pair once (k_grad_once + k_grad_recv;
 // a.rev, a.npre, a.recv set), else from both sides (k_grad_mixed).
 constexpr int kRecvTps = 8;  // lanes per site summing the received shares
-// The pass kernels walk the sites in the cell-coherent order of the last
-// cell-list build (Pd sites cell by cell, then H sites), so the sites of a
-// block are spatially close and their neighbors' state is reused from L1.
-// The order does not change any site's arithmetic.
-#ifndef A2C_SITE_ORDER
-#define A2C_SITE_ORDER 1
-#endif
-const int *site_order(const a2c_gpp_ctx *c) { return (A2C_SITE_ORDER && c->has_order) ? c->d_order : nullptr; }
-
 // Persistent grid size of a kernel at a block size on the current device
 // (resident blocks x SMs), computed once per (kernel, block, device) under
 // a lock, with the dynamic shared-memory limit raised on that device first.
@@ -970,11 +960,9 @@ void launch_pair_kernels(const MixArgs &a, cudaStream_t st, cudaEvent_t *ev, boo
     case 512: launch_grad<TPS, LIST, 512>(a, st, once); break;
     default: launch_grad<TPS, LIST, 256>(a, st, once); break;
   }
-  if (once) {  // in site order: the sites of a warp write one contiguous run of G
-    MixArgs r = a;
-    r.order = nullptr;
+  if (once) {
     const void *fn = (const void *)k_grad_recv<kRecvTps, LIST>;
-    k_grad_recv<kRecvTps, LIST><<<persistent_grid(a.N, kBlock / kRecvTps, grid_cap(fn, kBlock, 0)), kBlock, 0, st>>>(r);
+    k_grad_recv<kRecvTps, LIST><<<persistent_grid(a.N, kBlock / kRecvTps, grid_cap(fn, kBlock, 0)), kBlock, 0, st>>>(a);
   }
   if (ev) cudaEventRecord(ev[3], st);
 }
@@ -1215,7 +1203,6 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   a.npre = M->npre;
   a.recv = M->recv;
   a.Gown = M->Gown;
-  a.order = site_order(c);
   if (ev) cudaEventRecord(ev[0], c->stream);
   if (N > 0) {
     const SpanArgs sg = span_args(c);

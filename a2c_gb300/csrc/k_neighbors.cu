@@ -254,33 +254,6 @@ __global__ void k_cell_fill(GridArgs g, const int *cell, const int64_t *cstart, 
   items[cstart[c] + slot] = (int)s;
 }
 
-// The site visiting order of the mixed pair kernels (c->d_order): the Pd
-// sites cell by cell, then the H sites cell by cell (within a cell in
-// increasing id), so consecutive sites -- a block's -- are spatially close
-// and their neighbors' state stays in L1, while a warp still sees one
-// species.  Per cell: its Pd count (items are id-sorted, Pd ids first).
-__global__ void k_cell_npd(int64_t ncell, const int64_t *cstart, const int *items, int nPd, int64_t *npd_cell) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncell) return;
-  int64_t t = cstart[c];
-  const int64_t e = cstart[c + 1];
-  while (t < e && items[t] < nPd) ++t;
-  npd_cell[c] = t - cstart[c];
-}
-// pd_off: exclusive scan of the per-cell Pd counts
-__global__ void k_cell_order(int64_t ncell, const int64_t *cstart, const int *items, int nPd, const int64_t *pd_off,
-                             int *order) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncell) return;
-  const int64_t b = cstart[c], e = cstart[c + 1], p0 = pd_off[c], h0 = (int64_t)nPd + (b - p0);
-  int64_t np = 0;
-  for (int64_t t = b; t < e; ++t) {
-    const int s = items[t];
-    if (s < nPd) order[p0 + np++] = s;
-    else order[h0 + (t - b - np)] = s;
-  }
-}
-
 // Each cell's sites in increasing id (the fill above leaves them in the
 // order its atomics ran).
 __global__ void k_cell_sort(int64_t ncell, const int64_t *cstart, int *items) {
@@ -615,24 +588,7 @@ a2c_status lists_from_cells(a2c_gpp_ctx *c, const double *h_X, double cut, bool 
     k_cell_sort<<<grid_for(ncell, 256), 256, 0, st>>>(ncell, (const int64_t *)cstart.p, (int *)items.p);
     A2C_CUDA(cudaGetLastError());
   }
-  A2C_TRY(make_lists(c, g, CellSrc{(const int64_t *)cstart.p, (const int *)items.p}, ext));
-  // the visiting order from this cell list (any cell build serves: the
-  // order only needs to be spatially coherent)
-  if (N > 0 && c->d_order) {
-    DevBuf npc(st), poff(st);
-    A2C_CUDA(cudaMallocAsync(&npc.p, sizeof(int64_t) * (ncell + 1), st));
-    A2C_CUDA(cudaMallocAsync(&poff.p, sizeof(int64_t) * (ncell + 1), st));
-    A2C_CUDA(cudaMemsetAsync(npc.p, 0, sizeof(int64_t) * (ncell + 1), st));
-    k_cell_npd<<<grid_for(ncell, 256), 256, 0, st>>>(ncell, (const int64_t *)cstart.p, (const int *)items.p,
-                                                     c->p.nPd, (int64_t *)npc.p);
-    A2C_CUDA(cudaGetLastError());
-    A2C_TRY(scan_exclusive((const int64_t *)npc.p, (int64_t *)poff.p, ncell + 1, st));
-    k_cell_order<<<grid_for(ncell, 256), 256, 0, st>>>(ncell, (const int64_t *)cstart.p, (const int *)items.p,
-                                                       c->p.nPd, (const int64_t *)poff.p, c->d_order);
-    A2C_CUDA(cudaGetLastError());
-    c->has_order = true;
-  }
-  return A2C_OK;
+  return make_lists(c, g, CellSrc{(const int64_t *)cstart.p, (const int *)items.p}, ext);
 }
 
 }  // namespace

@@ -294,25 +294,3 @@ def test_mixed_chemical_potential_follows_fp64(gpu):
         assert np.array_equal(fm, f64)
         assert err < 1e-4
 
-
-def test_visiting_order_does_not_change_results(gpu):
-    """A context whose lists came from a cell-list build walks its sites in
-    the cell-coherent order of that build; a fresh context given the same
-    lists (no build, so no such order) walks them in site order.  A site's
-    arithmetic is the same either way: identical bits."""
-    from a2c_gb300 import _native as N
-
-    X, xH, box, per, nPd, nH, pb = make("config2_16cube")
-    with A.Gpp(nPd, nH, box=box, periodic=per, precision="mixed") as g:
-        g.set_occupancy(xH)
-        g.build_neighbors(X)
-        g.set_tile(2, 512, 256)
-        f1, G1 = g.eval(X)
-        lists = {lid: g.neighbors(lid) for lid in (N.LIST_PDPD, N.LIST_PDH, N.LIST_HPD, N.LIST_HH, N.LIST_HH1)}
-        shells = g.shell_counts()
-    with A.Gpp(nPd, nH, box=box, periodic=per, precision="mixed") as g:
-        g.set_occupancy(xH)
-        g.set_neighbor_lists(X, lists, shells)
-        g.set_tile(2, 512, 256)
-        f2, G2 = g.eval(X)
-    assert f1 == f2 and np.array_equal(G1, G2)
