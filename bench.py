@@ -490,6 +490,17 @@ def run_batch_case(args):
     def reasons(r):
         return {int(k): int(v) for k, v in zip(*np.unique(r.reason, return_counts=True))}
 
+    def by_reason(r):
+        """Per stopping reason: instances, their sites and their atom-evals
+        (so that the work of instances that stalled above gatol is told
+        apart from that of converged ones)."""
+        out = {}
+        for k in np.unique(r.reason):
+            sel = r.reason == k
+            out[int(k)] = {"instances": int(sel.sum()), "sites": int(sizes[sel].sum()),
+                           "atom_evals": float((sizes[sel] * r.nfev[sel]).sum())}
+        return out
+
     res = {}
     with A.Batch(inst, precision="mixed", device=dev) as b:
         b.set_occupancy(xH)
@@ -506,7 +517,7 @@ def run_batch_case(args):
             evals = float((sizes * r.nfev).sum())
             res[name] = r
             out[name] = {"wall_s": wall, "device_s": r.seconds, "ticks": r.ticks, "atom_evals": evals,
-                         "atom_evals_per_s": evals / r.seconds, "reasons": reasons(r),
+                         "atom_evals_per_s": evals / r.seconds, "reasons": reasons(r), "by_reason": by_reason(r),
                          "mixed_iters_mean": float(r.mixed_iters.mean()),
                          "fp64_polish_iters_mean": float(r.fp64_iters.mean()),
                          "fp64_polish_iters_max": int(r.fp64_iters.max()), "nfev_max": int(r.nfev.max())}
