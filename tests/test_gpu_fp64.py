@@ -24,7 +24,7 @@ TOL_F = 1e-11
 TOL_G = 1e-11
 
 CASES = {
-    # name: (ncell, periodic, pos_std, sigma range, x_center, x_half, seed[, T])
+    # name: (ncell, periodic, pos_std, sigma range, x_center, x_half, seed[, T[, lattice options]])
     "free3": ((3, 3, 3), (0, 0, 0), 0.02, (0.10, 0.10), 0.05, 0.01, 1),
     "config1_6cube": ((6, 6, 6), (1, 1, 1), 0.02, (0.10, 0.10), 0.05, 0.01, 1),
     "slab_4x5x6": ((4, 5, 6), (1, 1, 0), 0.03, (0.08, 0.14), 0.15, 0.15, 7),
@@ -35,13 +35,24 @@ CASES = {
     # surfaces in z, x = 0.01, T = 400 K (24,576 sites)
     "config5_slab_16x16x12": ((16, 16, 12), (1, 1, 0), 0.02, (0.10, 0.10), 0.01, 0.0, 5, 400.0),
 }
+# the configurations' full sizes (objective, gradient and densities): the
+# coupled-DMD slab at 48^3 cells (884,736 sites) and the hydride-nucleus
+# lattice at 64^3 cells (2,097,152 sites)
+FULL_CASES = {
+    "config5_slab_48cube": ((48, 48, 48), (1, 1, 0), 0.02, (0.10, 0.10), 0.01, 0.0, 5, 400.0),
+    "config3_64cube_nucleus": ((64, 64, 64), (1, 1, 1), 0.02, (0.10, 0.10), 0.0, 0.0, 3, 300.0,
+                               dict(x_mode=1, x_matrix=0.02, x_nucleus=0.60, nucleus_radius=80.0,
+                                    interface_width=5.0)),
+}
 
 
 def make(case):
-    ncell, per, ps, sg, xc, xh, seed, *T = CASES[case]
+    ncell, per, ps, sg, xc, xh, seed, *rest = {**CASES, **FULL_CASES}[case]
+    T = rest[0] if rest else 300.0
+    extra = rest[1] if len(rest) > 1 else {}
     X, xH, surf, box, nPd, nH = A.lattice_fcc(ncell, periodic=per, pos_std=ps, sigma=sg, x_center=xc, x_half=xh,
-                                             seed=seed)
-    pb = O.Problem(nPd, nH, box=box, periodic=per, T=T[0] if T else 300.0)
+                                             seed=seed, **extra)
+    pb = O.Problem(nPd, nH, box=box, periodic=per, T=T)
     return X, xH, surf, box, per, nPd, nH, pb
 
 
@@ -106,6 +117,34 @@ def test_objective_gradient_fp64(gpu, case):
     assert np.array_equal(rho, rho_dev)
     assert np.array_equal(G, G_dev)
     assert f == f_dev
+
+
+@pytest.mark.parametrize("case", list(FULL_CASES))
+def test_objective_gradient_fp64_full_size(gpu, case):
+    """The full sizes: objective and gradient against the reference
+    arithmetic to the plain form's limit, densities bit for bit against the
+    device arithmetic (the oracle's correctly rounded pow makes a whole
+    device-arithmetic gradient take minutes at these sizes on the host)."""
+    X, xH, surf, box, per, nPd, nH, pb = make(case)
+    off, nbr, *_ = O.neighbors(pb, X)
+    f_ref, G_ref, rho_ref, _ = O.evaluate(pb, X, xH, off, nbr, mode=1)
+    with O.arithmetic("device"):
+        rho_dev = O.density(pb, X, xH, off, nbr)
+    del off, nbr
+    with gpp(nPd, nH, box, per, T=pb.p.T) as g:
+        g.set_occupancy(xH)
+        g.build_neighbors(X)
+        f, G = g.eval(X)
+        rho = g.density()
+    rel_f = abs(f - f_ref) / abs(f_ref)
+    rel_g = np.linalg.norm(G - G_ref) / np.linalg.norm(G_ref)
+    rel_rho = np.max(np.abs(rho - rho_ref) / np.maximum(np.abs(rho_ref), 1e-300))
+    print(f"{case} ({nPd + nH} sites): rel_f={rel_f:.3e} rel_G={rel_g:.3e} max_rel_rho={rel_rho:.3e}; "
+          f"rho equal to device arithmetic {np.array_equal(rho, rho_dev)}")
+    assert rel_rho < 1e-13
+    assert rel_f < TOL_F
+    assert rel_g < TOL_G
+    assert np.array_equal(rho, rho_dev)
 
 
 def test_eval_device_pointers(gpu):
