@@ -155,6 +155,17 @@ struct DeviceGuard {
   explicit DeviceGuard(int d) { cudaSetDevice(d); }
 };
 
+// Host memory the device can address directly (pinned or registered): its
+// device-side address, else null.
+const void *mapped(const void *p) {
+  cudaPointerAttributes a;
+  if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 a2c_status copy_in(a2c_gpp_ctx *c, double *dst, const double *src, int64_t n) {
   if (n <= 0) return A2C_OK;
   A2C_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
@@ -489,13 +500,10 @@ a2c_status a2c_gpp_get_state(a2c_gpp_ctx *c, double *X) {
 a2c_status a2c_gpp_build_neighbors(a2c_gpp_ctx *c, const double *X, int *max_neighbors) {
   if (!c || (!X && c->N > 0)) return A2C_ERR_INVALID;
   DeviceGuard g(c->device);
-  for (int64_t t = 0; t < 4 * c->N; ++t)
-    if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
-  for (int d = 0; d < 3; ++d)  // images are limited to one box length either way
-    if (c->p.periodic[d])
-      for (int64_t s = 0; s < c->N; ++s)
-        if (X[4 * s + d] < -0.5 * c->p.box[d] || X[4 * s + d] > 1.5 * c->p.box[d]) return A2C_ERR_INVALID;
-  A2C_TRY(copy_in(c, c->d_X, X, 4 * c->N));
+  // finite, and periodic coordinates within [-L/2, 3L/2] (images are limited
+  // to one box length either way): checked on the device
+  int moved = 0;
+  A2C_TRY(stage_positions(c, X, (uintptr_t)X % 8 == 0 ? (const double *)mapped(X) : nullptr, &moved));
   c->has_state = true;
   c->has_neighbors = false;
   c->has_density = false;
@@ -584,17 +592,14 @@ a2c_status a2c_gpp_update_neighbors(a2c_gpp_ctx *c, const double *X, int *max_ne
     return a2c_gpp_build_neighbors(c, X, max_neighbors);
   }
   DeviceGuard g(c->device);
-  for (int64_t t = 0; t < 4 * c->N; ++t)
-    if (!std::isfinite(X[t])) return A2C_ERR_NONFINITE;
-  for (int d = 0; d < 3; ++d)
-    if (c->p.periodic[d])
-      for (int64_t s = 0; s < c->N; ++s)
-        if (X[4 * s + d] < -0.5 * c->p.box[d] || X[4 * s + d] > 1.5 * c->p.box[d]) return A2C_ERR_INVALID;
-  A2C_TRY(copy_in(c, c->d_X, X, 4 * c->N));
+  // checked on the device: pinned X is read there directly, other memory
+  // is copied first
+  int moved = 0;
+  A2C_TRY(stage_positions(c, X, (uintptr_t)X % 8 == 0 ? (const double *)mapped(X) : nullptr, &moved));
   c->has_state = true;
   c->has_neighbors = false;
   c->has_density = false;
-  A2C_TRY(update_neighbors_device(c, X, rebuilt));
+  A2C_TRY(update_neighbors_device(c, X, rebuilt, moved));
   c->has_neighbors = true;
   A2C_TRY(mixed_lists_changed(c));
   if (max_neighbors) *max_neighbors = c->max_neighbors;
@@ -802,24 +807,14 @@ a2c_status a2c_gpp_profile_eval(a2c_gpp_ctx *c, const double *dX, double *df, do
   return check_status_word(c);
 }
 
-// Host memory the device can address directly (pinned or registered): its
-// device-side address, else null.
-const void *mapped(const void *p) {
-  cudaPointerAttributes a;
-  if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
-}
-
 a2c_status a2c_gpp_eval(a2c_gpp_ctx *c, const double *X, double *f, double *G) {
   if (!c || (!X && c->N > 0) || !f || (!G && c->N > 0)) return A2C_ERR_INVALID;
   if (!c->has_neighbors) return A2C_ERR_STATE;
   DeviceGuard g(c->device);
   // Mixed form with pinned caller buffers: the prep kernel reads X and pass 2
   // writes G through the coherent host link while they compute, instead of
-  // bulk copies before and after; the small results come back in one copy.
+  // bulk copies before and after; f and the status word come back through
+  // pinned memory the last kernel writes.
   const double *mX = (c->p.precision == A2C_MIXED && c->N > 0 && (uintptr_t)X % 32 == 0)
                          ? (const double *)mapped(X) : nullptr;  // read as double4
   double *mG = (mX && (uintptr_t)G % 8 == 0) ? (double *)mapped(G) : nullptr;
@@ -827,11 +822,14 @@ a2c_status a2c_gpp_eval(a2c_gpp_ctx *c, const double *X, double *f, double *G) {
   if (mX && mG && c->h_small) {
     c->has_state = true;
     double *d_f = c->d_red + 2 * 1024 + 8;
-    A2C_TRY(mixed_eval(c, mX, d_f, mG, nullptr, c->d_X));
+    double *hs = (double *)mapped(c->h_small);
+    A2C_TRY(mixed_eval(c, mX, d_f, mG, nullptr, c->d_X, hs));
     c->has_density = false;
-    A2C_CUDA(cudaMemcpyAsync(c->h_small, d_f, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    A2C_CUDA(cudaMemcpyAsync(c->h_small + 1, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    A2C_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+    if (!hs) {
+      A2C_CUDA(cudaMemcpyAsync(c->h_small, d_f, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      A2C_CUDA(cudaMemcpyAsync(c->h_small + 1, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      A2C_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+    }
     A2C_CUDA(cudaStreamSynchronize(c->stream));
     *f = c->h_small[0];
     int st = 0;
@@ -1101,7 +1099,7 @@ a2c_status a2c_gpp_dmd_run(a2c_gpp_ctx *c, double *X, double *xH, double *gamma,
     int it = 0, fev = 0, why = 0;
     if (k > 0 && dp->neighbor_update) {  // findNeighbors + findLocalNeighbors at the current positions
       if (c->skin > 0.0) {
-        s = update_neighbors_device(c, nullptr, nullptr);
+        s = update_neighbors_device(c, nullptr, nullptr, -1);
       } else {
         hX.resize((size_t)(4 * c->N));
         if (cudaMemcpyAsync(hX.data(), c->d_X, sizeof(double) * 4 * c->N, cudaMemcpyDeviceToHost, st) ||

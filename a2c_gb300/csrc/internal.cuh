@@ -189,7 +189,13 @@ a2c_status check_status_word(a2c_gpp_ctx *c);
 a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X);
 // skin path (positions in c->d_X; h_X may be null): rebuild the extended
 // lists if needed, then re-filter at rc
-a2c_status update_neighbors_device(a2c_gpp_ctx *c, const double *h_X, int *rebuilt);
+a2c_status update_neighbors_device(a2c_gpp_ctx *c, const double *h_X, int *rebuilt, int moved);
+// The skin path's new positions X (host memory; mX its device-visible view
+// when pinned, else null), checked on the device -- A2C_ERR_NONFINITE,
+// A2C_ERR_INVALID for a periodic coordinate outside [-L/2, 3L/2], d_X then
+// unchanged -- and moved into d_X; moved = 1 when a site moved more than
+// half the skin since the extended lists were built.
+a2c_status stage_positions(a2c_gpp_ctx *c, const double *X, const double *mX, int *moved);
 
 // The span guard of the mixed form: per direction, how far a site may move
 // from the position the lists were built at before a listed pair could
@@ -203,8 +209,11 @@ void span_limits(const a2c_gpp_ctx *c, double lim[3], const double **xlist);
 // stage (prep, pass 1, pass 2, reduction) on the context's stream
 // Xcopy: X is the caller's pinned host memory (device-mapped); the prep
 // kernel also copies it to Xcopy and flags non-finite values
+// h_out: pinned host memory (2 doubles) that receives f and the status word
+// (an int in the second; the device word is cleared), written by the last
+// kernel where it finishes the objective, else copied
 a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev = nullptr,
-                      double *Xcopy = nullptr);
+                      double *Xcopy = nullptr, double *h_out = nullptr);
 void mixed_free(a2c_gpp_ctx *c);
 a2c_status mixed_set_threads_per_site(a2c_gpp_ctx *c, int tps);
 int mixed_threads_per_site(a2c_gpp_ctx *c);

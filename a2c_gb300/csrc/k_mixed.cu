@@ -68,6 +68,8 @@ struct Mixed {
   int *npre = nullptr;
   float4 *recv = nullptr;
   double *Gown = nullptr;  // 4 per site: the owner's share of the gradient (k_grad_once)
+  void *fpart = nullptr;     // the objective's block sums: one ObjSum per block of k_objective
+  unsigned *fcount = nullptr;
   int64_t sym_entries = 0, sym_sites = 0;  // capacities
   uint64_t sym_version = ~0ull;            // list version the index was built for
   bool sym_ok = false;
@@ -105,6 +107,7 @@ struct ExpTerms {
   float fK, fC, fdC;
   MorseExp pdh, hh;
 };
+struct ObjSum;
 struct MixArgs {
   int64_t N;
   int nPd;
@@ -126,6 +129,15 @@ struct MixArgs {
   const int *npre;
   float4 *recv;
   double *Gown;
+  // A single system's objective (k_objective): per block its sums, the
+  // count of blocks done, f and its two sums.
+  ObjSum *fpart;
+  unsigned *fcount;
+  double *f, *fsums;
+  // host-pointer calls: pinned memory that receives f and the status word
+  // (then cleared), null otherwise
+  double *hout;
+  int *status;
 };
 
 __device__ __forceinline__ float ex2(float x) {
@@ -267,6 +279,17 @@ __device__ __forceinline__ void walk_neighbors(const MixArgs &a, int64_t begin, 
   }
 }
 
+// The per-site finish of pass 1: rho = W * (sum of the density terms), then
+// F'(rho) and F(rho) from the embedding table of the site's species.
+__device__ __forceinline__ void rho_finish(const MixArgs &a, int64_t s, bool iPd, float tot) {
+  const float rho = tot * a.W;
+  float x = fminf(fmaxf(rho * (float)kEmbInvH, 0.0f), (float)kEmbN - 0.5f);
+  const int i = (int)x;
+  const float tt = x - (float)i;
+  const float4 c = __ldg(&a.tabEmb[(iPd ? 0 : kEmbN) + i]);
+  a.FF[s] = make_float2(hd(c, tt) * (float)kEmbInvH, hv(c, tt));
+}
+
 // ---------------------------------------------------------------- pass 1
 // The f_Pd table in shared memory as 8 interleaved copies: interval i of
 // copy c is float4 number 8 i + c, in bank group c.  A 128-bit shared load
@@ -288,7 +311,7 @@ constexpr size_t kRhoSmem = sizeof(float4) * kRhoTabN * kRhoCopies;  // 98,304 B
 #define A2C_GRAD_COPIES 1
 #endif
 constexpr int kGradCopies = A2C_GRAD_COPIES;
-constexpr int kGradTabN = kGradCopies > 1 ? kRhoTabN : kTabN;
+constexpr int kGradTabN = kTabN;  // phi_Pd is -3e-4 eV at 5.8 A: every interval
 constexpr size_t kGradSmem = 2 * sizeof(float4) * kGradTabN * kGradCopies;
 
 template <int TPS, bool LIST, int BLOCK>
@@ -352,15 +375,7 @@ __global__ void __launch_bounds__(BLOCK, rho_min_blocks<BLOCK>()) k_rho_mixed(Mi
   float tot = acc;
 #pragma unroll
   for (int o = TPS / 2; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-  if (live && lane == 0) {
-    const float rho = tot * a.W;
-    const bool iPd = R.iPd;
-    float x = fminf(fmaxf(rho * (float)kEmbInvH, 0.0f), (float)kEmbN - 0.5f);
-    const int i = (int)x;
-    const float tt = x - (float)i;
-    const float4 c = __ldg(&a.tabEmb[(iPd ? 0 : kEmbN) + i]);
-    a.FF[s] = make_float2(hd(c, tt) * (float)kEmbInvH, hv(c, tt));
-  }
+  if (live && lane == 0) rho_finish(a, s, R.iPd, tot);
   }
 }
 
@@ -459,6 +474,145 @@ __device__ __forceinline__ void add_pair(SiteAcc &A, const PairAcc &p, float3 D,
   A.s[2] = fmaf(wx, fmaf(D.z, p.csum, p.e[2]), A.s[2]);
   A.s[3] = fmaf(wx, p.sig, A.s[3]);
   kahan(A.s[4], A.c[4], vx * p.v);
+}
+
+// The objective of a single system, f = (1/T) sum_i V_i - 3 kB sum_i x_i
+// ln sigma_i (minimizer.cpp:353), in one launch: every block sums a
+// stride of the per-site terms and the last block to finish adds the block
+// sums (15 us at 262,144 sites on a GB300, where the two-kernel FP64
+// reduction the plain form keeps took 18 us; appended to k_grad_once the
+// same tail cost its main loop 8%, to k_grad_recv 25 us).  The sums do not
+// depend on the order of their terms, so neither the tile, the grid nor
+// the order in which blocks finish changes a bit: every term is added as a
+// 64.64 fixed-point number (a signed 128-bit integer in units of 2^-64,
+// exact integer adds; a term's bits below 2^-64 are dropped, some 1e-19
+// eV); terms of magnitude 2^40 or more or not finite go to plain double
+// sums that then decide f (a state no minimization reaches; their order
+// follows the blocks').  The last block resets the counter for the next
+// launch and, for a host-pointer call, writes f and the status word to
+// pinned memory.
+struct Fix {
+  unsigned long long lo;
+  long long hi;
+};
+__device__ __forceinline__ Fix fix_add(Fix a, Fix b) {
+  Fix r;
+  r.lo = a.lo + b.lo;
+  r.hi = a.hi + b.hi + (r.lo < a.lo ? 1 : 0);
+  return r;
+}
+// A double of magnitude below 2^40 (biased exponent e < 1063) as 64.64
+// fixed point, its magnitude truncated to a multiple of 2^-64, from its bits
+// with integer operations only (GB300's FP64 pipe is narrow): v = m
+// 2^(e - 1075) with the 53-bit significand m, i.e. m 2^(e - 1011) units.
+__device__ __forceinline__ Fix fix_of_bits(unsigned long long b, int e) {
+  if (e == 0) return Fix{0ull, 0ll};  // zero or subnormal: below one unit
+  const unsigned long long m = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+  const int sh = e - 1011;  // below 52 for e < 1063
+  unsigned long long lo, hi;
+  if (sh >= 0) {
+    lo = m << sh;
+    hi = sh ? m >> (64 - sh) : 0ull;
+  } else {
+    lo = sh > -64 ? m >> -sh : 0ull;
+    hi = 0ull;
+  }
+  if (b >> 63) {  // two's complement of the 128-bit magnitude
+    lo = ~lo + 1ull;
+    hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+  }
+  return Fix{lo, (long long)hi};
+}
+__device__ __forceinline__ double fix_value(Fix a) { return (double)a.hi + (double)a.lo * 5.421010862427522e-20; }
+struct ObjSum {
+  Fix v, s;       // sum V, sum x ln sigma
+  double bv, bs;  // their terms left out of the fixed-point sums
+};
+__device__ __forceinline__ void obj_term(ObjSum &o, double v, bool second) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ffu);
+  if (e < 1063) {  // |v| < 2^40 (2^23 such terms still fit); not NaN or infinite
+    const Fix f = fix_of_bits(b, e);
+    if (second) o.s = fix_add(o.s, f);
+    else o.v = fix_add(o.v, f);
+  } else if (second) {
+    o.bs += v;
+  } else {
+    o.bv += v;
+  }
+}
+__device__ __forceinline__ ObjSum obj_add(ObjSum a, const ObjSum &b) {
+  a.v = fix_add(a.v, b.v);
+  a.s = fix_add(a.s, b.s);
+  a.bv += b.bv;
+  a.bs += b.bs;
+  return a;
+}
+__device__ __forceinline__ ObjSum obj_shfl(const ObjSum &a, int o) {
+  ObjSum r;
+  r.v.lo = __shfl_xor_sync(0xffffffffu, a.v.lo, o);
+  r.v.hi = __shfl_xor_sync(0xffffffffu, a.v.hi, o);
+  r.s.lo = __shfl_xor_sync(0xffffffffu, a.s.lo, o);
+  r.s.hi = __shfl_xor_sync(0xffffffffu, a.s.hi, o);
+  r.bv = __shfl_xor_sync(0xffffffffu, a.bv, o);
+  r.bs = __shfl_xor_sync(0xffffffffu, a.bs, o);
+  return r;
+}
+// the block's sum, in thread 0
+__device__ __forceinline__ ObjSum obj_block(ObjSum a, ObjSum *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a = obj_add(a, obj_shfl(a, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = a;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) a = obj_add(a, sh[k]);
+  __syncthreads();
+  return a;
+}
+
+__global__ void __launch_bounds__(kBlock) k_objective(MixArgs a) {
+  __shared__ ObjSum sh[32];
+  __shared__ bool last;
+  ObjSum o{};
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < a.N; s += (int64_t)gridDim.x * blockDim.x) {
+    obj_term(o, a.Vs[s], false);
+    obj_term(o, a.Ss[s], true);
+  }
+  o = obj_block(o, sh);
+  if (threadIdx.x == 0) {
+    a.fpart[blockIdx.x] = o;
+    __threadfence();
+    last = atomicAdd(a.fcount, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  ObjSum t{};
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+    const volatile ObjSum *q = a.fpart + i;
+    ObjSum b;
+    b.v.lo = q->v.lo;
+    b.v.hi = q->v.hi;
+    b.s.lo = q->s.lo;
+    b.s.hi = q->s.hi;
+    b.bv = q->bv;
+    b.bs = q->bs;
+    t = obj_add(t, b);
+  }
+  t = obj_block(t, sh);
+  if (threadIdx.x == 0) {
+    const double sa = fix_value(t.v) + t.bv, sb = fix_value(t.s) + t.bs;
+    const double f = 1.0 / a.T * sa - 3.0 * kB * sb;
+    *a.f = f;
+    a.fsums[0] = sa;
+    a.fsums[1] = sb;
+    *a.fcount = 0u;
+    if (a.hout) {  // every other kernel of the evaluation has finished: its status bits are in
+      a.hout[0] = f;
+      *reinterpret_cast<int *>(a.hout + 1) = atomicExch(a.status, 0);
+    }
+  }
 }
 
 template <int TPS, bool LIST, int BLOCK>
@@ -758,25 +912,33 @@ __global__ void __launch_bounds__(kBlock) k_chem_mixed(MixArgs a, int nH, double
 // per site the count of neighbors with a smaller id (npre), per owned entry
 // the slot of the reverse entry (rev).  Sets *bad when a list is not
 // strictly increasing, holds the site itself or an id out of range, or
-// lacks the reverse of an entry (asymmetric lists).
+// lacks the reverse of an entry (asymmetric lists).  kSymLanes lanes per
+// site share its entries, so the reverse searches (a chain of dependent
+// loads each) of one site run side by side.
+constexpr int kSymLanes = 8;
 __global__ void k_sym_index(int64_t N, const int64_t *off, const uint32_t *nbr, uint32_t *rev, int *npre, int *bad) {
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < N; s += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = (int)(threadIdx.x % kSymLanes);
+  const unsigned group = 0xffu << ((threadIdx.x % 32) & ~(kSymLanes - 1));  // this site's lanes in the warp
+  const int64_t stride = (int64_t)gridDim.x * (blockDim.x / kSymLanes);
+  for (int64_t s = (int64_t)blockIdx.x * (blockDim.x / kSymLanes) + threadIdx.x / kSymLanes; s < N; s += stride) {
     const int64_t b = off[s], e = off[s + 1];
-    int64_t p = b;
+    int below = 0;  // entries with an id below s: the owned head of a sorted list
     bool ok = true;
-    uint32_t prev = 0;
-    for (int64_t t = b; t < e; ++t) {
+    for (int64_t t = b + lane; t < e; t += kSymLanes) {
       const uint32_t id = nbr[t] & kIdMask;
-      if ((t > b && id <= prev) || (int64_t)id == s || (int64_t)id >= N) ok = false;
-      prev = id;
-      if ((int64_t)id < s) p = t + 1;
+      if ((t > b && id <= (nbr[t - 1] & kIdMask)) || (int64_t)id == s || (int64_t)id >= N) ok = false;
+      below += (int64_t)id < s;
     }
-    npre[s] = (int)(p - b);
+#pragma unroll
+    for (int o = kSymLanes / 2; o > 0; o >>= 1) below += __shfl_xor_sync(group, below, o);
+    ok = __all_sync(group, ok);
+    const int64_t p = b + below;
+    if (lane == 0) npre[s] = below;
     if (!ok) {
-      atomicOr(bad, 1);
+      if (lane == 0) atomicOr(bad, 1);
       continue;
     }
-    for (int64_t t = b; t < p; ++t) {
+    for (int64_t t = b + lane; t < p; t += kSymLanes) {
       const int64_t j = nbr[t] & kIdMask;
       int64_t lo = off[j], hi = off[j + 1];
       while (lo < hi) {  // first entry of j's list with id >= s
@@ -904,8 +1066,16 @@ const ExpTerms &exp_consts() {
 }
 
 // once = true: pass 2 evaluates every pair once (k_grad_once + k_grad_recv;
-// a.rev, a.npre, a.recv set), else from both sides (k_grad_mixed).
+// a.rev, a.npre, a.recv set), else from both sides (k_grad_mixed).  Pass 1
+// evaluates its pairs from both sides: a pairs-once pass 1 (a 4-byte
+// density share per pair, scattered to the neighbor's slot, and a receive
+// kernel) measured slower on a GB300 at 262,144 sites (0.184 against 0.139
+// ms at 2 threads per site) -- its share traffic costs more than the
+// arithmetic it saves.
 constexpr int kRecvTps = 8;  // lanes per site summing the received shares
+// k_objective's grid: blocks per SM at most (at 262,144 sites 2 per SM took
+// 12.3 us, 8 per SM 17.9 us: the last-block count is one contended atomic)
+constexpr int kObjBlocksPerSm = 2;
 // Persistent grid size of a kernel at a block size on the current device
 // (resident blocks x SMs), computed once per (kernel, block, device) under
 // a lock, with the dynamic shared-memory limit raised on that device first.
@@ -1023,6 +1193,10 @@ a2c_status ensure_mixed(a2c_gpp_ctx *c) {
       cudaMalloc(&M->tabPair, sizeof(float4) * 3 * kTabN) != cudaSuccess ||
       cudaMalloc(&M->tabEmb, sizeof(float4) * 2 * kEmbN) != cudaSuccess)
     return A2C_ERR_NOMEM;
+  if (cudaMalloc(&M->fpart, sizeof(ObjSum) * kObjBlocksPerSm * device_sms(c->device)) != cudaSuccess ||
+      cudaMalloc(&M->fcount, sizeof(unsigned)) != cudaSuccess)
+    return A2C_ERR_NOMEM;
+  A2C_CUDA(cudaMemsetAsync(M->fcount, 0, sizeof(unsigned), c->stream));
   std::vector<float> pair((size_t)12 * kTabN), embPd, embH;
   pair_tables(pair.data());
   build_embed_table(0, 1.0 / kEmbInvH, kEmbN, embPd);
@@ -1079,7 +1253,7 @@ a2c_status ensure_sym(a2c_gpp_ctx *c) {
   }
   A2C_CUDA(cudaMemsetAsync(M->npre + N, 0, sizeof(int), st));
   const int sms = device_sms(c->device);
-  k_sym_index<<<(unsigned)std::min<int64_t>(grid_for(N, 256), 8 * (int64_t)sms), 256, 0, st>>>(
+  k_sym_index<<<(unsigned)std::min<int64_t>(grid_for(N * kSymLanes, 256), 8 * (int64_t)sms), 256, 0, st>>>(
       N, c->d_off, c->d_nbr, M->rev, M->npre, M->npre + N);
   A2C_CUDA(cudaGetLastError());
   int bad = 1;
@@ -1131,7 +1305,7 @@ void mixed_free(a2c_gpp_ctx *c) {
   Mixed *M = c->mixed;
   if (!M) return;
   for (void *p : {(void *)M->P, (void *)M->occ, (void *)M->FF, (void *)M->tabPair, (void *)M->tabEmb,
-                  (void *)M->rev, (void *)M->npre, (void *)M->recv, (void *)M->Gown})
+                  (void *)M->rev, (void *)M->npre, (void *)M->recv, (void *)M->Gown, (void *)M->fpart, (void *)M->fcount})
     if (p) cudaFree(p);
   delete M;
   c->mixed = nullptr;
@@ -1173,7 +1347,8 @@ a2c_status mixed_set_threads_per_site(a2c_gpp_ctx *c, int tps) {
   return A2C_OK;
 }
 
-a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev, double *Xcopy) {
+a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG, cudaEvent_t *ev, double *Xcopy,
+                      double *h_out) {
   A2C_TRY(ensure_mixed(c));
   Mixed *M = c->mixed;
   const int64_t N = c->N;
@@ -1206,6 +1381,12 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   a.npre = M->npre;
   a.recv = M->recv;
   a.Gown = M->Gown;
+  a.fpart = (ObjSum *)M->fpart;  // k_objective
+  a.fcount = M->fcount;
+  a.f = d_f;
+  a.fsums = c->d_red + 2 * 1024;
+  a.hout = h_out;
+  a.status = c->d_status;
   if (ev) cudaEventRecord(ev[0], c->stream);
   if (N > 0) {
     const SpanArgs sg = span_args(c);
@@ -1221,7 +1402,10 @@ a2c_status mixed_eval(a2c_gpp_ctx *c, const double *dX, double *d_f, double *dG,
   } else if (ev) {
     for (int k2 = 1; k2 < 4; ++k2) cudaEventRecord(ev[k2], c->stream);
   }
-  A2C_TRY(reduce_objective(c, d_f));
+  k_objective<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(grid_for(N, kBlock),
+                                                                  kObjBlocksPerSm * (int64_t)device_sms(c->device))),
+                kBlock, 0, c->stream>>>(a);
+  A2C_CUDA(cudaGetLastError());
   if (ev) cudaEventRecord(ev[4], c->stream);
   return A2C_OK;
 }

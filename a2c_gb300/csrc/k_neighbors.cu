@@ -384,12 +384,104 @@ __global__ void k_max_count(const int64_t *count, int64_t n, int *out) {
   if (s < n) atomicMax(out, (int)count[s]);
 }
 
-// flag = 1 if any site moved more than `lim` from its reference position
-__global__ void k_moved(const double *X, const double *Xref, int64_t n, double lim2, int *flag) {
+// The skin path's position checks, one pass: kPosMoved when a site moved
+// more than sqrt(lim2) from its reference position (Xref, may be null),
+// kPosNonfinite for a coordinate or width that is not finite, kPosOutside
+// for a periodic coordinate outside [-L/2, 3L/2] (the host entry points'
+// checks).  X may be the caller's host memory (pinned: read through the
+// coherent link), copied then to Xout; Xout null checks X in place.
+constexpr int kPosMoved = 1, kPosNonfinite = 2, kPosOutside = 4;
+__global__ void k_check_positions(const double *X, double *Xout, const double *Xref, int64_t n, double lim2,
+                                  double L0, double L1, double L2, int per, int *flags) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const double dx = X[4 * s] - Xref[4 * s], dy = X[4 * s + 1] - Xref[4 * s + 1], dz = X[4 * s + 2] - Xref[4 * s + 2];
-  if (dx * dx + dy * dy + dz * dz > lim2) atomicOr(flag, 1);
+  const double x = X[4 * s], y = X[4 * s + 1], z = X[4 * s + 2], w = X[4 * s + 3];
+  if (Xout) {
+    Xout[4 * s] = x;
+    Xout[4 * s + 1] = y;
+    Xout[4 * s + 2] = z;
+    Xout[4 * s + 3] = w;
+  }
+  int f = 0;
+  if (!isfinite(x) || !isfinite(y) || !isfinite(z) || !isfinite(w)) f |= kPosNonfinite;
+  if (((per & 1) && (x < -0.5 * L0 || x > 1.5 * L0)) || ((per & 2) && (y < -0.5 * L1 || y > 1.5 * L1)) ||
+      ((per & 4) && (z < -0.5 * L2 || z > 1.5 * L2)))
+    f |= kPosOutside;
+  if (Xref) {
+    const double dx = x - Xref[4 * s], dy = y - Xref[4 * s + 1], dz = z - Xref[4 * s + 2];
+    if (dx * dx + dy * dy + dz * dz > lim2) f |= kPosMoved;
+  }
+  if (f) atomicOr(flags, f);
+}
+
+// Skin refilter, one exact pass over the extended lists: site i's
+// neighbors at rc go to tmp[ext_off[i] ...] in the extended list's order --
+// its Pd part, then its H part, each sorted by id, the order k_nbr_fill
+// gives -- with the counts of k_nbr_count.
+__global__ void __launch_bounds__(kBlock) k_refilter(GridArgs g, ExtSrc src, uint32_t *tmp, int64_t *count, int *npd,
+                                                     int64_t *hh1count, int *shell) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.N) return;
+  const int64_t w = src.off[i];
+  int64_t n = 0, nP = 0, n1 = 0;
+  int sh[3] = {0, 0, 0};
+  const bool iPd = i < g.nPd;
+  const float4 fi = g.Xf[i];
+  const float lim = prefilter_lim(g);
+  src.each(g, i, [&](int64_t j) {
+    uint32_t e;
+    double d2;
+    if (!pair_test(g, i, fi, lim, j, e, d2)) return;
+    tmp[w + n] = e;
+    ++n;
+    if (j < g.nPd) {
+      ++nP;
+      if (iPd) {  // minimizer.cpp:935-947
+        if (d2 < g.A75) ++sh[0];
+        else if (d2 > g.A75 && d2 < g.A125) ++sh[1];
+        else ++sh[2];
+      }
+    } else if (!iPd && d2 < g.A75) {  // minimizer.cpp:999-1004
+      ++n1;
+    }
+  });
+  count[i] = n;
+  npd[i] = (int)nP;
+  if (iPd) {
+    shell[3 * i] = sh[0];
+    shell[3 * i + 1] = sh[1];
+    shell[3 * i + 2] = sh[2];
+  } else {
+    hh1count[i - g.nPd] = n1;
+  }
+}
+
+// The re-filtered lists packed at their offsets, and each H site's first H
+// shell (k_nbr_fill's second part).
+__global__ void __launch_bounds__(kBlock) k_refilter_pack(GridArgs g, const int64_t *ext_off, const uint32_t *tmp,
+                                                          const int64_t *off, uint32_t *nbr, const int64_t *hh1_off,
+                                                          int *hh1, int *status) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.N) return;
+  const int64_t b = off[i], n = off[i + 1] - b;
+  const uint32_t *src = tmp + ext_off[i];
+  for (int64_t t = 0; t < n; ++t) nbr[b + t] = src[t];
+  if (i < g.nPd) return;
+  const int64_t h = i - g.nPd;
+  const float4 fi = g.Xf[i];
+  const float lim = prefilter_lim(g);
+  int64_t w1 = hh1_off[h];
+  for (int64_t t = 0; t < n; ++t) {
+    const int64_t j = src[t] & kIdMask;
+    if (j < g.nPd) continue;
+    uint32_t en;
+    double d2;
+    if (pair_test(g, i, fi, lim, j, en, d2) && d2 < g.A75) {
+      if (w1 < hh1_off[h + 1]) hh1[w1] = (int)(j - g.nPd);
+      ++w1;
+    }
+  }
+  if (w1 != hh1_off[h + 1]) atomicOr(status, kStatusBadIndex);
 }
 
 template <class T>
@@ -591,7 +683,103 @@ a2c_status lists_from_cells(a2c_gpp_ctx *c, const double *h_X, double cut, bool 
   return make_lists(c, g, CellSrc{(const int64_t *)cstart.p, (const int *)items.p}, ext);
 }
 
+// The lists at rc from the extended lists (the skin path): the same lists,
+// shells and first H shells as make_lists over ExtSrc, with one exact test
+// per candidate (k_refilter keeps the survivors) where make_lists tests
+// each twice (count, then fill).
+a2c_status refilter_lists(a2c_gpp_ctx *c, const GridArgs &g0) {
+  const int64_t N = c->N;
+  const a2c_gpp_params &p = c->p;
+  cudaStream_t st = c->stream;
+  DevBuf counts(st), hh1c(st), maxc(st), xf(st), qmax(st), tmp(st);
+  GridArgs g = g0;
+  A2C_CUDA(cudaMallocAsync(&xf.p, sizeof(float4) * std::max<int64_t>(N, 1), st));
+  A2C_CUDA(cudaMallocAsync(&qmax.p, sizeof(unsigned), st));
+  A2C_CUDA(cudaMemsetAsync(qmax.p, 0, sizeof(unsigned), st));
+  A2C_CUDA(cudaMallocAsync(&tmp.p, sizeof(uint32_t) * std::max<int64_t>(c->ext_total, 1), st));
+  A2C_CUDA(cudaMallocAsync(&counts.p, sizeof(int64_t) * (N + 1), st));
+  A2C_CUDA(cudaMallocAsync(&hh1c.p, sizeof(int64_t) * (p.nH + 1), st));
+  A2C_CUDA(cudaMallocAsync(&maxc.p, sizeof(int), st));
+  A2C_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int64_t) * (N + 1), st));
+  A2C_CUDA(cudaMemsetAsync(hh1c.p, 0, sizeof(int64_t) * (p.nH + 1), st));
+  A2C_CUDA(cudaMemsetAsync(maxc.p, 0, sizeof(int), st));
+  g.Xf = (const float4 *)xf.p;
+  g.qmax_bits = (const unsigned *)qmax.p;
+  if (N > 0) {
+    k_positions_f32<<<grid_for(N, 256), 256, 0, st>>>(c->d_X, N, (float4 *)xf.p, (unsigned *)qmax.p);
+    k_refilter<<<grid_for(N, kBlock), kBlock, 0, st>>>(g, ExtSrc{c->d_ext_off, c->d_ext_nbr}, (uint32_t *)tmp.p,
+                                                       (int64_t *)counts.p, c->d_npd, (int64_t *)hh1c.p, c->d_shell);
+    k_max_count<<<grid_for(N, 256), 256, 0, st>>>((const int64_t *)counts.p, N, (int *)maxc.p);
+    A2C_CUDA(cudaGetLastError());
+  }
+  A2C_TRY(scan_exclusive((const int64_t *)counts.p, c->d_off, N + 1, st));
+  A2C_TRY(scan_exclusive((const int64_t *)hh1c.p, c->d_hh1_off, (int64_t)p.nH + 1, st));
+  int64_t total = 0, total1 = 0;
+  int maxn = 0, stat = 0;
+  A2C_CUDA(cudaMemcpyAsync(&total, c->d_off + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaMemcpyAsync(&total1, c->d_hh1_off + p.nH, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaMemcpyAsync(&maxn, maxc.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaStreamSynchronize(st));
+  A2C_TRY(grow(&c->d_nbr, &c->nbr_cap, total));
+  A2C_TRY(grow(&c->d_hh1, &c->hh1_cap, total1));
+  c->nbr_total = total;
+  c->hh1_total = total1;
+  c->max_neighbors = maxn;
+  if (N > 0) {
+    k_refilter_pack<<<grid_for(N, kBlock), kBlock, 0, st>>>(g, c->d_ext_off, (const uint32_t *)tmp.p, c->d_off,
+                                                            c->d_nbr, c->d_hh1_off, c->d_hh1, c->d_status);
+    A2C_CUDA(cudaGetLastError());
+  }
+  A2C_CUDA(cudaMemcpyAsync(&stat, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaStreamSynchronize(st));
+  if (stat & kStatusBadIndex) return A2C_ERR_STATE;
+  ++c->nbr_version;
+  for (int d = 0; d < 3; ++d) c->list_reach[d] = p.periodic[d] ? 0.0 : g.rc;
+  if (c->d_xlist && N > 0)
+    A2C_CUDA(cudaMemcpyAsync(c->d_xlist, c->d_X, sizeof(double) * 4 * N, cudaMemcpyDeviceToDevice, st));
+  return A2C_OK;
+}
+
+// The k_check_positions flags for X (device memory, or a device-visible
+// view of host memory when Xout is the device copy to fill).
+a2c_status check_positions(a2c_gpp_ctx *c, const double *X, double *Xout, const double *Xref, int *flags) {
+  const int64_t N = c->N;
+  cudaStream_t st = c->stream;
+  *flags = 0;
+  if (N <= 0) return A2C_OK;
+  int per = 0;
+  for (int d = 0; d < 3; ++d) per |= c->p.periodic[d] ? 1 << d : 0;
+  const double half = 0.5 * c->skin;
+  DevBuf flag(st);
+  A2C_CUDA(cudaMallocAsync(&flag.p, sizeof(int), st));
+  A2C_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
+  k_check_positions<<<grid_for(N, 256), 256, 0, st>>>(X, Xout, Xref, N, half * half, c->p.box[0], c->p.box[1],
+                                                      c->p.box[2], per, (int *)flag.p);
+  A2C_CUDA(cudaGetLastError());
+  A2C_CUDA(cudaMemcpyAsync(flags, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  A2C_CUDA(cudaStreamSynchronize(st));
+  return A2C_OK;
+}
+
 }  // namespace
+
+a2c_status stage_positions(a2c_gpp_ctx *c, const double *X, const double *mX, int *moved) {
+  const int64_t N = c->N;
+  cudaStream_t st = c->stream;
+  *moved = 0;
+  if (N <= 0) return A2C_OK;
+  DevBuf stage(st);
+  A2C_CUDA(cudaMallocAsync(&stage.p, sizeof(double) * 4 * N, st));
+  double *S = (double *)stage.p;
+  if (!mX) A2C_CUDA(cudaMemcpyAsync(S, X, sizeof(double) * 4 * N, cudaMemcpyHostToDevice, st));
+  int f = 0;
+  A2C_TRY(check_positions(c, mX ? mX : S, mX ? S : nullptr, c->has_ext ? c->d_xref : nullptr, &f));
+  if (f & kPosNonfinite) return A2C_ERR_NONFINITE;
+  if (f & kPosOutside) return A2C_ERR_INVALID;
+  A2C_CUDA(cudaMemcpyAsync(c->d_X, S, sizeof(double) * 4 * N, cudaMemcpyDeviceToDevice, st));
+  *moved = (f & kPosMoved) ? 1 : 0;
+  return A2C_OK;
+}
 
 a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X) {
   c->has_ext = false;  // a full build invalidates the extended lists
@@ -601,21 +789,18 @@ a2c_status build_neighbors_device(a2c_gpp_ctx *c, const double *h_X) {
 // Skin path: rebuild the extended lists when a site has moved more than
 // skin/2 since they were built (or none exist), then re-filter at rc.
 // Positions are in c->d_X; h_X (may be null) serves the extended build's
-// free-direction extents, else it is copied from the device.
-a2c_status update_neighbors_device(a2c_gpp_ctx *c, const double *h_X, int *rebuilt) {
+// free-direction extents, else it is copied from the device.  moved: 0 or 1
+// when stage_positions has already checked the positions, -1 to check here.
+a2c_status update_neighbors_device(a2c_gpp_ctx *c, const double *h_X, int *rebuilt, int moved) {
   const int64_t N = c->N;
   cudaStream_t st = c->stream;
   bool need = !c->has_ext;
   if (!need && N > 0) {
-    DevBuf flag(st);
-    int moved = 0;
-    A2C_CUDA(cudaMallocAsync(&flag.p, sizeof(int), st));
-    A2C_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
-    const double half = 0.5 * c->skin;
-    k_moved<<<grid_for(N, 256), 256, 0, st>>>(c->d_X, c->d_xref, N, half * half, (int *)flag.p);
-    A2C_CUDA(cudaGetLastError());
-    A2C_CUDA(cudaMemcpyAsync(&moved, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    A2C_CUDA(cudaStreamSynchronize(st));
+    if (moved < 0) {
+      int f = 0;
+      A2C_TRY(check_positions(c, c->d_X, nullptr, c->d_xref, &f));
+      moved = f & kPosMoved;
+    }
     need = moved != 0;
   }
   if (need) {
@@ -636,7 +821,7 @@ a2c_status update_neighbors_device(a2c_gpp_ctx *c, const double *h_X, int *rebui
   GridArgs g;
   make_grid(c, nullptr, c->p.rc, g);  // only the cutoff and box are read on this path
   A2C_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), st));
-  return make_lists(c, g, ExtSrc{c->d_ext_off, c->d_ext_nbr}, false);
+  return refilter_lists(c, g);
 }
 
 }  // namespace a2c

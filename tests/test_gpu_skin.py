@@ -74,3 +74,47 @@ def test_skin_validation(gpu):
         g.set_neighbor_skin(0.0)  # no skin: an update is a full build
         _, r = g.update_neighbors(X)
         assert r
+
+
+def test_refilter_pinned_positions_and_checks(gpu):
+    """Positions in pinned host memory (read by the device directly) give
+    the lists pageable positions give; non-finite positions and periodic
+    coordinates outside [-L/2, 3L/2] are refused (checked on the device) and
+    leave the lists as they were."""
+    import torch
+
+    from a2c_gb300 import _native as N
+
+    X, xH, _, box, nPd, nH = A.lattice_fcc(5, periodic=(1, 1, 1), pos_std=0.02, sigma=(0.1, 0.1),
+                                           x_center=0.2, x_half=0.05, seed=11)
+    rng = np.random.default_rng(5)
+    Y4 = X.reshape(-1, 4).copy()
+    Y4[:, :3] += rng.uniform(-0.05, 0.05, size=(nPd + nH, 3))
+    Y = Y4.reshape(-1)
+    Yp = torch.empty(Y.size, dtype=torch.float64, pin_memory=True)
+    Yp.copy_(torch.from_numpy(Y))
+    with A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1)) as g, A.Gpp(nPd, nH, box=box, periodic=(1, 1, 1)) as ref:
+        g.set_neighbor_skin(0.6)
+        g.update_neighbors(X)
+        m, r = g.update_neighbors(Yp.numpy())
+        assert not r
+        ref.build_neighbors(Y)
+        assert same(lists(g), lists(ref))
+        before = lists(g)
+        bad = Y.copy()
+        bad[4 * 7 + 3] = np.nan
+        with pytest.raises(A.A2CError) as e:
+            g.update_neighbors(bad)
+        assert e.value.status == N.A2C_ERR_NONFINITE
+        with pytest.raises(A.A2CError) as e:
+            ref.build_neighbors(bad)  # the full build's checks
+        assert e.value.status == N.A2C_ERR_NONFINITE
+        bad = Y.copy()
+        bad[4 * 9 + 1] = 1.6 * box[1]
+        with pytest.raises(A.A2CError) as e:
+            g.update_neighbors(bad)
+        assert e.value.status == N.A2C_ERR_INVALID
+        # the refused calls changed nothing: the last positions still give the same lists
+        m2, r2 = g.update_neighbors(Y)
+        assert not r2 and m2 == m
+        assert same(lists(g), before)
