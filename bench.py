@@ -10,7 +10,8 @@ gradient evaluation (both quadrature passes and the free-entropy reduction)
 at a fixed state; one atom-eval = one site's contribution.
 
 Headline `value`: the mixed-precision form (FP32 pair quadrature,
-compensated per-site sums, FP64 reductions), device-resident inputs, CUDA
+compensated per-site sums, FP64 per-site finish, the objective summed as
+64.64 fixed point), device-resident inputs, CUDA
 events on the evaluator's stream, L2 (129 MB) flushed by writing a 256 MB
 buffer before every step.  Also reported: the FP64 plain form, the errors of
 the mixed form against it, `e2e` through the public host-pointer entry
@@ -863,7 +864,7 @@ def run_ours(args):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * 4 * Ns,
                         "d2h_bytes_per_step": 8 * 4 * Ns + 8},
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-                "gpu_launches": (6 if once else 5) * args.steps,
+                "gpu_launches": (5 if once else 4) * args.steps,  # k_prep, k_rho_mixed, pass 2 (1 or 2), k_objective
                 "fp64_plain": {"value": value_64, "unit": UNIT, "steps": args.fp64_steps,
                                "ms_per_step": dev_time_64 * 1e3 / args.fp64_steps},
                 "mixed_over_fp64": value / value_64,

@@ -49,7 +49,8 @@ enum {
 /* Arithmetic forms of the evaluator. */
 enum {
   A2C_FP64 = 0,  /* plain form: the reference's FP64 arithmetic and order */
-  A2C_MIXED = 1  /* FP32 pair quadrature, FP64 reductions and entropy terms */
+  A2C_MIXED = 1  /* FP32 pair quadrature; FP64 per-site finish and entropy terms; the
+                    objective summed exactly (fixed point), a batch's by an FP64 tree */
 };
 
 /* Neighbor list ids for a2c_gpp_get_neighbors. */
