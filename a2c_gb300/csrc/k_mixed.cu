@@ -1686,10 +1686,21 @@ extern "C" a2c_status a2c_gpp_eval_mixed_noalloc(a2c_gpp_ctx *c, const double *d
   double *pa = (double *)(base + kNaPart), *pb = pa + kNaRedGrid;
   // No region needs clearing: every word a kernel reads was written earlier
   // in this call (P, occupancy, F/F', energy partials, block partials).
+  // Pass 2 evaluates each pair once when the context holds a current
+  // pairs-once index (a mixed-precision context builds it, with its share
+  // buffers, when its lists change); nothing is allocated here.
+  const bool once = N > 0 && c->mixed && use_once(c);
+  if (once) {
+    const Mixed *M = c->mixed;
+    a.rev = M->rev;
+    a.npre = M->npre;
+    a.recv = M->recv;
+    a.Gown = M->Gown;
+  }
   if (N > 0) {
     k_prep<<<grid_for(N, 256), 256, 0, c->stream>>>(dX, c->d_occ, N, k[0], k[1], k[2], (int4 *)(base + kNaP),
                                                      (float *)(base + kNaOcc), span_args(c));
-    launch_tile(a, c->stream, nullptr, false, effective_tile(mixed_tile(c), N, device_sms(c->device)), false);
+    launch_tile(a, c->stream, nullptr, once, effective_tile(mixed_tile(c), N, device_sms(c->device)), false);
   }
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(kNaRedGrid, (N + kNaRedBlock - 1) / kNaRedBlock));
   k_na_partial<<<grid, kNaRedBlock, 0, c->stream>>>(a.Vs, a.Ss, N, pa, pb);

@@ -202,8 +202,10 @@ a2c_status a2c_gpp_eval_device(a2c_gpp_ctx *ctx, const double *dX, double *df, d
  * driver that forbids allocation during recording.  It has no counterpart
  * in the reference.  Inputs dX (4N doubles) and outputs df (1 double), dG
  * (4N doubles) are device pointers; the context supplies the neighbor lists
- * (build them first) and the occupancy; pass 2 visits pairs from both
- * sides.  All scratch lives in one fixed device array of about 5.8 MB that
+ * (build them first) and the occupancy; pass 2 evaluates each pair once
+ * when the context holds a current pairs-once index (a mixed-precision
+ * context builds it, and its share buffers, with its lists), else from
+ * both sides.  All scratch lives in one fixed device array of about 5.8 MB that
  * every GPU loading the library keeps until the process exits, so problems
  * above 131,072 sites are rejected with A2C_ERR_INVALID.  The first call on
  * a device finds the array's address and loads constant tables into it

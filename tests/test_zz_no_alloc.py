@@ -4,9 +4,10 @@ It serves callers that cannot allocate device memory while they evaluate
 (a solver callback inside another framework's memory pool, or recording
 under a driver that forbids allocation); its scratch is a fixed device
 array inside the library.  Checked against the context path
-(a2c_gpp_eval_device in mixed precision) on two calls in a row, within the
-mixed form's tolerances: free entropy 1e-6 relative, gradient 1e-4 in the
-2-norm.  This file is collected last so that a run stopping at the first
+(a2c_gpp_eval_device in mixed precision) on two calls in a row: within the
+mixed form's tolerances (free entropy 1e-6 relative, gradient 1e-4 in the
+2-norm), and, since both run the same pair kernels at the same tile, the
+gradient bit for bit in either pair mode.  This file is collected last so that a run stopping at the first
 failure has already run every other test.
 """
 import ctypes as C
@@ -62,6 +63,19 @@ def test_noalloc_matches_context_path_twice(gpu, size):
             f2, G2 = df2.item(), dG2.cpu().numpy()
             assert abs(f2 - f_ref) <= TOL_F * abs(f_ref)
             assert np.linalg.norm(G2 - G_ref) <= TOL_G * np.linalg.norm(G_ref)
+            # the same pair kernels as the context path (pairs once, same
+            # tile): the same gradient bits; f differs only in how the
+            # per-site terms are summed (FP64 tree here, exact fixed point there)
+            assert np.array_equal(G2, G_ref)
+            assert abs(f2 - f_ref) <= 1e-12 * abs(f_ref)
+        # pairs from both sides: the both-sides pass 2 of the context path
+        g.set_pair_mode("both")
+        g.eval_device(dX.data_ptr(), df.data_ptr(), dG.data_ptr())
+        g.synchronize()
+        G_both = dG.cpu().numpy()
+        assert fn(g.handle, dX.data_ptr(), df2.data_ptr(), dG2.data_ptr()) == N.A2C_OK
+        g.synchronize()
+        assert np.array_equal(dG2.cpu().numpy(), G_both)
 
 
 def test_noalloc_rejects_problems_above_its_fixed_size(gpu):
