@@ -136,13 +136,24 @@ __device__ __forceinline__ uint32_t encode(int64_t j, const int m[3]) {
   return (uint32_t)j | ((uint32_t)((m[0] + 1) + 3 * (m[1] + 1) + 9 * (m[2] + 1)) << kIdBits);
 }
 
+// The shell class of a pair for the Pd shell counts and the first H shell
+// (minimizer.cpp:935-947, 999-1004): 0 below 0.75 a^2, 1 strictly between
+// 0.75 a^2 and 1.25 a^2, 2 otherwise.
+template <class T>
+__device__ __forceinline__ int shell_class(T d2, T A75, T A125) {
+  return d2 < A75 ? 0 : (d2 > A75 && d2 < A125 ? 1 : 2);
+}
+
 // Candidate j of site i.  The FP32 pass rejects everything farther than
-// rc + guard and accepts, with its d^2, every pair whose decisions it
-// settles (fp32_decides: nearly all); the rest take the FP64 test.  lim <= 0
+// rc + guard and accepts every pair whose decisions it settles
+// (fp32_decides: nearly all), its shell class from the FP32 values too (d^2
+// lies at least the guard band away from both thresholds, so the FP32
+// comparisons give the FP64 answers; GB300's FP64 pipe made the widened
+// comparisons the refilter's bound); the rest take the FP64 test.  lim <= 0
 // (the prefilter cannot be used: a periodic box of at most 2 (rc + guard))
 // takes the image from the FP64 division and the FP64 test.
 __device__ __forceinline__ bool pair_test(const GridArgs &g, int64_t i, float4 fi, float lim, int64_t j,
-                                          uint32_t &entry, double &d2) {
+                                          uint32_t &entry, int &cls) {
   int m[3];
   if (i == j) return false;
   if (lim > 0.0f) {
@@ -151,7 +162,7 @@ __device__ __forceinline__ bool pair_test(const GridArgs &g, int64_t i, float4 f
     if (fp32_decides(g, dd, d2f, lim - g.rcf) && m[0] >= -1 && m[0] <= 1 && m[1] >= -1 && m[1] <= 1 && m[2] >= -1 &&
         m[2] <= 1) {
       entry = encode(j, m);
-      d2 = (double)d2f;
+      cls = shell_class(d2f, g.A75f, g.A125f);
       return true;
     }
   } else {
@@ -159,7 +170,10 @@ __device__ __forceinline__ bool pair_test(const GridArgs &g, int64_t i, float4 f
     for (int d = 0; d < 3; ++d)
       m[d] = g.periodic[d] ? -(int)rint((g.X[4 * j + d] - g.X[4 * i + d]) / g.box[d]) : 0;
   }
-  return exact_test(g, i, j, m, entry, d2);
+  double d2;
+  if (!exact_test(g, i, j, m, entry, d2)) return false;
+  cls = shell_class(d2, g.A75, g.A125);
+  return true;
 }
 
 // The prefilter's cutoff for this build, or 0 when it cannot be used.
@@ -284,18 +298,16 @@ __global__ void __launch_bounds__(kBlock) k_nbr_count(GridArgs g, Src src, int64
   const float lim = prefilter_lim(g);
   src.each(g, i, [&](int64_t j) {
     uint32_t e;
-    double d2;
-    if (!pair_test(g, i, fi, lim, j, e, d2)) return;
+    int cls;
+    if (!pair_test(g, i, fi, lim, j, e, cls)) return;
     ++n;
     const bool jPd = j < g.nPd;
     if (jPd) {
       ++nP;
       if (iPd) {  // minimizer.cpp:935-947
-        if (d2 < g.A75) ++sh[0];
-        else if (d2 > g.A75 && d2 < g.A125) ++sh[1];
-        else ++sh[2];
+        ++sh[cls];
       }
-    } else if (!iPd && d2 < g.A75) {  // minimizer.cpp:999-1004
+    } else if (!iPd && cls == 0) {  // minimizer.cpp:999-1004
       ++n1;
     }
   });
@@ -345,8 +357,8 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, Src src, const 
   const float lim = prefilter_lim(g);
   src.each(g, i, [&](int64_t j) {
     uint32_t en;
-    double d2;
-    if (!pair_test(g, i, fi, lim, j, en, d2)) return;
+    int cls;
+    if (!pair_test(g, i, fi, lim, j, en, cls)) return;
     if (j < g.nPd) {
       if (wP < m) nbr[wP] = en;
       ++wP;
@@ -369,8 +381,8 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(GridArgs g, Src src, const 
       const int64_t j = ent & kIdMask;
       if (j < g.nPd) continue;
       uint32_t en;
-      double d2;
-      if (pair_test(g, i, fi, lim, j, en, d2) && d2 < g.A75) {
+      int cls;
+      if (pair_test(g, i, fi, lim, j, en, cls) && cls == 0) {
         if (w1 < hh1_off[h + 1]) hh1[w1] = (int)(j - g.nPd);
         ++w1;
       }
@@ -430,18 +442,16 @@ __global__ void __launch_bounds__(kBlock) k_refilter(GridArgs g, ExtSrc src, uin
   const float lim = prefilter_lim(g);
   src.each(g, i, [&](int64_t j) {
     uint32_t e;
-    double d2;
-    if (!pair_test(g, i, fi, lim, j, e, d2)) return;
+    int cls;
+    if (!pair_test(g, i, fi, lim, j, e, cls)) return;
     tmp[w + n] = e;
     ++n;
     if (j < g.nPd) {
       ++nP;
       if (iPd) {  // minimizer.cpp:935-947
-        if (d2 < g.A75) ++sh[0];
-        else if (d2 > g.A75 && d2 < g.A125) ++sh[1];
-        else ++sh[2];
+        ++sh[cls];
       }
-    } else if (!iPd && d2 < g.A75) {  // minimizer.cpp:999-1004
+    } else if (!iPd && cls == 0) {  // minimizer.cpp:999-1004
       ++n1;
     }
   });
@@ -475,8 +485,8 @@ __global__ void __launch_bounds__(kBlock) k_refilter_pack(GridArgs g, const int6
     const int64_t j = src[t] & kIdMask;
     if (j < g.nPd) continue;
     uint32_t en;
-    double d2;
-    if (pair_test(g, i, fi, lim, j, en, d2) && d2 < g.A75) {
+    int cls;
+    if (pair_test(g, i, fi, lim, j, en, cls) && cls == 0) {
       if (w1 < hh1_off[h + 1]) hh1[w1] = (int)(j - g.nPd);
       ++w1;
     }
